@@ -1,0 +1,188 @@
+/*
+ * ncg.h — C ABI of the GB300 batched convex narrow phase (GJK + EPA).
+ *
+ * Every entry point replaces a per-pair function of ncollide3d 0.33 with a
+ * batched call over N independent pairs (Isometry3, SupportMap, Isometry3,
+ * SupportMap).  Plain pointers and sizes only: no CUDA, torch or C++ types.
+ * Functions named *_batch take DEVICE pointers and are asynchronous on the
+ * given stream (a cudaStream_t passed as void*, NULL = legacy default stream);
+ * functions named *_batch_host take HOST pointers, copy inputs to the device,
+ * run, copy results back and return when the results are in host memory.
+ *
+ * Reference interfaces (paths inside the ncollide repository):
+ *   contact    src/query/contact/contact_support_map_support_map.rs:9-30, 38-88
+ *   distance   src/query/distance/distance_support_map_support_map.rs:8-53
+ *   proximity  src/query/proximity/proximity_support_map_support_map.rs:10-75
+ *   closest    src/query/closest_points/closest_points_support_map_support_map.rs:9-67
+ * The per-pair arithmetic is gjk::closest_points (src/query/algorithms/gjk.rs:76-177)
+ * with VoronoiSimplex (voronoi_simplex3.rs) and EPA (epa3.rs:219-454).
+ */
+#ifndef NCG_H
+#define NCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NCG_ABI_VERSION 1
+
+/* ---- shape kinds: the ncollide3d shapes that implement SupportMap ------- */
+enum ncg_shape_kind {
+    NCG_BALL = 0,        /* src/shape/ball.rs:29-49        p = {radius}                 */
+    NCG_CUBOID = 1,      /* src/shape/cuboid.rs:135-146    p = {hx, hy, hz}             */
+    NCG_CAPSULE = 2,     /* src/shape/capsule.rs:72-84     p = {half_height, radius}    */
+    NCG_CONE = 3,        /* src/shape/cone.rs:45-67        p = {half_height, radius}    */
+    NCG_CYLINDER = 4,    /* src/shape/cylinder.rs:47-63    p = {half_height, radius}    */
+    NCG_CONVEX_HULL = 5  /* src/shape/convex.rs:418-423    points[hull_off .. +hull_n]  */
+};
+
+/* Isometry3<f32>: unit quaternion (i, j, k, w) — nalgebra's coordinate order —
+ * then the translation.  32 bytes so one pose is two 128-bit loads. */
+typedef struct ncg_pose {
+    float q[4];
+    float t[3];
+    float pad;
+} ncg_pose;
+
+/* One shape record, 32 bytes.  Convex hull vertices live in one flat array of
+ * float4 (x, y, z, unused) shared by all hulls; a hull owns the slice
+ * [hull_off, hull_off + hull_n) of it.  The arg-max over that slice is
+ * ncollide's point_cloud_support_point (first maximum wins). */
+typedef struct ncg_shape {
+    uint32_t kind;
+    uint32_t hull_off;
+    uint32_t hull_n;
+    uint32_t pad;
+    float p[4];
+} ncg_shape;
+
+/* query::Contact<f32> (src/query/contact/contact.rs:15-27). */
+typedef struct ncg_contact {
+    float world1[3];
+    float world2[3];
+    float normal[3];
+    float depth;
+} ncg_contact;
+
+/* One batch of pairs.  Pair i is (m1[i], shapes[g1[i]], m2[i], shapes[g2[i]]).
+ * init_dir, when not NULL, holds 3 floats per pair: the unit direction the
+ * *_with_params functions accept as `init_dir` (GJK warm start). */
+typedef struct ncg_batch {
+    const ncg_shape* shapes;
+    const float* hull_points;   /* 4 floats per vertex, 16-byte aligned */
+    uint32_t n_shapes;
+    uint32_t pad0;
+    uint64_t n_hull_points;
+    const ncg_pose* m1;
+    const uint32_t* g1;
+    const ncg_pose* m2;
+    const uint32_t* g2;
+    uint64_t n_pairs;
+    const float* init_dir;
+} ncg_batch;
+
+/* Proximity (src/query/proximity/proximity.rs:4-11), same discriminants. */
+enum ncg_proximity { NCG_INTERSECTING = 0, NCG_WITHIN_MARGIN = 1, NCG_DISJOINT = 2 };
+
+/* ClosestPoints (src/query/closest_points/closest_points.rs:8-15). */
+enum ncg_closest_points { NCG_CP_INTERSECTING = 0, NCG_CP_WITHIN_MARGIN = 1, NCG_CP_DISJOINT = 2 };
+
+/* Per-pair status bits.  The reference panics or silently returns None in
+ * these cases; the batch API never traps and reports them instead. */
+#define NCG_STATUS_OK            0u
+#define NCG_STATUS_GJK_MAX_ITER  (1u << 0) /* gjk.rs:172-175 iteration cap          */
+#define NCG_STATUS_EPA_FAILED    (1u << 1) /* EPA returned None: epa3.rs:278-293,369-372,404,409-413 */
+#define NCG_STATUS_EPA_MAX_ITER  (1u << 2) /* epa3.rs:421-424 iteration cap          */
+#define NCG_STATUS_EPA_CAPACITY  (1u << 3) /* polytope outgrew the device capacity   */
+#define NCG_STATUS_EPA_NO_FACE   (1u << 4) /* reference panics at epa3.rs:325        */
+#define NCG_STATUS_DEGENERATE    (1u << 5) /* reference asserts (point_tetrahedron.rs:295) */
+#define NCG_STATUS_BAD_INPUT     (1u << 6) /* shape index out of range, bad hull slice */
+
+/* Return codes. */
+#define NCG_OK          0
+#define NCG_EINVAL     (-1)  /* bad argument (e.g. margin < 0, NULL required pointer) */
+#define NCG_ECUDA      (-2)  /* a CUDA call failed; ncg_last_error() has the text     */
+#define NCG_ENOMEM     (-3)
+#define NCG_ENOTBUILT  (-4)
+
+/* Tolerance sets.  NCG_TOL_REFERENCE uses the reference's own f32 constants
+ * (eps = f32::EPSILON: gjk eps_tol = 10 eps, eps_rel = sqrt(eps_tol), EPA
+ * termination 100 eps).  NCG_TOL_PRECISE tightens the termination tests so
+ * that results land within 1e-5 relative of the f64 reference. */
+enum ncg_tolerance { NCG_TOL_REFERENCE = 0, NCG_TOL_PRECISE = 1 };
+
+/* Warm-start sources for the first GJK direction. */
+enum ncg_warm_start {
+    NCG_WARM_NONE = 0,      /* reference default: normalize(t2 - t1) (contact/proximity) */
+    NCG_WARM_INIT_DIR = 1,  /* batch->init_dir (the *_with_params init_dir argument)      */
+    NCG_WARM_MLP = 2        /* the context's learned model predicts the direction        */
+};
+
+typedef struct ncg_ctx ncg_ctx;
+
+/* Per-call statistics (host-visible after the call's stream work completes). */
+typedef struct ncg_stats {
+    uint64_t n_pairs;
+    uint64_t n_epa;          /* pairs that went through EPA                   */
+    uint64_t n_epa_overflow; /* pairs re-run with the global-memory polytope  */
+    uint64_t gjk_iters;      /* sum over pairs                                */
+    uint64_t epa_iters;      /* sum over pairs                                */
+    uint32_t kernels_launched;
+    uint32_t pad;
+} ncg_stats;
+
+/* ---- context --------------------------------------------------------------- */
+/* Creates a context on `device`.  The context owns scratch memory (EPA queue,
+ * pair buckets), CUDA graphs and the learned warm-start model. */
+int ncg_ctx_create(ncg_ctx** out, int device);
+int ncg_ctx_destroy(ncg_ctx* ctx);
+int ncg_ctx_set_tolerance(ncg_ctx* ctx, int tolerance);
+int ncg_ctx_set_warm_start(ncg_ctx* ctx, int warm_start);
+int ncg_sync(ncg_ctx* ctx, void* stream);
+int ncg_get_stats(ncg_ctx* ctx, ncg_stats* out);
+const char* ncg_last_error(void);
+int ncg_abi_version(void);
+
+/* ---- batched queries on device memory (asynchronous) ----------------------- */
+
+/* contact_support_map_support_map_with_params for every pair.
+ * out[i] is valid when has_contact[i] == 1.  out_dir (nullable, 3 floats per
+ * pair) receives the direction the reference returns for reuse as the next
+ * init_dir.  iters (nullable) = gjk_iterations | (epa_iterations << 16). */
+int ncg_contact_batch(ncg_ctx* ctx, const ncg_batch* batch, float prediction,
+                      ncg_contact* out, uint8_t* has_contact, float* out_dir,
+                      uint32_t* status, uint32_t* iters, void* stream);
+
+/* distance_support_map_support_map_with_params for every pair. */
+int ncg_distance_batch(ncg_ctx* ctx, const ncg_batch* batch, float* out_dist,
+                       uint32_t* status, uint32_t* iters, void* stream);
+
+/* proximity_support_map_support_map_with_params for every pair.  Returns
+ * NCG_EINVAL when margin < 0 (the reference asserts). out_sep_axis nullable. */
+int ncg_proximity_batch(ncg_ctx* ctx, const ncg_batch* batch, float margin,
+                        uint8_t* out_prox, float* out_sep_axis, uint32_t* status,
+                        uint32_t* iters, void* stream);
+
+/* closest_points_support_map_support_map_with_params for every pair.
+ * out_points: 6 floats per pair (p1, p2), valid when tag == NCG_CP_WITHIN_MARGIN. */
+int ncg_closest_points_batch(ncg_ctx* ctx, const ncg_batch* batch, float prediction,
+                             uint8_t* out_tag, float* out_points, uint32_t* status,
+                             uint32_t* iters, void* stream);
+
+/* ---- the same on host memory (synchronous; copies in and out) -------------- */
+int ncg_contact_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float prediction,
+                           ncg_contact* out, uint8_t* has_contact, float* out_dir,
+                           uint32_t* status);
+int ncg_distance_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float* out_dist,
+                            uint32_t* status);
+int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
+                             uint8_t* out_prox, float* out_sep_axis, uint32_t* status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NCG_H */

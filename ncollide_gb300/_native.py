@@ -1,0 +1,94 @@
+"""ctypes binding of libncg.so (include/ncg.h).
+
+The shared library is built in-tree (ncollide_gb300/_lib/libncg.so) by
+ncollide_gb300.build.  There is no fallback: when the library is missing the
+import of the query API raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB_PATH
+
+NCG_OK, NCG_EINVAL, NCG_ECUDA, NCG_ENOMEM = 0, -1, -2, -3
+TOL_REFERENCE, TOL_PRECISE = 0, 1
+WARM_NONE, WARM_INIT_DIR, WARM_MLP = 0, 1, 2
+
+STATUS_GJK_MAX_ITER = 1 << 0
+STATUS_EPA_FAILED = 1 << 1
+STATUS_EPA_MAX_ITER = 1 << 2
+STATUS_EPA_CAPACITY = 1 << 3
+STATUS_EPA_NO_FACE = 1 << 4
+STATUS_DEGENERATE = 1 << 5
+STATUS_BAD_INPUT = 1 << 6
+
+# Every symbol include/ncg.h declares.
+EXPORTED = [
+    "ncg_ctx_create", "ncg_ctx_destroy", "ncg_ctx_set_tolerance", "ncg_ctx_set_warm_start", "ncg_sync",
+    "ncg_get_stats", "ncg_last_error", "ncg_abi_version", "ncg_contact_batch", "ncg_distance_batch",
+    "ncg_proximity_batch", "ncg_closest_points_batch", "ncg_contact_batch_host", "ncg_distance_batch_host",
+    "ncg_proximity_batch_host",
+]
+
+
+class NcgBatch(ctypes.Structure):
+    _fields_ = [("shapes", ctypes.c_void_p), ("hull_points", ctypes.c_void_p), ("n_shapes", ctypes.c_uint32),
+                ("pad0", ctypes.c_uint32), ("n_hull_points", ctypes.c_uint64), ("m1", ctypes.c_void_p),
+                ("g1", ctypes.c_void_p), ("m2", ctypes.c_void_p), ("g2", ctypes.c_void_p),
+                ("n_pairs", ctypes.c_uint64), ("init_dir", ctypes.c_void_p)]
+
+
+class NcgStats(ctypes.Structure):
+    _fields_ = [("n_pairs", ctypes.c_uint64), ("n_epa", ctypes.c_uint64), ("n_epa_overflow", ctypes.c_uint64),
+                ("gjk_iters", ctypes.c_uint64), ("epa_iters", ctypes.c_uint64),
+                ("kernels_launched", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+
+
+class NcgError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    """Loads libncg.so; builds it first when the sources are newer."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(LIB_PATH):
+        raise NcgError(f"libncg.so is not built ({LIB_PATH}); run ncollide_gb300.build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i32, f32, u32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_uint32
+    P = ctypes.POINTER
+    L.ncg_ctx_create.argtypes = [P(vp), i32]
+    L.ncg_ctx_destroy.argtypes = [vp]
+    L.ncg_ctx_set_tolerance.argtypes = [vp, i32]
+    L.ncg_ctx_set_warm_start.argtypes = [vp, i32]
+    L.ncg_sync.argtypes = [vp, vp]
+    L.ncg_get_stats.argtypes = [vp, P(NcgStats)]
+    L.ncg_last_error.restype = ctypes.c_char_p
+    L.ncg_contact_batch.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp, vp, vp]
+    L.ncg_distance_batch.argtypes = [vp, P(NcgBatch), vp, vp, vp, vp]
+    L.ncg_proximity_batch.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp, vp]
+    L.ncg_closest_points_batch.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp, vp]
+    L.ncg_contact_batch_host.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp]
+    L.ncg_distance_batch_host.argtypes = [vp, P(NcgBatch), vp, vp]
+    L.ncg_proximity_batch_host.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp]
+    for name in EXPORTED:
+        if name != "ncg_last_error":
+            getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def check(rc, what="ncg call"):
+    if rc != NCG_OK:
+        msg = load().ncg_last_error()
+        raise NcgError(f"{what} failed (rc={rc}): {msg.decode() if msg else ''}")
+    return rc

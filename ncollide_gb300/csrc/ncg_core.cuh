@@ -1,0 +1,651 @@
+// ncg_core.cuh — device side of the batched narrow phase: vector math, the
+// support maps, CSO points, the Voronoi simplex and the GJK loop.
+//
+// Arithmetic split: support mapping and CSO points in f32; the simplex
+// sub-solve (segment / triangle / tetrahedron Voronoi projection), GJK's bound
+// tests and the search direction in f64.  The library is compiled with
+// -fmad=false and every expression keeps the reference's evaluation order, so
+// a pair's result is a deterministic function of its inputs (no contraction,
+// IEEE division and square root).
+//
+// Reference (ncollide 0.33): src/shape/support_map.rs:25-28,
+// src/shape/{ball,cuboid,capsule,cone,cylinder}.rs, src/shape/convex.rs:418-423,
+// src/utils/point_cloud_support_point.rs:6-33, src/query/algorithms/cso_point.rs:66-81,
+// src/query/algorithms/voronoi_simplex3.rs:42-280, src/query/point/point_segment.rs:52-91,
+// src/query/point/point_triangle.rs:61-309, src/query/point/point_tetrahedron.rs:35-353,
+// src/query/algorithms/gjk.rs:76-177,367-388.
+#pragma once
+
+#include <cstdint>
+#include <cfloat>
+
+#include "../../include/ncg.h"
+
+#define NCG_DEV __device__ __forceinline__
+
+namespace ncg {
+
+// ------------------------------------------------------------------ vectors
+template <class T> struct vec3 {
+    T x, y, z;
+};
+template <class T> NCG_DEV vec3<T> mk(T x, T y, T z) { return vec3<T>{x, y, z}; }
+template <class T> NCG_DEV vec3<T> operator+(vec3<T> a, vec3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class T> NCG_DEV vec3<T> operator-(vec3<T> a, vec3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class T> NCG_DEV vec3<T> operator-(vec3<T> a) { return {-a.x, -a.y, -a.z}; }
+template <class T> NCG_DEV vec3<T> operator*(vec3<T> a, T s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class T> NCG_DEV vec3<T> operator/(vec3<T> a, T s) { return {a.x / s, a.y / s, a.z / s}; }
+template <class T> NCG_DEV T dot(vec3<T> a, vec3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> NCG_DEV vec3<T> cross(vec3<T> a, vec3<T> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class T> NCG_DEV T norm_sq(vec3<T> a) { return dot(a, a); }
+NCG_DEV float vnorm(vec3<float> a) { return sqrtf(norm_sq(a)); }
+NCG_DEV double vnorm(vec3<double> a) { return sqrt(norm_sq(a)); }
+NCG_DEV vec3<double> to_d(vec3<float> a) { return {(double)a.x, (double)a.y, (double)a.z}; }
+NCG_DEV vec3<float> to_f(vec3<double> a) { return {(float)a.x, (float)a.y, (float)a.z}; }
+template <class T> NCG_DEV vec3<T> zero3() { return {T(0), T(0), T(0)}; }
+
+// Unit::try_new_and_get: None when |v| <= min_norm.
+template <class T> NCG_DEV bool try_normalize(vec3<T> v, T min_norm, vec3<T>& out, T& n) {
+    n = vnorm(v);
+    if (n <= min_norm) return false;
+    out = v / n;
+    return true;
+}
+
+// UnitQuaternion * Vector3: t = 2 (q.v x v); v' = (t*w + q.v x t) + v.
+NCG_DEV vec3<float> qrot(float4 q, vec3<float> v) {
+    vec3<float> qv{q.x, q.y, q.z};
+    vec3<float> t = cross(qv, v) * 2.0f;
+    vec3<float> c = cross(qv, t);
+    return (t * q.w + c) + v;
+}
+NCG_DEV vec3<float> qrot_inv(float4 q, vec3<float> v) { return qrot(make_float4(-q.x, -q.y, -q.z, q.w), v); }
+
+struct Pose {
+    float4 q;
+    vec3<float> t;
+};
+NCG_DEV Pose load_pose(const ncg_pose* p) {
+    const float4* f = reinterpret_cast<const float4*>(p);
+    float4 a = __ldg(f), b = __ldg(f + 1);
+    return Pose{a, {b.x, b.y, b.z}};
+}
+
+struct Shape {
+    uint32_t kind, off, n;
+    float p0, p1, p2;
+};
+
+// Validates and loads a shape record; returns false on a bad index or hull slice.
+NCG_DEV bool load_shape(const ncg_batch& b, uint32_t id, Shape& s) {
+    if (id >= b.n_shapes) return false;
+    const uint4* r = reinterpret_cast<const uint4*>(b.shapes + id);
+    uint4 h = __ldg(r);
+    float4 p = __ldg(reinterpret_cast<const float4*>(r + 1));
+    s.kind = h.x;
+    s.off = h.y;
+    s.n = h.z;
+    s.p0 = p.x;
+    s.p1 = p.y;
+    s.p2 = p.z;
+    if (s.kind > NCG_CONVEX_HULL) return false;
+    if (s.kind == NCG_CONVEX_HULL && (s.n == 0 || (uint64_t)s.off + s.n > b.n_hull_points)) return false;
+    return true;
+}
+
+// ------------------------------------------------------------------ hull scans
+// point_cloud_support_point: arg-max of <p, d>, the first maximum wins.
+struct ThreadScan {
+    const float4* pts;
+    NCG_DEV uint32_t argmax(const Shape& s, vec3<float> d) const {
+        const float4* p = pts + s.off;
+        float4 v = __ldg(p);
+        float best = dot(vec3<float>{v.x, v.y, v.z}, d);
+        uint32_t bi = 0;
+        for (uint32_t i = 1; i < s.n; ++i) {
+            v = __ldg(p + i);
+            float x = dot(vec3<float>{v.x, v.y, v.z}, d);
+            if (x > best) {
+                best = x;
+                bi = i;
+            }
+        }
+        return bi;
+    }
+};
+
+// All 32 lanes of a warp call argmax with the same arguments; lane l scans
+// points l, l+32, ... (one coalesced 128-bit load per lane per step), then a
+// butterfly reduction keeps (larger dot, smaller index) so every lane gets
+// the first maximum, as the serial scan would.
+struct WarpScan {
+    const float4* pts;
+    NCG_DEV uint32_t argmax(const Shape& s, vec3<float> d) const {
+        const unsigned lane = threadIdx.x & 31u;
+        const float4* p = pts + s.off;
+        // Key (dot, index) ordered by larger dot then smaller index; NaN dots
+        // rank as -inf so that every lane pair agrees (a strict total order).
+        float best = -INFINITY;
+        uint32_t bi = 0xffffffffu;
+        for (uint32_t i = lane; i < s.n; i += 32) {
+            float4 v = __ldg(p + i);
+            float x = dot(vec3<float>{v.x, v.y, v.z}, d);
+            x = (x != x) ? -INFINITY : x;
+            if (bi == 0xffffffffu || x > best) {
+                best = x;
+                bi = i;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            bool take = ob > best || (ob == best && oi < bi);
+            if (take) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        return bi;
+    }
+};
+
+// Local support functions.
+template <class Scan> NCG_DEV vec3<float> local_support(const Shape& s, vec3<float> d, const Scan& scan) {
+    switch (s.kind) {
+    case NCG_BALL: {
+        vec3<float> u = d / vnorm(d);
+        return u * s.p0;
+    }
+    case NCG_CUBOID:
+        return {copysignf(s.p0, d.x), copysignf(s.p1, d.y), copysignf(s.p2, d.z)};
+    case NCG_CAPSULE: {
+        vec3<float> u = d / vnorm(d);
+        vec3<float> r{0.0f, copysignf(s.p0, u.y), 0.0f};
+        return r + u * s.p1;
+    }
+    case NCG_CONE: {
+        vec3<float> v{d.x, 0.0f, d.z};
+        float n = vnorm(v);
+        v = v / n;
+        if (n == 0.0f) return {0.0f, copysignf(s.p0, d.y), 0.0f};
+        v = v * s.p1;
+        v.y = -s.p0;
+        if (dot(d, v) < d.y * s.p0) return {0.0f, s.p0, 0.0f};
+        return v;
+    }
+    case NCG_CYLINDER: {
+        vec3<float> v{d.x, 0.0f, d.z};
+        float n = vnorm(v);
+        v = v / n;
+        if (n == 0.0f) v = zero3<float>();
+        else v = v * s.p1;
+        v.y = copysignf(s.p0, d.y);
+        return v;
+    }
+    default: {
+        uint32_t i = scan.argmax(s, d);
+        float4 v = __ldg(scan.pts + s.off + i);
+        return {v.x, v.y, v.z};
+    }
+    }
+}
+
+// World-space support point (Ball overrides the default transform).
+template <class Scan>
+NCG_DEV vec3<float> support_point(const Pose& m, const Shape& s, vec3<float> d, const Scan& scan) {
+    if (s.kind == NCG_BALL) {
+        vec3<float> u = d / vnorm(d);
+        return m.t + u * s.p0;
+    }
+    vec3<float> l = qrot_inv(m.q, d);
+    return qrot(m.q, local_support(s, l, scan)) + m.t;
+}
+
+struct CSO {
+    vec3<float> p, o1, o2;
+};
+
+struct PairGeom {
+    Pose m1, m2;
+    Shape g1, g2;
+};
+
+template <class Scan> NCG_DEV CSO cso_support(const PairGeom& g, vec3<float> d, const Scan& scan) {
+    vec3<float> a = support_point(g.m1, g.g1, d, scan);
+    vec3<float> b = support_point(g.m2, g.g2, -d, scan);
+    return CSO{a - b, a, b};
+}
+
+// ------------------------------------------------------------------ tolerances
+// gjk.rs:26-29, :92; epa3.rs:231-232; utils/triangle.rs:94-101.  Computed on
+// the host in f64 from the chosen epsilon.
+struct Tol {
+    double eps, eps_tol, eps_rel, epa_eps_tol, affine_eps;
+    float init_eps;  // f32::EPSILON: Unit::try_new on the initial direction
+};
+
+// ------------------------------------------------------------------ projections
+enum { LOC_VERTEX = 0, LOC_EDGE = 1, LOC_FACE = 2, LOC_SOLID = 3 };
+struct Loc {
+    int kind, i;
+    double b0, b1, b2;
+};
+
+NCG_DEV vec3<double> proj_segment(vec3<double> a, vec3<double> b, Loc& loc) {
+    vec3<double> p = zero3<double>();
+    vec3<double> ab = b - a, ap = p - a;
+    double ab_ap = dot(ab, ap), sqnab = norm_sq(ab);
+    if (ab_ap <= 0.0) {
+        loc = Loc{LOC_VERTEX, 0, 1.0, 0.0, 0.0};
+        return a;
+    } else if (ab_ap >= sqnab) {
+        loc = Loc{LOC_VERTEX, 1, 1.0, 0.0, 0.0};
+        return b;
+    }
+    double u = ab_ap / sqnab;
+    loc = Loc{LOC_EDGE, 0, 1.0 - u, u, 0.0};
+    return a + ab * u;
+}
+
+NCG_DEV vec3<double> proj_triangle(vec3<double> a, vec3<double> b, vec3<double> c, Loc& loc) {
+    vec3<double> p = zero3<double>();
+    vec3<double> ab = b - a, ac = c - a, ap = p - a;
+    double ab_ap = dot(ab, ap), ac_ap = dot(ac, ap);
+    if (ab_ap <= 0.0 && ac_ap <= 0.0) {
+        loc = Loc{LOC_VERTEX, 0, 1.0, 0.0, 0.0};
+        return a;
+    }
+    vec3<double> bp = p - b;
+    double ab_bp = dot(ab, bp), ac_bp = dot(ac, bp);
+    if (ab_bp >= 0.0 && ac_bp <= ab_bp) {
+        loc = Loc{LOC_VERTEX, 1, 1.0, 0.0, 0.0};
+        return b;
+    }
+    vec3<double> cp = p - c;
+    double ab_cp = dot(ab, cp), ac_cp = dot(ac, cp);
+    if (ac_cp >= 0.0 && ab_cp <= ac_cp) {
+        loc = Loc{LOC_VERTEX, 2, 1.0, 0.0, 0.0};
+        return c;
+    }
+    vec3<double> bc = c - b;
+    vec3<double> n = cross(ab, ac);
+    double vc = dot(n, cross(ab, ap));
+    if (vc < 0.0 && ab_ap >= 0.0 && ab_bp <= 0.0) {
+        double v = ab_ap / norm_sq(ab);
+        loc = Loc{LOC_EDGE, 0, 1.0 - v, v, 0.0};
+        return a + ab * v;
+    }
+    double vb = -dot(n, cross(ac, cp));
+    if (vb < 0.0 && ac_ap >= 0.0 && ac_cp <= 0.0) {
+        double w = ac_ap / norm_sq(ac);
+        loc = Loc{LOC_EDGE, 2, 1.0 - w, w, 0.0};
+        return a + ac * w;
+    }
+    double va = dot(n, cross(bc, bp));
+    if (va < 0.0 && ac_bp - ab_bp >= 0.0 && ab_cp - ac_cp >= 0.0) {
+        double w = dot(bc, bp) / norm_sq(bc);
+        loc = Loc{LOC_EDGE, 1, 1.0 - w, w, 0.0};
+        return b + bc * w;
+    }
+    int cw = dot(n, ap) >= 0.0 ? 0 : 1;
+    if (va + vb + vc != 0.0) {
+        double denom = 1.0 / (va + vb + vc);
+        double v = vb * denom, w = vc * denom;
+        loc = Loc{LOC_FACE, cw, 1.0 - v - w, v, w};
+        return (a + ab * v) + ac * w;
+    }
+    loc = Loc{LOC_SOLID, 0, 0.0, 0.0, 0.0};
+    return p;
+}
+
+struct EdgeTest {
+    double d1, d2;
+    bool hit;
+    double u;
+};
+NCG_DEV EdgeTest tet_edge(vec3<double> nabc, vec3<double> nabd, vec3<double> ap, vec3<double> ab, double ap_ab,
+                          double bp_ab) {
+    EdgeTest r;
+    double ab_ab = ap_ab - bp_ab;
+    vec3<double> x = cross(ap, ab);
+    r.d1 = dot(x, nabc);
+    r.d2 = dot(x, nabd);
+    r.hit = ab_ab != 0.0 && r.d1 >= 0.0 && r.d2 >= 0.0 && ap_ab >= 0.0 && ap_ab <= ab_ab;
+    r.u = r.hit ? ap_ab / ab_ab : 0.0;
+    return r;
+}
+NCG_DEV bool tet_face(vec3<double> a, vec3<double> b, vec3<double> c, vec3<double> ap, vec3<double> bp,
+                      vec3<double> cp, vec3<double> ab, vec3<double> ac, vec3<double> ad, double dabc, double dbca,
+                      double dacb, double eps, vec3<double>& proj, double bc[3], uint32_t& status) {
+    if (dabc < 0.0 && dbca < 0.0 && dacb < 0.0) {
+        vec3<double> n = cross(ab, ac);
+        if (dot(n, ad) * dot(n, ap) < 0.0) {
+            vec3<double> nn;
+            double len;
+            if (!try_normalize(n, eps, nn, len)) return false;
+            double vc = dot(nn, cross(ap, bp));
+            double va = dot(nn, cross(bp, cp));
+            double vb = dot(nn, cross(cp, ap));
+            double denom = va + vb + vc;
+            if (denom == 0.0) status |= NCG_STATUS_DEGENERATE;
+            double inv = 1.0 / denom;
+            bc[0] = va * inv;
+            bc[1] = vb * inv;
+            bc[2] = vc * inv;
+            proj = (a * bc[0] + b * bc[1]) + c * bc[2];
+            return true;
+        }
+    }
+    return false;
+}
+NCG_DEV vec3<double> proj_tetrahedron(vec3<double> a, vec3<double> b, vec3<double> c, vec3<double> d, double eps,
+                                      Loc& loc, uint32_t& status) {
+    vec3<double> p = zero3<double>();
+    vec3<double> ab = b - a, ac = c - a, ad = d - a, ap = p - a;
+    double ap_ab = dot(ap, ab), ap_ac = dot(ap, ac), ap_ad = dot(ap, ad);
+    if (ap_ab <= 0.0 && ap_ac <= 0.0 && ap_ad <= 0.0) {
+        loc = Loc{LOC_VERTEX, 0, 1.0, 0.0, 0.0};
+        return a;
+    }
+    vec3<double> bc = c - b, bd = d - b, bp = p - b;
+    double bp_bc = dot(bp, bc), bp_bd = dot(bp, bd), bp_ab = dot(bp, ab);
+    if (bp_bc <= 0.0 && bp_bd <= 0.0 && bp_ab >= 0.0) {
+        loc = Loc{LOC_VERTEX, 1, 1.0, 0.0, 0.0};
+        return b;
+    }
+    vec3<double> cd = d - c, cp = p - c;
+    double cp_ac = dot(cp, ac), cp_bc = dot(cp, bc), cp_cd = dot(cp, cd);
+    if (cp_cd <= 0.0 && cp_bc >= 0.0 && cp_ac >= 0.0) {
+        loc = Loc{LOC_VERTEX, 2, 1.0, 0.0, 0.0};
+        return c;
+    }
+    vec3<double> dp = p - d;
+    double dp_cd = dot(dp, cd), dp_bd = dot(dp, bd), dp_ad = dot(dp, ad);
+    if (dp_ad >= 0.0 && dp_bd >= 0.0 && dp_cd >= 0.0) {
+        loc = Loc{LOC_VERTEX, 3, 1.0, 0.0, 0.0};
+        return d;
+    }
+    vec3<double> nabc = cross(ab, ac), nabd = cross(ab, ad);
+    EdgeTest e = tet_edge(nabc, nabd, ap, ab, ap_ab, bp_ab);
+    if (e.hit) { loc = Loc{LOC_EDGE, 0, 1.0 - e.u, e.u, 0.0}; return a + ab * e.u; }
+    double dabc = e.d1, dabd = e.d2;
+    vec3<double> nacd = cross(ac, ad);
+    e = tet_edge(nacd, -nabc, ap, ac, ap_ac, cp_ac);
+    if (e.hit) { loc = Loc{LOC_EDGE, 1, 1.0 - e.u, e.u, 0.0}; return a + ac * e.u; }
+    double dacd = e.d1, dacb = e.d2;
+    e = tet_edge(-nabd, -nacd, ap, ad, ap_ad, dp_ad);
+    if (e.hit) { loc = Loc{LOC_EDGE, 2, 1.0 - e.u, e.u, 0.0}; return a + ad * e.u; }
+    double dadb = e.d1, dadc = e.d2;
+    vec3<double> nbcd = cross(bc, bd);
+    e = tet_edge(nabc, nbcd, bp, bc, bp_bc, cp_bc);
+    if (e.hit) { loc = Loc{LOC_EDGE, 3, 1.0 - e.u, e.u, 0.0}; return b + bc * e.u; }
+    double dbca = e.d1, dbcd = e.d2;
+    e = tet_edge(-nbcd, nabd, bp, bd, bp_bd, dp_bd);
+    if (e.hit) { loc = Loc{LOC_EDGE, 4, 1.0 - e.u, e.u, 0.0}; return b + bd * e.u; }
+    double dbdc = e.d1, dbda = e.d2;
+    e = tet_edge(nacd, nbcd, cp, cd, cp_cd, dp_cd);
+    if (e.hit) { loc = Loc{LOC_EDGE, 5, 1.0 - e.u, e.u, 0.0}; return c + cd * e.u; }
+    double dcda = e.d1, dcdb = e.d2;
+
+    vec3<double> pr;
+    double bw[3];
+    if (tet_face(a, b, c, ap, bp, cp, ab, ac, ad, dabc, dbca, dacb, eps, pr, bw, status)) {
+        loc = Loc{LOC_FACE, 0, bw[0], bw[1], bw[2]};
+        return pr;
+    }
+    if (tet_face(a, b, d, ap, bp, dp, ab, ad, ac, dadb, dabd, dbda, eps, pr, bw, status)) {
+        loc = Loc{LOC_FACE, 1, bw[0], bw[1], bw[2]};
+        return pr;
+    }
+    if (tet_face(a, c, d, ap, cp, dp, ac, ad, ab, dacd, dcda, dadc, eps, pr, bw, status)) {
+        loc = Loc{LOC_FACE, 2, bw[0], bw[1], bw[2]};
+        return pr;
+    }
+    if (tet_face(b, c, d, bp, cp, dp, bc, bd, -ab, dbcd, dcdb, dbdc, eps, pr, bw, status)) {
+        loc = Loc{LOC_FACE, 3, bw[0], bw[1], bw[2]};
+        return pr;
+    }
+    loc = Loc{LOC_SOLID, 0, 0.0, 0.0, 0.0};
+    return p;
+}
+
+// ------------------------------------------------------------------ simplex
+struct Simplex {
+    CSO v[4];
+    double proj[3];
+    double prev_proj[3];
+    int prev_v[4];
+    int dim, prev_dim;
+
+    NCG_DEV vec3<double> pt(int i) const { return to_d(v[i].p); }
+    NCG_DEV void swap(int i, int j) {
+        CSO t = v[i];
+        v[i] = v[j];
+        v[j] = t;
+        int k = prev_v[i];
+        prev_v[i] = prev_v[j];
+        prev_v[j] = k;
+    }
+    NCG_DEV void reset(const CSO& c) {
+        dim = 0;
+        prev_dim = 0;
+        v[0] = c;
+        prev_v[0] = 0; prev_v[1] = 1; prev_v[2] = 2; prev_v[3] = 3;
+        proj[0] = proj[1] = proj[2] = 0.0;
+        prev_proj[0] = prev_proj[1] = prev_proj[2] = 0.0;
+    }
+    NCG_DEV bool add_point(const CSO& c, const Tol& tol) {
+        prev_dim = dim;
+        prev_proj[0] = proj[0];
+        prev_proj[1] = proj[1];
+        prev_proj[2] = proj[2];
+        prev_v[0] = 0; prev_v[1] = 1; prev_v[2] = 2; prev_v[3] = 3;
+        vec3<double> ps = to_d(c.p);
+        if (dim == 0) {
+            if (norm_sq(pt(0) - ps) < tol.eps_tol) return false;
+        } else if (dim == 1) {
+            vec3<double> ab = pt(1) - pt(0), ac = ps - pt(0);
+            if (norm_sq(cross(ab, ac)) < tol.eps_tol) return false;
+        } else {
+            vec3<double> ab = pt(1) - pt(0), ac = pt(2) - pt(0), ap = ps - pt(0);
+            vec3<double> cr = cross(ab, ac);
+            vec3<double> n = cr / vnorm(cr);
+            if (fabs(dot(n, ap)) < tol.eps_tol) return false;
+        }
+        dim += 1;
+        v[dim] = c;
+        return true;
+    }
+    NCG_DEV vec3<double> project_origin_and_reduce(const Tol& tol, uint32_t& status) {
+        if (dim == 0) {
+            proj[0] = 1.0;
+            return pt(0);
+        } else if (dim == 1) {
+            Loc loc;
+            vec3<double> r = proj_segment(pt(0), pt(1), loc);
+            if (loc.kind == LOC_VERTEX && loc.i == 0) {
+                proj[0] = 1.0;
+                dim = 0;
+            } else if (loc.kind == LOC_VERTEX) {
+                swap(0, 1);
+                proj[0] = 1.0;
+                dim = 0;
+            } else {
+                proj[0] = loc.b0;
+                proj[1] = loc.b1;
+            }
+            return r;
+        } else if (dim == 2) {
+            Loc loc;
+            vec3<double> r = proj_triangle(pt(0), pt(1), pt(2), loc);
+            if (loc.kind == LOC_VERTEX) {
+                swap(0, loc.i);
+                proj[0] = 1.0;
+                dim = 0;
+            } else if (loc.kind == LOC_EDGE) {
+                if (loc.i == 0) {
+                    proj[0] = loc.b0;
+                    proj[1] = loc.b1;
+                } else if (loc.i == 1) {
+                    swap(0, 2);
+                    proj[0] = loc.b1;
+                    proj[1] = loc.b0;
+                } else {
+                    swap(1, 2);
+                    proj[0] = loc.b0;
+                    proj[1] = loc.b1;
+                }
+                dim = 1;
+            } else if (loc.kind == LOC_FACE) {
+                proj[0] = loc.b0;
+                proj[1] = loc.b1;
+                proj[2] = loc.b2;
+            }
+            return r;
+        }
+        Loc loc;
+        vec3<double> r = proj_tetrahedron(pt(0), pt(1), pt(2), pt(3), tol.eps, loc, status);
+        if (loc.kind == LOC_VERTEX) {
+            swap(0, loc.i);
+            proj[0] = 1.0;
+            dim = 0;
+        } else if (loc.kind == LOC_EDGE) {
+            switch (loc.i) {
+            case 1: swap(1, 2); break;
+            case 2: swap(1, 3); break;
+            case 3: swap(0, 2); break;
+            case 4: swap(0, 3); break;
+            case 5: swap(0, 2); swap(1, 3); break;
+            default: break;
+            }
+            if (loc.i == 3 || loc.i == 4) {
+                proj[0] = loc.b1;
+                proj[1] = loc.b0;
+            } else {
+                proj[0] = loc.b0;
+                proj[1] = loc.b1;
+            }
+            dim = 1;
+        } else if (loc.kind == LOC_FACE) {
+            if (loc.i == 0) {
+                proj[0] = loc.b0; proj[1] = loc.b1; proj[2] = loc.b2;
+            } else if (loc.i == 1) {
+                v[2] = v[3];
+                proj[0] = loc.b0; proj[1] = loc.b1; proj[2] = loc.b2;
+            } else if (loc.i == 2) {
+                v[1] = v[3];
+                proj[0] = loc.b0; proj[1] = loc.b2; proj[2] = loc.b1;
+            } else {
+                v[0] = v[3];
+                proj[0] = loc.b2; proj[1] = loc.b0; proj[2] = loc.b1;
+            }
+            dim = 2;
+        }
+        return r;
+    }
+};
+
+// ------------------------------------------------------------------ GJK
+enum { GJK_INTERSECTION = 0, GJK_CLOSEST_POINTS = 1, GJK_PROXIMITY = 2, GJK_NO_INTERSECTION = 3 };
+struct GjkOut {
+    int kind;
+    vec3<double> p1, p2, dir;
+};
+
+NCG_DEV void gjk_result(const Simplex& s, bool prev, vec3<double>& p1, vec3<double>& p2) {
+    vec3<double> r1 = zero3<double>(), r2 = zero3<double>();
+    if (prev) {
+        for (int i = 0; i < s.prev_dim + 1; ++i) {
+            double c = s.prev_proj[i];
+            const CSO& p = s.v[s.prev_v[i]];
+            r1 = r1 + to_d(p.o1) * c;
+            r2 = r2 + to_d(p.o2) * c;
+        }
+    } else {
+        for (int i = 0; i < s.dim + 1; ++i) {
+            double c = s.proj[i];
+            const CSO& p = s.v[i];
+            r1 = r1 + to_d(p.o1) * c;
+            r2 = r2 + to_d(p.o2) * c;
+        }
+    }
+    p1 = r1;
+    p2 = r2;
+}
+
+// gjk::closest_points.  `iters` counts loop entries (one CSO support each).
+template <class Scan>
+NCG_DEV GjkOut gjk(const PairGeom& g, double max_dist, bool exact, Simplex& s, const Tol& tol, const Scan& scan,
+                   uint32_t& iters, uint32_t& status, int max_iter) {
+    GjkOut r;
+    r.p1 = r.p2 = r.dir = zero3<double>();
+    vec3<double> proj = s.project_origin_and_reduce(tol, status);
+    vec3<double> old_dir, dir;
+    {
+        vec3<double> u;
+        double n;
+        if (try_normalize(proj, 0.0, u, n)) old_dir = -u;
+        else { r.kind = GJK_INTERSECTION; return r; }
+    }
+    double max_bound = DBL_MAX;
+    int niter = 0;
+    for (;;) {
+        iters++;
+        double old_max_bound = max_bound;
+        {
+            vec3<double> u;
+            double n;
+            if (try_normalize(-proj, tol.eps_tol, u, n)) { dir = u; max_bound = n; }
+            else { r.kind = GJK_INTERSECTION; return r; }
+        }
+        if (max_bound >= old_max_bound) {
+            if (exact) { gjk_result(s, true, r.p1, r.p2); r.kind = GJK_CLOSEST_POINTS; }
+            else r.kind = GJK_PROXIMITY;
+            r.dir = old_dir;
+            return r;
+        }
+        CSO c = cso_support(g, to_f(dir), scan);
+        double min_bound = -dot(dir, to_d(c.p));
+        if (min_bound != min_bound) status |= NCG_STATUS_BAD_INPUT;
+        if (min_bound > max_dist) {
+            r.kind = GJK_NO_INTERSECTION; r.dir = dir; return r;
+        } else if (!exact && min_bound > 0.0 && max_bound <= max_dist) {
+            r.kind = GJK_PROXIMITY; r.dir = old_dir; return r;
+        } else if (max_bound - min_bound <= tol.eps_rel * max_bound) {
+            if (exact) { gjk_result(s, false, r.p1, r.p2); r.kind = GJK_CLOSEST_POINTS; }
+            else r.kind = GJK_PROXIMITY;
+            r.dir = dir;
+            return r;
+        }
+        if (!s.add_point(c, tol)) {
+            if (exact) { gjk_result(s, false, r.p1, r.p2); r.kind = GJK_CLOSEST_POINTS; }
+            else r.kind = GJK_PROXIMITY;
+            r.dir = dir;
+            return r;
+        }
+        old_dir = dir;
+        proj = s.project_origin_and_reduce(tol, status);
+        if (s.dim == 3) {
+            if (min_bound >= tol.eps_tol) {
+                if (exact) { gjk_result(s, true, r.p1, r.p2); r.kind = GJK_CLOSEST_POINTS; }
+                else r.kind = GJK_PROXIMITY;
+                r.dir = old_dir;
+                return r;
+            }
+            r.kind = GJK_INTERSECTION;
+            return r;
+        }
+        niter += 1;
+        if (niter == max_iter) {
+            status |= NCG_STATUS_GJK_MAX_ITER;
+            r.kind = GJK_NO_INTERSECTION;
+            r.dir = mk(1.0, 0.0, 0.0);
+            return r;
+        }
+    }
+}
+
+}  // namespace ncg

@@ -1,0 +1,726 @@
+// ncg_kernels.cu — batched GJK/EPA kernels for sm_103a and the C ABI of include/ncg.h.
+//
+// One batch call runs, on one stream and without host synchronisation:
+//   1. classify     1 thread/pair: validates the pair, routes it to the
+//                   analytic list (no ConvexHull) or the hull list.
+//   2. gjk_thread   1 thread/pair over the analytic list (persistent grid).
+//   3. gjk_warp     1 warp/pair over the hull list (dynamic queue); the hull
+//                   arg-max is warp-parallel with coalesced 128-bit loads.
+//   4. epa_shared   contact only: 1 warp per intersecting pair, polytope in
+//                   shared memory (dynamic queue).
+//   5. epa_global   contact only: pairs whose polytope outgrew shared memory,
+//                   re-run with a polytope in a global-memory slab per warp.
+// Pairs are independent; the GJK stage writes its outputs directly or appends
+// the final simplex to the EPA queue.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ncg.h"
+#include "ncg_core.cuh"
+#include "ncg_epa.cuh"
+
+using namespace ncg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+enum QueryKind { Q_CONTACT = 0, Q_DISTANCE = 1, Q_PROXIMITY = 2, Q_CLOSEST = 3 };
+
+struct Outputs {
+    ncg_contact* contact;
+    uint8_t* tag;
+    float* dir;
+    float* value;
+    float* points;
+    uint32_t* status;
+    uint32_t* iters;
+};
+
+struct QueryParams {
+    int query;
+    int use_init_dir;
+    int gjk_max_iter;
+    int epa_max_iter;
+    double param;  // prediction / margin (f64 copy of the f32 argument)
+    Tol tol;
+};
+
+// EPA work item: the pair and GJK's final simplex (dim + 1 CSO points).
+struct __align__(16) EpaItem {
+    uint32_t pair;
+    uint32_t gjk_iters;
+    uint32_t status;
+    int32_t dim;
+    float v[4][9];
+};
+
+struct DevCounters {
+    unsigned long long n_analytic, n_hull, epa_count, ovf_count;
+    unsigned long long hull_next, epa_next, ovf_next;
+    unsigned long long gjk_iters, epa_iters;
+    unsigned long long pad[7];
+};
+
+struct Scratch {
+    uint32_t* analytic;
+    uint32_t* hull;
+    uint32_t* ovf;
+    EpaItem* items;
+    DevCounters* ctr;
+    char* slabs;
+    size_t slab_bytes;
+    int n_slabs;
+};
+
+// Global-memory EPA store capacities (overflow pass).
+constexpr int G_VC = 10240, G_FC = 65535, G_SC = 4096, G_TC = 16384;
+// Shared-memory EPA store capacities (first pass).
+constexpr int S_VC = 64, S_FC = 256, S_SC = 64, S_TC = 128;
+constexpr int EPA_WARPS = 2;  // warps per block in epa_shared
+
+NCG_DEV uint32_t pack_iters(uint32_t g, uint32_t e) { return (g > 0xffffu ? 0xffffu : g) | ((e > 0xffffu ? 0xffffu : e) << 16); }
+
+NCG_DEV void wr3(float* p, vec3<double> v) {
+    p[0] = (float)v.x;
+    p[1] = (float)v.y;
+    p[2] = (float)v.z;
+}
+
+// Writes the outputs of a finished pair (every query except an EPA-bound contact).
+NCG_DEV void write_outputs(const QueryParams& qp, const Outputs& o, uint32_t i, const GjkOut& r,
+                           vec3<float> init_dir, uint32_t status, uint32_t iters) {
+    switch (qp.query) {
+    case Q_CONTACT: {
+        ncg_contact c;
+        memset(&c, 0, sizeof(c));
+        uint8_t tag = 0;
+        if (r.kind == GJK_CLOSEST_POINTS) {
+            tag = 1;
+            wr3(c.world1, r.p1);
+            wr3(c.world2, r.p2);
+            wr3(c.normal, r.dir);
+            c.depth = (float)(-dot(r.dir, r.p2 - r.p1));
+        }
+        o.contact[i] = c;
+        o.tag[i] = tag;
+        if (o.dir) wr3(o.dir + 3 * (size_t)i, r.dir);
+        break;
+    }
+    case Q_DISTANCE:
+        o.value[i] = r.kind == GJK_CLOSEST_POINTS ? (float)vnorm(r.p2 - r.p1) : 0.0f;
+        break;
+    case Q_PROXIMITY: {
+        uint8_t t = r.kind == GJK_INTERSECTION ? NCG_INTERSECTING
+                    : r.kind == GJK_PROXIMITY  ? NCG_WITHIN_MARGIN
+                                               : NCG_DISJOINT;
+        o.tag[i] = t;
+        if (o.dir) {
+            float* d = o.dir + 3 * (size_t)i;
+            if (r.kind == GJK_INTERSECTION) { d[0] = init_dir.x; d[1] = init_dir.y; d[2] = init_dir.z; }
+            else wr3(d, r.dir);
+        }
+        break;
+    }
+    default: {
+        uint8_t t = r.kind == GJK_CLOSEST_POINTS ? NCG_CP_WITHIN_MARGIN
+                    : r.kind == GJK_NO_INTERSECTION ? NCG_CP_DISJOINT
+                                                    : NCG_CP_INTERSECTING;
+        o.tag[i] = t;
+        if (o.points) {
+            float* p = o.points + 6 * (size_t)i;
+            if (t == NCG_CP_WITHIN_MARGIN) { wr3(p, r.p1); wr3(p + 3, r.p2); }
+            else { for (int k = 0; k < 6; ++k) p[k] = 0.0f; }
+        }
+        break;
+    }
+    }
+    o.status[i] = status;
+    if (o.iters) o.iters[i] = iters;
+}
+
+// A pair with an invalid shape index or hull slice: no contact, distance 0,
+// Disjoint, and NCG_STATUS_BAD_INPUT (the reference would index out of bounds).
+NCG_DEV void write_bad(const QueryParams& qp, const Outputs& o, uint32_t i) {
+    GjkOut r;
+    r.kind = GJK_NO_INTERSECTION;
+    r.p1 = r.p2 = r.dir = zero3<double>();
+    write_outputs(qp, o, i, r, zero3<float>(), NCG_STATUS_BAD_INPUT, 0);
+}
+
+// First search direction of each *_with_params wrapper.
+NCG_DEV vec3<float> initial_dir(const QueryParams& qp, const ncg_batch& b, uint32_t i, const PairGeom& g) {
+    vec3<float> d;
+    float n;
+    if (qp.query == Q_CONTACT || qp.query == Q_PROXIMITY) {
+        if (qp.use_init_dir && b.init_dir) {
+            const float* p = b.init_dir + 3 * (size_t)i;
+            return {p[0], p[1], p[2]};
+        }
+        if (try_normalize(g.m2.t - g.m1.t, qp.tol.init_eps, d, n)) return d;
+        return {1.0f, 0.0f, 0.0f};
+    }
+    vec3<float> d0 = g.m1.t - g.m2.t;
+    if (qp.use_init_dir && b.init_dir) {
+        const float* p = b.init_dir + 3 * (size_t)i;
+        d0 = {p[0], p[1], p[2]};
+    }
+    if (try_normalize(d0, qp.tol.init_eps, d, n)) return d;
+    return {1.0f, 0.0f, 0.0f};
+}
+
+// Runs one pair through GJK; writes its outputs or its EPA work item.
+// All lanes of a warp call this with the same pair when Scan is WarpScan.
+template <class Scan>
+NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, uint32_t i,
+                      const Scan& scan, bool writer, unsigned long long& iter_acc) {
+    PairGeom g;
+    load_shape(b, b.g1[i], g.g1);
+    load_shape(b, b.g2[i], g.g2);
+    g.m1 = load_pose(b.m1 + i);
+    g.m2 = load_pose(b.m2 + i);
+    vec3<float> d = initial_dir(qp, b, i, g);
+    Simplex sx;
+    sx.reset(cso_support(g, d, scan));
+    uint32_t iters = 0, status = 0;
+    double max_dist = qp.query == Q_DISTANCE ? DBL_MAX : qp.param;
+    bool exact = qp.query != Q_PROXIMITY;
+    GjkOut r = gjk(g, max_dist, exact, sx, qp.tol, scan, iters, status, qp.gjk_max_iter);
+    iter_acc += iters;
+    if (qp.query == Q_CONTACT && r.kind == GJK_INTERSECTION) {
+        if (writer) {
+            unsigned long long slot = atomicAdd(&s.ctr->epa_count, 1ull);
+            EpaItem& it = s.items[slot];
+            it.pair = i;
+            it.gjk_iters = iters;
+            it.status = status;
+            it.dim = sx.dim;
+            for (int k = 0; k <= sx.dim; ++k) {
+                const CSO& c = sx.v[k];
+                float* w = it.v[k];
+                w[0] = c.p.x; w[1] = c.p.y; w[2] = c.p.z;
+                w[3] = c.o1.x; w[4] = c.o1.y; w[5] = c.o1.z;
+                w[6] = c.o2.x; w[7] = c.o2.y; w[8] = c.o2.z;
+            }
+        }
+        return;
+    }
+    if (writer) write_outputs(qp, o, i, r, d, status, pack_iters(iters, 0));
+}
+
+__global__ void k_classify(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool hull = false, analytic = false;
+    if (i < b.n_pairs) {
+        Shape a, c;
+        bool ok = load_shape(b, b.g1[i], a) && load_shape(b, b.g2[i], c);
+        if (!ok) write_bad(qp, o, (uint32_t)i);
+        else if (a.kind == NCG_CONVEX_HULL || c.kind == NCG_CONVEX_HULL) hull = true;
+        else analytic = true;
+    }
+    // warp-aggregated appends
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned mh = __ballot_sync(0xffffffffu, hull), ma = __ballot_sync(0xffffffffu, analytic);
+    unsigned long long bh = 0, ba = 0;
+    if (lane == 0) {
+        if (mh) bh = atomicAdd(&s.ctr->n_hull, (unsigned long long)__popc(mh));
+        if (ma) ba = atomicAdd(&s.ctr->n_analytic, (unsigned long long)__popc(ma));
+    }
+    bh = __shfl_sync(0xffffffffu, bh, 0);
+    ba = __shfl_sync(0xffffffffu, ba, 0);
+    unsigned below = (1u << lane) - 1u;
+    if (hull) s.hull[bh + __popc(mh & below)] = (uint32_t)i;
+    if (analytic) s.analytic[ba + __popc(ma & below)] = (uint32_t)i;
+}
+
+NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31u) == 0 && v) atomicAdd(dst, v);
+}
+
+__global__ void __launch_bounds__(128) k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->n_analytic;
+    ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
+    unsigned long long acc = 0;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long start = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned long long rounds = (n + stride - 1) / stride;
+    for (unsigned long long r = 0; r < rounds; ++r) {
+        unsigned long long k = start + r * stride;
+        if (k < n) gjk_pair(b, qp, o, s, s.analytic[k], scan, true, acc);
+    }
+    warp_add(&s.ctr->gjk_iters, acc);
+}
+
+__global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->n_hull;
+    WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long acc = 0;
+    for (;;) {
+        unsigned long long k = 0;
+        if (lane == 0) k = atomicAdd(&s.ctr->hull_next, 1ull);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= n) break;
+        unsigned long long a = 0;
+        gjk_pair(b, qp, o, s, s.hull[k], scan, lane == 0, a);
+        if (lane == 0) acc += a;
+    }
+    warp_add(&s.ctr->gjk_iters, acc);
+}
+
+// Writes a contact finished by EPA.
+NCG_DEV void write_epa(const Outputs& o, const EpaItem& it, const EpaResult& r, uint32_t extra_status) {
+    const uint32_t i = it.pair;
+    ncg_contact c;
+    memset(&c, 0, sizeof(c));
+    uint8_t tag = 0;
+    vec3<double> dir = mk(1.0, 0.0, 0.0);
+    if (r.exit >= EPA_OK_DIM0 && r.exit <= EPA_OK_HEAP_EMPTY) {
+        tag = 1;
+        wr3(c.world1, r.p1);
+        wr3(c.world2, r.p2);
+        wr3(c.normal, r.n);
+        c.depth = (float)(-dot(r.n, r.p2 - r.p1));
+        dir = r.n;
+    }
+    o.contact[i] = c;
+    o.tag[i] = tag;
+    if (o.dir) wr3(o.dir + 3 * (size_t)i, dir);
+    o.status[i] = it.status | r.status | extra_status;
+    if (o.iters) o.iters[i] = pack_iters(it.gjk_iters, r.iters);
+}
+
+NCG_DEV PairGeom load_geom(const ncg_batch& b, uint32_t i) {
+    PairGeom g;
+    load_shape(b, b.g1[i], g.g1);
+    load_shape(b, b.g2[i], g.g2);
+    g.m1 = load_pose(b.m1 + i);
+    g.m2 = load_pose(b.m2 + i);
+    return g;
+}
+
+NCG_DEV void load_simplex(const EpaItem& it, CSO* sv) {
+    for (int k = 0; k <= it.dim; ++k) {
+        const float* w = it.v[k];
+        sv[k] = CSO{{w[0], w[1], w[2]}, {w[3], w[4], w[5]}, {w[6], w[7], w[8]}};
+    }
+}
+
+__global__ void __launch_bounds__(EPA_WARPS * 32) k_epa_shared(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+    extern __shared__ __align__(16) char smem[];
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    EpaStore st;
+    const size_t bytes = EpaStore::bytes(S_VC, S_FC, S_SC, S_TC);
+    st.carve(smem + warp * bytes, S_VC, S_FC, S_SC, S_TC);
+    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count;
+    WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
+    unsigned long long acc = 0;
+    for (;;) {
+        unsigned long long k = 0;
+        if (lane == 0) k = atomicAdd(&s.ctr->epa_next, 1ull);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= n) break;
+        const EpaItem& it = s.items[k];
+        PairGeom g = load_geom(b, it.pair);
+        CSO sv[4];
+        load_simplex(it, sv);
+        EpaResult r = epa_warp(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
+        if (r.exit == EPA_OVERFLOW) {
+            if (lane == 0) {
+                unsigned long long q = atomicAdd(&s.ctr->ovf_count, 1ull);
+                s.ovf[q] = (uint32_t)k;
+            }
+        } else {
+            acc += r.iters;
+            if (lane == 0) write_epa(o, it, r, 0);
+        }
+        __syncwarp();
+    }
+    if (lane == 0 && acc) atomicAdd(&s.ctr->epa_iters, acc);
+}
+
+__global__ void __launch_bounds__(128) k_epa_global(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= (unsigned)s.n_slabs) return;
+    EpaStore st;
+    st.carve(s.slabs + (size_t)gw * s.slab_bytes, G_VC, G_FC, G_SC, G_TC);
+    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->ovf_count;
+    WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
+    unsigned long long acc = 0;
+    for (;;) {
+        unsigned long long k = 0;
+        if (lane == 0) k = atomicAdd(&s.ctr->ovf_next, 1ull);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= n) break;
+        const EpaItem& it = s.items[s.ovf[k]];
+        PairGeom g = load_geom(b, it.pair);
+        CSO sv[4];
+        load_simplex(it, sv);
+        EpaResult r = epa_warp(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
+        acc += r.iters;
+        if (lane == 0) {
+            if (r.exit == EPA_OVERFLOW) {
+                EpaResult none = r;
+                none.exit = EPA_NONE;
+                write_epa(o, it, none, NCG_STATUS_EPA_CAPACITY);
+            } else {
+                write_epa(o, it, r, 0);
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0 && acc) atomicAdd(&s.ctr->epa_iters, acc);
+}
+
+// ------------------------------------------------------------------ host side
+bool cuda_ok(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return false;
+}
+
+Tol make_tol(int mode) {
+    Tol t;
+    double e = mode == NCG_TOL_PRECISE ? (double)DBL_EPSILON : (double)FLT_EPSILON;
+    t.eps = e;
+    t.eps_tol = e * 10.0;
+    t.eps_rel = std::sqrt(t.eps_tol);
+    t.epa_eps_tol = mode == NCG_TOL_PRECISE ? 1e-6 : e * 100.0;
+    double a = e * 100.0;
+    t.affine_eps = a * a;
+    t.init_eps = FLT_EPSILON;
+    return t;
+}
+
+}  // namespace
+
+struct ncg_ctx {
+    int device = 0;
+    int num_sms = 0;
+    int tol_mode = NCG_TOL_REFERENCE;
+    int warm = NCG_WARM_NONE;
+    int occ_thread = 1, occ_warp = 1, occ_epa = 1, occ_classify = 1;
+    char* scratch = nullptr;
+    size_t scratch_cap_pairs = 0;
+    char* slabs = nullptr;
+    int n_slabs = 0;
+    size_t slab_bytes = 0;
+    DevCounters* host_ctr = nullptr;  // pinned
+    ncg_stats last{};
+    uint32_t launches = 0;
+    // host-API staging buffers
+    char* stage = nullptr;
+    size_t stage_cap = 0;
+    cudaStream_t own_stream = nullptr;
+};
+
+namespace {
+
+bool ensure_scratch(ncg_ctx* c, uint64_t n) {
+    if (n <= c->scratch_cap_pairs && c->scratch) return true;
+    if (c->scratch) cudaFree(c->scratch);
+    c->scratch = nullptr;
+    uint64_t cap = n < 1024 ? 1024 : n;
+    size_t bytes = 3 * 4 * cap + sizeof(EpaItem) * cap + sizeof(DevCounters) + 1024;
+    if (!cuda_ok(cudaMalloc(&c->scratch, bytes), "cudaMalloc(scratch)")) return false;
+    c->scratch_cap_pairs = cap;
+    return true;
+}
+
+Scratch carve_scratch(ncg_ctx* c) {
+    Scratch s;
+    uint64_t cap = c->scratch_cap_pairs;
+    char* p = c->scratch;
+    s.ctr = (DevCounters*)p; p += 256;
+    s.items = (EpaItem*)p; p += sizeof(EpaItem) * cap;
+    s.analytic = (uint32_t*)p; p += 4 * cap;
+    s.hull = (uint32_t*)p; p += 4 * cap;
+    s.ovf = (uint32_t*)p;
+    s.slabs = c->slabs;
+    s.slab_bytes = c->slab_bytes;
+    s.n_slabs = c->n_slabs;
+    return s;
+}
+
+int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outputs& o, cudaStream_t st) {
+    if (!c || !b) { g_last_error = "null context or batch"; return NCG_EINVAL; }
+    if (b->n_pairs == 0) return NCG_OK;
+    if (b->n_pairs > 0xffffffffull) { g_last_error = "more than 2^32-1 pairs"; return NCG_EINVAL; }
+    if (!b->shapes || !b->m1 || !b->m2 || !b->g1 || !b->g2 || !o.status) {
+        g_last_error = "null required pointer";
+        return NCG_EINVAL;
+    }
+    if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    if (!ensure_scratch(c, b->n_pairs)) return NCG_ENOMEM;
+    Scratch s = carve_scratch(c);
+    QueryParams qp;
+    qp.query = query;
+    qp.use_init_dir = (c->warm == NCG_WARM_INIT_DIR && b->init_dir) ? 1 : 0;
+    qp.gjk_max_iter = 10000;
+    qp.epa_max_iter = 10000;
+    qp.param = (double)param;
+    qp.tol = make_tol(c->tol_mode);
+    ncg_batch bb = *b;
+    uint32_t launches = 0;
+    if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset counters")) return NCG_ECUDA;
+    unsigned n = (unsigned)b->n_pairs;
+    k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
+    launches++;
+    k_gjk_thread<<<c->num_sms * c->occ_thread, 128, 0, st>>>(bb, qp, o, s);
+    launches++;
+    k_gjk_warp<<<c->num_sms * c->occ_warp, 128, 0, st>>>(bb, qp, o, s);
+    launches++;
+    if (query == Q_CONTACT) {
+        size_t smem = EPA_WARPS * EpaStore::bytes(S_VC, S_FC, S_SC, S_TC);
+        k_epa_shared<<<c->num_sms * c->occ_epa, EPA_WARPS * 32, smem, st>>>(bb, qp, o, s);
+        launches++;
+        k_epa_global<<<(c->n_slabs * 32 + 127) / 128, 128, 0, st>>>(bb, qp, o, s);
+        launches++;
+    }
+    if (!cuda_ok(cudaGetLastError(), "kernel launch")) return NCG_ECUDA;
+    if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st),
+                 "copy counters"))
+        return NCG_ECUDA;
+    c->launches = launches;
+    c->last.n_pairs = b->n_pairs;
+    return NCG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ncg_abi_version(void) { return NCG_ABI_VERSION; }
+const char* ncg_last_error(void) { return g_last_error.c_str(); }
+
+int ncg_ctx_create(ncg_ctx** out, int device) {
+    if (!out) return NCG_EINVAL;
+    *out = nullptr;
+    int ndev = 0;
+    if (!cuda_ok(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount")) return NCG_ECUDA;
+    if (device < 0 || device >= ndev) { g_last_error = "no such device"; return NCG_EINVAL; }
+    if (!cuda_ok(cudaSetDevice(device), "cudaSetDevice")) return NCG_ECUDA;
+    ncg_ctx* c = new ncg_ctx();
+    c->device = device;
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    size_t smem = EPA_WARPS * EpaStore::bytes(S_VC, S_FC, S_SC, S_TC);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_epa_shared, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_thread, k_gjk_thread, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_warp, k_gjk_warp, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa, k_epa_shared, EPA_WARPS * 32, smem);
+    if (c->occ_thread < 1) c->occ_thread = 1;
+    if (c->occ_warp < 1) c->occ_warp = 1;
+    if (c->occ_epa < 1) c->occ_epa = 1;
+    c->slab_bytes = (EpaStore::bytes(G_VC, G_FC, G_SC, G_TC) + 255) & ~size_t(255);
+    c->n_slabs = c->num_sms;
+    if (!cuda_ok(cudaMalloc(&c->slabs, c->slab_bytes * c->n_slabs), "cudaMalloc(slabs)") ||
+        !cuda_ok(cudaMallocHost(&c->host_ctr, sizeof(DevCounters)), "cudaMallocHost")) {
+        ncg_ctx_destroy(c);
+        return NCG_ENOMEM;
+    }
+    memset(c->host_ctr, 0, sizeof(DevCounters));
+    *out = c;
+    return NCG_OK;
+}
+
+int ncg_ctx_destroy(ncg_ctx* c) {
+    if (!c) return NCG_OK;
+    cudaSetDevice(c->device);
+    if (c->scratch) cudaFree(c->scratch);
+    if (c->slabs) cudaFree(c->slabs);
+    if (c->stage) cudaFree(c->stage);
+    if (c->host_ctr) cudaFreeHost(c->host_ctr);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return NCG_OK;
+}
+
+int ncg_ctx_set_tolerance(ncg_ctx* c, int tol) {
+    if (!c || (tol != NCG_TOL_REFERENCE && tol != NCG_TOL_PRECISE)) return NCG_EINVAL;
+    c->tol_mode = tol;
+    return NCG_OK;
+}
+
+int ncg_ctx_set_warm_start(ncg_ctx* c, int w) {
+    if (!c || w < NCG_WARM_NONE || w > NCG_WARM_INIT_DIR) return NCG_EINVAL;
+    c->warm = w;
+    return NCG_OK;
+}
+
+int ncg_sync(ncg_ctx* c, void* stream) {
+    if (!c) return NCG_EINVAL;
+    if (!cuda_ok(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize")) return NCG_ECUDA;
+    return NCG_OK;
+}
+
+int ncg_get_stats(ncg_ctx* c, ncg_stats* out) {
+    if (!c || !out) return NCG_EINVAL;
+    // host_ctr was filled by an asynchronous copy at the end of the last call;
+    // the caller synchronises the stream before reading the statistics.
+    out->n_pairs = c->last.n_pairs;
+    out->n_epa = c->host_ctr->epa_count;
+    out->n_epa_overflow = c->host_ctr->ovf_count;
+    out->gjk_iters = c->host_ctr->gjk_iters;
+    out->epa_iters = c->host_ctr->epa_iters;
+    out->kernels_launched = c->launches;
+    out->pad = 0;
+    return NCG_OK;
+}
+
+int ncg_contact_batch(ncg_ctx* c, const ncg_batch* b, float prediction, ncg_contact* out, uint8_t* has_contact,
+                      float* out_dir, uint32_t* status, uint32_t* iters, void* stream) {
+    if (c && b && b->n_pairs == 0) return NCG_OK;
+    if (!out || !has_contact) { g_last_error = "null output"; return NCG_EINVAL; }
+    Outputs o{out, has_contact, out_dir, nullptr, nullptr, status, iters};
+    return run_query(c, b, Q_CONTACT, prediction, o, (cudaStream_t)stream);
+}
+
+int ncg_distance_batch(ncg_ctx* c, const ncg_batch* b, float* out_dist, uint32_t* status, uint32_t* iters,
+                       void* stream) {
+    if (c && b && b->n_pairs == 0) return NCG_OK;
+    if (!out_dist) { g_last_error = "null output"; return NCG_EINVAL; }
+    Outputs o{nullptr, nullptr, nullptr, out_dist, nullptr, status, iters};
+    return run_query(c, b, Q_DISTANCE, 0.0f, o, (cudaStream_t)stream);
+}
+
+int ncg_proximity_batch(ncg_ctx* c, const ncg_batch* b, float margin, uint8_t* out_prox, float* out_sep_axis,
+                        uint32_t* status, uint32_t* iters, void* stream) {
+    if (!(margin >= 0.0f)) { g_last_error = "The proximity margin must be positive or zero."; return NCG_EINVAL; }
+    if (c && b && b->n_pairs == 0) return NCG_OK;
+    if (!out_prox) { g_last_error = "null output"; return NCG_EINVAL; }
+    Outputs o{nullptr, out_prox, out_sep_axis, nullptr, nullptr, status, iters};
+    return run_query(c, b, Q_PROXIMITY, margin, o, (cudaStream_t)stream);
+}
+
+int ncg_closest_points_batch(ncg_ctx* c, const ncg_batch* b, float prediction, uint8_t* out_tag, float* out_points,
+                             uint32_t* status, uint32_t* iters, void* stream) {
+    if (c && b && b->n_pairs == 0) return NCG_OK;
+    if (!out_tag) { g_last_error = "null output"; return NCG_EINVAL; }
+    Outputs o{nullptr, out_tag, nullptr, nullptr, out_points, status, iters};
+    return run_query(c, b, Q_CLOSEST, prediction, o, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ host-memory entry points
+namespace {
+
+struct HostRun {
+    ncg_batch dev;
+    char* out;
+};
+
+size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Copies a host batch into the context's staging buffer; returns the device batch
+// and a pointer to `out_bytes` of device output space after the inputs.
+int stage_batch(ncg_ctx* c, const ncg_batch* h, size_t out_bytes, cudaStream_t st, HostRun& hr) {
+    const uint64_t n = h->n_pairs;
+    size_t need = al(sizeof(ncg_shape) * h->n_shapes) + al(16 * h->n_hull_points) + 2 * al(sizeof(ncg_pose) * n) +
+                  2 * al(4 * n) + (h->init_dir ? al(12 * n) : 0) + al(out_bytes);
+    if (need > c->stage_cap) {
+        if (c->stage) cudaFree(c->stage);
+        c->stage = nullptr;
+        if (!cuda_ok(cudaMalloc(&c->stage, need), "cudaMalloc(stage)")) return NCG_ENOMEM;
+        c->stage_cap = need;
+    }
+    char* p = c->stage;
+    ncg_batch d = *h;
+    auto put = [&](const void* src, size_t bytes) -> char* {
+        char* dst = p;
+        if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+        p += al(bytes);
+        return dst;
+    };
+    d.shapes = (const ncg_shape*)put(h->shapes, sizeof(ncg_shape) * h->n_shapes);
+    d.hull_points = (const float*)put(h->hull_points, 16 * h->n_hull_points);
+    d.m1 = (const ncg_pose*)put(h->m1, sizeof(ncg_pose) * n);
+    d.m2 = (const ncg_pose*)put(h->m2, sizeof(ncg_pose) * n);
+    d.g1 = (const uint32_t*)put(h->g1, 4 * n);
+    d.g2 = (const uint32_t*)put(h->g2, 4 * n);
+    d.init_dir = h->init_dir ? (const float*)put(h->init_dir, 12 * n) : nullptr;
+    hr.dev = d;
+    hr.out = p;
+    return cuda_ok(cudaGetLastError(), "stage copies") ? NCG_OK : NCG_ECUDA;
+}
+
+cudaStream_t host_stream(ncg_ctx* c) {
+    if (!c->own_stream) cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    return c->own_stream;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ncg_contact_batch_host(ncg_ctx* c, const ncg_batch* b, float prediction, ncg_contact* out, uint8_t* has_contact,
+                           float* out_dir, uint32_t* status) {
+    if (!c || !b || !out || !has_contact || !status) return NCG_EINVAL;
+    cudaSetDevice(c->device);
+    cudaStream_t st = host_stream(c);
+    const uint64_t n = b->n_pairs;
+    size_t ob = al(40 * n) + al(n) + al(12 * n) + al(4 * n);
+    HostRun hr;
+    int rc = stage_batch(c, b, ob, st, hr);
+    if (rc) return rc;
+    ncg_contact* dc = (ncg_contact*)hr.out;
+    uint8_t* dt = (uint8_t*)(hr.out + al(40 * n));
+    float* dd = (float*)(hr.out + al(40 * n) + al(n));
+    uint32_t* ds = (uint32_t*)(hr.out + al(40 * n) + al(n) + al(12 * n));
+    rc = ncg_contact_batch(c, &hr.dev, prediction, dc, dt, out_dir ? dd : nullptr, ds, nullptr, st);
+    if (rc) return rc;
+    cudaMemcpyAsync(out, dc, 40 * n, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(has_contact, dt, n, cudaMemcpyDeviceToHost, st);
+    if (out_dir) cudaMemcpyAsync(out_dir, dd, 12 * n, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(status, ds, 4 * n, cudaMemcpyDeviceToHost, st);
+    return cuda_ok(cudaStreamSynchronize(st), "contact_batch_host") ? NCG_OK : NCG_ECUDA;
+}
+
+int ncg_distance_batch_host(ncg_ctx* c, const ncg_batch* b, float* out_dist, uint32_t* status) {
+    if (!c || !b || !out_dist || !status) return NCG_EINVAL;
+    cudaSetDevice(c->device);
+    cudaStream_t st = host_stream(c);
+    const uint64_t n = b->n_pairs;
+    HostRun hr;
+    int rc = stage_batch(c, b, al(4 * n) + al(4 * n), st, hr);
+    if (rc) return rc;
+    float* dd = (float*)hr.out;
+    uint32_t* ds = (uint32_t*)(hr.out + al(4 * n));
+    rc = ncg_distance_batch(c, &hr.dev, dd, ds, nullptr, st);
+    if (rc) return rc;
+    cudaMemcpyAsync(out_dist, dd, 4 * n, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(status, ds, 4 * n, cudaMemcpyDeviceToHost, st);
+    return cuda_ok(cudaStreamSynchronize(st), "distance_batch_host") ? NCG_OK : NCG_ECUDA;
+}
+
+int ncg_proximity_batch_host(ncg_ctx* c, const ncg_batch* b, float margin, uint8_t* out_prox, float* out_sep_axis,
+                             uint32_t* status) {
+    if (!c || !b || !out_prox || !status) return NCG_EINVAL;
+    if (!(margin >= 0.0f)) { g_last_error = "The proximity margin must be positive or zero."; return NCG_EINVAL; }
+    cudaSetDevice(c->device);
+    cudaStream_t st = host_stream(c);
+    const uint64_t n = b->n_pairs;
+    HostRun hr;
+    int rc = stage_batch(c, b, al(n) + al(12 * n) + al(4 * n), st, hr);
+    if (rc) return rc;
+    uint8_t* dt = (uint8_t*)hr.out;
+    float* dd = (float*)(hr.out + al(n));
+    uint32_t* ds = (uint32_t*)(hr.out + al(n) + al(12 * n));
+    rc = ncg_proximity_batch(c, &hr.dev, margin, dt, out_sep_axis ? dd : nullptr, ds, nullptr, st);
+    if (rc) return rc;
+    cudaMemcpyAsync(out_prox, dt, n, cudaMemcpyDeviceToHost, st);
+    if (out_sep_axis) cudaMemcpyAsync(out_sep_axis, dd, 12 * n, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(status, ds, 4 * n, cudaMemcpyDeviceToHost, st);
+    return cuda_ok(cudaStreamSynchronize(st), "proximity_batch_host") ? NCG_OK : NCG_ECUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,222 @@
+"""Batched queries: the drop-in for ncollide3d's support-map query functions.
+
+    contact_batch        contact_support_map_support_map[_with_params]
+                         (src/query/contact/contact_support_map_support_map.rs:9-88)
+    distance_batch       distance_support_map_support_map[_with_params]
+                         (src/query/distance/distance_support_map_support_map.rs:8-53)
+    proximity_batch      proximity_support_map_support_map[_with_params]
+                         (src/query/proximity/proximity_support_map_support_map.rs:10-75)
+    closest_points_batch closest_points_support_map_support_map[_with_params]
+                         (src/query/closest_points/closest_points_support_map_support_map.rs:9-67)
+
+Each takes a Context and a DeviceBatch (pairs resident in device memory) and
+returns device tensors; the work is queued on the current torch CUDA stream.
+The *_host variants take a host PairBatch and copy in and out through the
+library's synchronous host entry points.  PyTorch only supplies device memory
+and streams; every computation runs in libncg.so.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .shapes import CONTACT_DTYPE, PairBatch
+
+
+class Context:
+    """Owns an ncg_ctx: scratch memory, EPA slabs and settings for one device."""
+
+    def __init__(self, device=0, tolerance=N.TOL_REFERENCE, warm_start=N.WARM_NONE):
+        self._L = N.load()
+        self._p = ctypes.c_void_p()
+        if isinstance(device, torch.device):
+            device = device.index or 0
+        self.device = int(device)
+        N.check(self._L.ncg_ctx_create(ctypes.byref(self._p), self.device), "ncg_ctx_create")
+        self.set_tolerance(tolerance)
+        self.set_warm_start(warm_start)
+
+    @property
+    def handle(self):
+        return self._p
+
+    def set_tolerance(self, mode):
+        if isinstance(mode, str):
+            mode = {"reference": N.TOL_REFERENCE, "precise": N.TOL_PRECISE}[mode]
+        N.check(self._L.ncg_ctx_set_tolerance(self._p, int(mode)), "ncg_ctx_set_tolerance")
+        self.tolerance = int(mode)
+
+    def set_warm_start(self, mode):
+        N.check(self._L.ncg_ctx_set_warm_start(self._p, int(mode)), "ncg_ctx_set_warm_start")
+        self.warm_start = int(mode)
+
+    def stats(self):
+        s = N.NcgStats()
+        N.check(self._L.ncg_get_stats(self._p, ctypes.byref(s)), "ncg_get_stats")
+        return {k: int(getattr(s, k)) for k, _ in N.NcgStats._fields_ if k != "pad"}
+
+    def close(self):
+        if self._p:
+            self._L.ncg_ctx_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+@dataclass
+class DeviceBatch:
+    """A PairBatch resident in device memory (torch tensors, ncg_batch layout)."""
+    shapes: torch.Tensor       # uint8 [S*32]
+    hull_points: torch.Tensor  # float32 [P,4]
+    m1: torch.Tensor           # float32 [N,8]
+    g1: torch.Tensor           # int32 [N] (read as uint32)
+    m2: torch.Tensor
+    g2: torch.Tensor
+    init_dir: torch.Tensor | None = None
+    n_shapes: int = 0
+
+    @property
+    def n_pairs(self):
+        return int(self.g1.shape[0])
+
+    @classmethod
+    def from_host(cls, b: PairBatch, device="cuda", non_blocking=False):
+        def t(a, dt=None):
+            x = torch.from_numpy(np.ascontiguousarray(a))
+            if dt is not None:
+                x = x.view(dt)
+            return x.to(device, non_blocking=non_blocking)
+        return cls(shapes=t(b.shapes.view(np.uint8)), hull_points=t(b.hull_points.astype(np.float32)),
+                   m1=t(b.m1.astype(np.float32)), g1=t(b.g1.astype(np.uint32).view(np.int32)),
+                   m2=t(b.m2.astype(np.float32)), g2=t(b.g2.astype(np.uint32).view(np.int32)),
+                   init_dir=None if b.init_dir is None else t(b.init_dir.astype(np.float32)),
+                   n_shapes=len(b.shapes))
+
+    def with_init_dir(self, init_dir):
+        return DeviceBatch(self.shapes, self.hull_points, self.m1, self.g1, self.m2, self.g2,
+                           None if init_dir is None else init_dir.contiguous(), self.n_shapes)
+
+    def c_struct(self):
+        return N.NcgBatch(self.shapes.data_ptr(), self.hull_points.data_ptr(), self.n_shapes, 0,
+                          int(self.hull_points.shape[0]), self.m1.data_ptr(), self.g1.data_ptr(),
+                          self.m2.data_ptr(), self.g2.data_ptr(), self.n_pairs,
+                          None if self.init_dir is None else self.init_dir.data_ptr())
+
+
+def _stream(stream):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _empty(n, shape, dtype, device):
+    return torch.empty((n,) + tuple(shape), dtype=dtype, device=device)
+
+
+def contact_batch(ctx: Context, db: DeviceBatch, prediction=0.0, with_dir=True, with_iters=False, stream=None):
+    """Returns dict: contact [N,10] (world1, world2, normal, depth), has_contact [N] uint8,
+    dir [N,3] (the direction to pass back as init_dir), status [N] int32, iters [N] int32."""
+    n, dev = db.n_pairs, db.m1.device
+    out = {"contact": _empty(n, (10,), torch.float32, dev), "has_contact": _empty(n, (), torch.uint8, dev),
+           "status": _empty(n, (), torch.int32, dev)}
+    out["dir"] = _empty(n, (3,), torch.float32, dev) if with_dir else None
+    out["iters"] = _empty(n, (), torch.int32, dev) if with_iters else None
+    cb = db.c_struct()
+    N.check(ctx._L.ncg_contact_batch(ctx.handle, ctypes.byref(cb), ctypes.c_float(prediction), _ptr(out["contact"]),
+                                     _ptr(out["has_contact"]), _ptr(out["dir"]), _ptr(out["status"]),
+                                     _ptr(out["iters"]), _stream(stream)), "ncg_contact_batch")
+    return out
+
+
+def distance_batch(ctx: Context, db: DeviceBatch, with_iters=False, stream=None):
+    n, dev = db.n_pairs, db.m1.device
+    out = {"distance": _empty(n, (), torch.float32, dev), "status": _empty(n, (), torch.int32, dev),
+           "iters": _empty(n, (), torch.int32, dev) if with_iters else None}
+    cb = db.c_struct()
+    N.check(ctx._L.ncg_distance_batch(ctx.handle, ctypes.byref(cb), _ptr(out["distance"]), _ptr(out["status"]),
+                                      _ptr(out["iters"]), _stream(stream)), "ncg_distance_batch")
+    return out
+
+
+def proximity_batch(ctx: Context, db: DeviceBatch, margin=0.0, with_dir=True, with_iters=False, stream=None):
+    n, dev = db.n_pairs, db.m1.device
+    out = {"proximity": _empty(n, (), torch.uint8, dev), "status": _empty(n, (), torch.int32, dev),
+           "dir": _empty(n, (3,), torch.float32, dev) if with_dir else None,
+           "iters": _empty(n, (), torch.int32, dev) if with_iters else None}
+    cb = db.c_struct()
+    N.check(ctx._L.ncg_proximity_batch(ctx.handle, ctypes.byref(cb), ctypes.c_float(margin), _ptr(out["proximity"]),
+                                       _ptr(out["dir"]), _ptr(out["status"]), _ptr(out["iters"]),
+                                       _stream(stream)), "ncg_proximity_batch")
+    return out
+
+
+def closest_points_batch(ctx: Context, db: DeviceBatch, prediction=0.0, with_iters=False, stream=None):
+    n, dev = db.n_pairs, db.m1.device
+    out = {"tag": _empty(n, (), torch.uint8, dev), "points": _empty(n, (6,), torch.float32, dev),
+           "status": _empty(n, (), torch.int32, dev),
+           "iters": _empty(n, (), torch.int32, dev) if with_iters else None}
+    cb = db.c_struct()
+    N.check(ctx._L.ncg_closest_points_batch(ctx.handle, ctypes.byref(cb), ctypes.c_float(prediction),
+                                            _ptr(out["tag"]), _ptr(out["points"]), _ptr(out["status"]),
+                                            _ptr(out["iters"]), _stream(stream)), "ncg_closest_points_batch")
+    return out
+
+
+def _host_struct(b: PairBatch, keep):
+    arrs = {"shapes": np.ascontiguousarray(b.shapes), "hull": np.ascontiguousarray(b.hull_points, np.float32),
+            "m1": np.ascontiguousarray(b.m1, np.float32), "g1": np.ascontiguousarray(b.g1, np.uint32),
+            "m2": np.ascontiguousarray(b.m2, np.float32), "g2": np.ascontiguousarray(b.g2, np.uint32),
+            "init": None if b.init_dir is None else np.ascontiguousarray(b.init_dir, np.float32)}
+    keep.append(arrs)
+    p = lambda a: None if a is None else a.ctypes.data
+    return N.NcgBatch(p(arrs["shapes"]), p(arrs["hull"]), len(b.shapes), 0, arrs["hull"].shape[0], p(arrs["m1"]),
+                      p(arrs["g1"]), p(arrs["m2"]), p(arrs["g2"]), b.n_pairs, p(arrs["init"]))
+
+
+def contact_batch_host(ctx: Context, b: PairBatch, prediction=0.0):
+    """Host-memory contact query (copies inputs in and results out)."""
+    keep = []
+    cb = _host_struct(b, keep)
+    n = b.n_pairs
+    contact = np.zeros(n, CONTACT_DTYPE)
+    has = np.zeros(n, np.uint8)
+    d = np.zeros((n, 3), np.float32)
+    st = np.zeros(n, np.uint32)
+    N.check(ctx._L.ncg_contact_batch_host(ctx.handle, ctypes.byref(cb), ctypes.c_float(prediction),
+                                          contact.ctypes.data, has.ctypes.data, d.ctypes.data, st.ctypes.data),
+            "ncg_contact_batch_host")
+    return {"contact": contact, "has_contact": has, "dir": d, "status": st}
+
+
+def distance_batch_host(ctx: Context, b: PairBatch):
+    keep = []
+    cb = _host_struct(b, keep)
+    n = b.n_pairs
+    dist = np.zeros(n, np.float32)
+    st = np.zeros(n, np.uint32)
+    N.check(ctx._L.ncg_distance_batch_host(ctx.handle, ctypes.byref(cb), dist.ctypes.data, st.ctypes.data),
+            "ncg_distance_batch_host")
+    return {"distance": dist, "status": st}
+
+
+def proximity_batch_host(ctx: Context, b: PairBatch, margin=0.0):
+    keep = []
+    cb = _host_struct(b, keep)
+    n = b.n_pairs
+    prox = np.zeros(n, np.uint8)
+    d = np.zeros((n, 3), np.float32)
+    st = np.zeros(n, np.uint32)
+    N.check(ctx._L.ncg_proximity_batch_host(ctx.handle, ctypes.byref(cb), ctypes.c_float(margin), prox.ctypes.data,
+                                            d.ctypes.data, st.ctypes.data), "ncg_proximity_batch_host")
+    return {"proximity": prox, "dir": d, "status": st}

@@ -1,0 +1,203 @@
+"""Seeded synthetic pair batches (the reference publishes no dataset).
+
+Workloads, all f32:
+  cuboid_pairs         65,536 Cuboid-Cuboid pairs (half extents U[0.1,1]^3)
+  mixed_convex         1,048,576 pairs, kinds uniform over Ball, Cuboid,
+                       Capsule, Cone, ConvexHull (n log-uniform in [8,1024],
+                       ellipsoid samples with radial jitter U[0.95,1])
+  precision_stress     the same mix with thin shapes and near-touching
+                       placements (see ncollide_gb300.stress)
+  coherent_hull_pairs  ConvexHull-ConvexHull pairs drawn from a pool of
+                       shared hulls, moved by small steps frame to frame
+
+Poses: rotations are normalised 4-D Gaussians, shape A's centre is uniform
+in [-1,1]^3 and B's centre sits at d*(rA+rB) from A's along a uniform random
+unit direction with d ~ U[0,1.2], r being each shape's circumradius, so
+about half of the pairs intersect.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .shapes import (BALL, CAPSULE, CONE, CONVEX_HULL, CUBOID, CYLINDER, SHAPE_DTYPE,
+                     PairBatch)
+
+MIXED_KINDS = (BALL, CUBOID, CAPSULE, CONE, CONVEX_HULL)
+
+
+def random_unit_quaternions(rng, n):
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return q  # (i, j, k, w)
+
+
+def random_unit_vectors(rng, n):
+    v = rng.standard_normal((n, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    return v
+
+
+def log_uniform_int(rng, lo, hi, n):
+    return np.clip(np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), n))), lo, hi).astype(np.int64)
+
+
+def _hull_points(rng, counts, semi_axes_lo=0.2, thin_axis=None, thin_scale=None):
+    """Ellipsoid samples with radial jitter; one hull per entry of counts."""
+    total = int(counts.sum())
+    dirs = rng.standard_normal((total, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    dirs *= rng.uniform(0.95, 1.0, (total, 1))
+    axes = rng.uniform(semi_axes_lo, 1.0, (len(counts), 3))
+    if thin_axis is not None:
+        axes[np.arange(len(counts)), thin_axis] *= thin_scale
+    dirs *= np.repeat(axes, counts, axis=0)
+    pts = np.zeros((total, 4), np.float32)
+    pts[:, :3] = dirs
+    return pts
+
+
+def _circumradius(shapes, hull_points):
+    kind = shapes["kind"]
+    p = shapes["p"].astype(np.float64)
+    r = np.zeros(len(shapes))
+    r[kind == BALL] = p[kind == BALL, 0]
+    m = kind == CUBOID
+    r[m] = np.linalg.norm(p[m, :3], axis=1)
+    m = kind == CAPSULE
+    r[m] = p[m, 0] + p[m, 1]
+    m = (kind == CONE) | (kind == CYLINDER)
+    r[m] = np.hypot(p[m, 0], p[m, 1])
+    hulls = np.nonzero(kind == CONVEX_HULL)[0]
+    if len(hulls):
+        sq = (hull_points[:, :3].astype(np.float64) ** 2).sum(1)
+        off = shapes["hull_off"][hulls].astype(np.int64)
+        cnt = shapes["hull_n"][hulls].astype(np.int64)
+        # max over each contiguous slice
+        order = np.argsort(off)
+        starts = off[order]
+        mx = np.maximum.reduceat(sq, starts) if len(starts) else np.zeros(0)
+        # reduceat over sorted starts covers each hull's slice when slices tile the array
+        rr = np.empty(len(hulls))
+        rr[order] = np.sqrt(mx)
+        assert np.all(cnt > 0)
+        r[hulls] = rr
+    return r
+
+
+def random_shapes(rng, n, kinds=MIXED_KINDS, hull_n=(8, 1024), thin=False):
+    """n shape records with kinds drawn uniformly from `kinds`."""
+    kind = np.asarray(kinds, np.uint32)[rng.integers(0, len(kinds), n)]
+    shapes = np.zeros(n, SHAPE_DTYPE)
+    shapes["kind"] = kind
+    p = np.zeros((n, 4), np.float64)
+    m = kind == BALL
+    p[m, 0] = rng.uniform(0.1, 1.0, m.sum())
+    m = kind == CUBOID
+    p[m, :3] = rng.uniform(0.1, 1.0, (m.sum(), 3))
+    m = kind == CAPSULE
+    p[m, 0] = rng.uniform(0.1, 1.0, m.sum())
+    p[m, 1] = rng.uniform(0.05, 0.5, m.sum())
+    m = (kind == CONE) | (kind == CYLINDER)
+    p[m, 0] = rng.uniform(0.1, 1.0, m.sum())
+    p[m, 1] = rng.uniform(0.1, 1.0, m.sum())
+    hulls = np.nonzero(kind == CONVEX_HULL)[0]
+    thin_axis = thin_scale = None
+    if thin:
+        s = np.exp(rng.uniform(np.log(1e-3), 0.0, n))
+        ax = rng.integers(0, 3, n)
+        m = kind == CUBOID
+        p[m, ax[m]] *= s[m]
+        m = (kind == CAPSULE) | (kind == CONE) | (kind == CYLINDER)
+        # axis 0 -> half height, otherwise the radius
+        p[m, np.where(ax[m] == 0, 0, 1)] *= s[m]
+        thin_axis, thin_scale = ax[hulls], s[hulls]
+    shapes["p"] = p.astype(np.float32)
+    if len(hulls):
+        counts = log_uniform_int(rng, hull_n[0], hull_n[1], len(hulls))
+        pts = _hull_points(rng, counts, thin_axis=thin_axis, thin_scale=thin_scale)
+        offs = np.concatenate([[0], np.cumsum(counts)[:-1]])
+        shapes["hull_off"][hulls] = offs.astype(np.uint32)
+        shapes["hull_n"][hulls] = counts.astype(np.uint32)
+    else:
+        pts = np.zeros((1, 4), np.float32)
+    return shapes, pts
+
+
+def _poses(rng, n, ra, rb, dmax=1.2):
+    m1 = np.zeros((n, 8), np.float32)
+    m2 = np.zeros((n, 8), np.float32)
+    m1[:, :4] = random_unit_quaternions(rng, n)
+    m2[:, :4] = random_unit_quaternions(rng, n)
+    ta = rng.uniform(-1.0, 1.0, (n, 3))
+    u = random_unit_vectors(rng, n)
+    d = rng.uniform(0.0, dmax, (n, 1))
+    m1[:, 4:7] = ta
+    m2[:, 4:7] = ta + d * (ra + rb)[:, None] * u
+    return m1, m2
+
+
+def _pair_batch(shapes, pts, m1, m2, radii, meta):
+    n = m1.shape[0]
+    g1 = np.arange(0, 2 * n, 2, dtype=np.uint32)
+    g2 = np.arange(1, 2 * n, 2, dtype=np.uint32)
+    return PairBatch(shapes, np.ascontiguousarray(pts), m1, g1, m2, g2,
+                     scale=radii[g1] + radii[g2], meta=meta)
+
+
+def cuboid_pairs(n=65536, seed=0):
+    """Cuboid-Cuboid pairs, half extents U[0.1,1]^3."""
+    rng = np.random.default_rng(seed)
+    shapes, pts = random_shapes(rng, 2 * n, kinds=(CUBOID,))
+    radii = _circumradius(shapes, pts)
+    m1, m2 = _poses(rng, n, radii[0::2], radii[1::2])
+    return _pair_batch(shapes, pts, m1, m2, radii, {"workload": "cuboid_pairs", "n": n, "seed": seed})
+
+
+def mixed_convex(n=1 << 20, seed=1, kinds=MIXED_KINDS, hull_n=(8, 1024), thin=False, dmax=1.2):
+    """Mixed convex pairs with uneven costs (ConvexHull sizes 8..1024)."""
+    rng = np.random.default_rng(seed)
+    shapes, pts = random_shapes(rng, 2 * n, kinds=kinds, hull_n=hull_n, thin=thin)
+    radii = _circumradius(shapes, pts)
+    m1, m2 = _poses(rng, n, radii[0::2], radii[1::2], dmax=dmax)
+    return _pair_batch(shapes, pts, m1, m2, radii,
+                       {"workload": "mixed_convex", "n": n, "seed": seed, "thin": thin})
+
+
+def coherent_hull_pairs(n=1 << 24, seed=5, pool=1 << 16, hull_n=(32, 1024)):
+    """ConvexHull-ConvexHull pairs over a pool of `pool` shared hulls."""
+    rng = np.random.default_rng(seed)
+    shapes, pts = random_shapes(rng, pool, kinds=(CONVEX_HULL,), hull_n=hull_n)
+    radii = _circumradius(shapes, pts)
+    g1 = rng.integers(0, pool, n).astype(np.uint32)
+    g2 = rng.integers(0, pool, n).astype(np.uint32)
+    m1, m2 = _poses(rng, n, radii[g1], radii[g2])
+    return PairBatch(shapes, pts, m1, g1, m2, g2, scale=radii[g1] + radii[g2],
+                     meta={"workload": "coherent_hull_pairs", "n": n, "seed": seed, "pool": pool})
+
+
+def _quat_mul(a, b):
+    ai, aj, ak, aw = a[:, 0], a[:, 1], a[:, 2], a[:, 3]
+    bi, bj, bk, bw = b[:, 0], b[:, 1], b[:, 2], b[:, 3]
+    return np.stack([aw * bi + ai * bw + aj * bk - ak * bj,
+                     aw * bj - ai * bk + aj * bw + ak * bi,
+                     aw * bk + ai * bj - aj * bi + ak * bw,
+                     aw * bw - ai * bi - aj * bj - ak * bk], axis=1)
+
+
+def advance_frame(batch, rng, sigma_t=0.01, sigma_r=0.02):
+    """One frame of coherent motion: every pose gets a translation step
+    N(0, sigma_t^2) per axis and a rotation about a random axis by N(0, sigma_r^2)."""
+    out = []
+    for m in (batch.m1, batch.m2):
+        n = m.shape[0]
+        m = m.copy()
+        ax = random_unit_vectors(rng, n)
+        ang = rng.normal(0.0, sigma_r, n)
+        dq = np.concatenate([ax * np.sin(ang / 2)[:, None], np.cos(ang / 2)[:, None]], axis=1)
+        q = _quat_mul(dq, m[:, :4].astype(np.float64))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+        m[:, :4] = q
+        m[:, 4:7] += rng.normal(0.0, sigma_t, (n, 3))
+        out.append(m)
+    return PairBatch(batch.shapes, batch.hull_points, out[0], batch.g1, out[1], batch.g2,
+                     batch.init_dir, batch.scale, dict(batch.meta))

@@ -1,0 +1,247 @@
+// oracle_capi.cpp — TEST INFRASTRUCTURE ONLY: extern "C" batch driver of the
+// oracle (ncg_oracle.hpp) for ctypes.  Reads the same packed inputs as the GPU
+// library (include/ncg.h) and runs the reference algorithm per pair on
+// std::threads (one static contiguous chunk of pairs per thread).
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "../include/ncg.h"
+#include "ncg_oracle.hpp"
+
+using namespace ncgo;
+
+namespace {
+
+enum Policy { POLICY_F32 = 0, POLICY_F64 = 1, POLICY_MIXED = 2 };
+enum Query { Q_CONTACT = 0, Q_DISTANCE = 1, Q_PROXIMITY = 2, Q_CLOSEST = 3 };
+
+// Inputs either in the library's f32 layout or as f64 arrays (known-answer tests
+// use decimal literals that f32 cannot hold; the f64 oracle must see them exactly).
+struct InF32 {
+    const ncg_shape* shapes;
+    uint32_t n_shapes;
+    const float* pts;
+    uint64_t n_pts;
+    const ncg_pose* m1;
+    const uint32_t* g1;
+    const ncg_pose* m2;
+    const uint32_t* g2;
+    const float* init_dir;
+};
+struct InF64 {
+    const int32_t* kinds;
+    const uint32_t* hull_off;
+    const uint32_t* hull_n;
+    const double* params;  // 4 per shape
+    uint32_t n_shapes;
+    const double* pts;     // 4 per point
+    uint64_t n_pts;
+    const double* m1;      // 8 per pair: qi qj qk qw tx ty tz pad
+    const uint32_t* g1;
+    const double* m2;
+    const uint32_t* g2;
+    const double* init_dir;
+};
+
+template <class N> bool load_shape(const InF32& in, uint32_t id, Shape<N>* s) {
+    if (id >= in.n_shapes) return false;
+    const ncg_shape& r = in.shapes[id];
+    s->kind = (int)r.kind;
+    s->p0 = N(r.p[0]);
+    s->p1 = N(r.p[1]);
+    s->p2 = N(r.p[2]);
+    s->pts4 = nullptr;
+    s->pts4d = nullptr;
+    s->n = 0;
+    if (r.kind > NCG_CONVEX_HULL) return false;
+    if (r.kind == NCG_CONVEX_HULL) {
+        if (r.hull_n == 0 || (uint64_t)r.hull_off + r.hull_n > in.n_pts) return false;
+        s->pts4 = in.pts + 4 * (uint64_t)r.hull_off;
+        s->n = r.hull_n;
+    }
+    return true;
+}
+template <class N> bool load_shape(const InF64& in, uint32_t id, Shape<N>* s) {
+    if (id >= in.n_shapes) return false;
+    s->kind = in.kinds[id];
+    s->p0 = N(in.params[4 * id]);
+    s->p1 = N(in.params[4 * id + 1]);
+    s->p2 = N(in.params[4 * id + 2]);
+    s->pts4 = nullptr;
+    s->pts4d = nullptr;
+    s->n = 0;
+    if (s->kind < 0 || s->kind > NCG_CONVEX_HULL) return false;
+    if (s->kind == NCG_CONVEX_HULL) {
+        if (in.hull_n[id] == 0 || (uint64_t)in.hull_off[id] + in.hull_n[id] > in.n_pts) return false;
+        s->pts4d = in.pts + 4 * (uint64_t)in.hull_off[id];
+        s->n = in.hull_n[id];
+    }
+    return true;
+}
+template <class N> Iso<N> load_pose(const ncg_pose& p) {
+    return Iso<N>{Quat<N>{N(p.q[0]), N(p.q[1]), N(p.q[2]), N(p.q[3])}, V3<N>{N(p.t[0]), N(p.t[1]), N(p.t[2])}};
+}
+template <class N> Iso<N> load_pose(const double* p) {
+    return Iso<N>{Quat<N>{N(p[0]), N(p[1]), N(p[2]), N(p[3])}, V3<N>{N(p[4]), N(p[5]), N(p[6])}};
+}
+template <class N> Iso<N> pose1(const InF32& in, uint64_t i) { return load_pose<N>(in.m1[i]); }
+template <class N> Iso<N> pose2(const InF32& in, uint64_t i) { return load_pose<N>(in.m2[i]); }
+template <class N> Iso<N> pose1(const InF64& in, uint64_t i) { return load_pose<N>(in.m1 + 8 * i); }
+template <class N> Iso<N> pose2(const InF64& in, uint64_t i) { return load_pose<N>(in.m2 + 8 * i); }
+template <class N> bool init_dir(const InF32& in, uint64_t i, V3<N>* d) {
+    if (!in.init_dir) return false;
+    *d = V3<N>{N(in.init_dir[3 * i]), N(in.init_dir[3 * i + 1]), N(in.init_dir[3 * i + 2])};
+    return true;
+}
+template <class N> bool init_dir(const InF64& in, uint64_t i, V3<N>* d) {
+    if (!in.init_dir) return false;
+    *d = V3<N>{N(in.init_dir[3 * i]), N(in.init_dir[3 * i + 1]), N(in.init_dir[3 * i + 2])};
+    return true;
+}
+
+struct Outs {
+    double* out16;
+    uint8_t* tag;
+    uint32_t* status;
+    uint32_t* counters8;
+};
+
+template <class N, class S, class In>
+void run_range(const In& in, int query, S param, const Tol<S>& tol, uint64_t lo, uint64_t hi, const Outs& o) {
+    for (uint64_t i = lo; i < hi; ++i) {
+        Counters cnt;
+        Shape<N> s1, s2;
+        QueryOut<S> r{};
+        bool ok = load_shape<N>(in, in.g1[i], &s1) && load_shape<N>(in, in.g2[i], &s2);
+        if (!ok) {
+            cnt.status |= ST_BAD_INPUT;
+        } else {
+            Iso<N> m1 = pose1<N>(in, i), m2 = pose2<N>(in, i);
+            V3<N> d;
+            const V3<N>* dp = init_dir<N>(in, i, &d) ? &d : nullptr;
+            switch (query) {
+            case Q_CONTACT: r = contact<N, S>(m1, s1, m2, s2, param, dp, tol, &cnt); break;
+            case Q_DISTANCE: r = distance<N, S>(m1, s1, m2, s2, dp, tol, &cnt); break;
+            case Q_PROXIMITY: r = proximity<N, S>(m1, s1, m2, s2, param, dp, tol, &cnt); break;
+            default: r = closest_points<N, S>(m1, s1, m2, s2, param, dp, tol, &cnt); break;
+            }
+        }
+        if (o.out16) {
+            double* w = o.out16 + 16 * i;
+            w[0] = r.p1.x; w[1] = r.p1.y; w[2] = r.p1.z;
+            w[3] = r.p2.x; w[4] = r.p2.y; w[5] = r.p2.z;
+            w[6] = r.dir.x; w[7] = r.dir.y; w[8] = r.dir.z;
+            w[9] = r.value;
+            w[10] = r.gjk_kind;
+            for (int k = 11; k < 16; ++k) w[k] = 0.0;
+        }
+        if (o.tag) o.tag[i] = (uint8_t)r.tag;
+        if (o.status) o.status[i] = cnt.status;
+        if (o.counters8) {
+            uint32_t* c = o.counters8 + 8 * i;
+            c[0] = cnt.gjk_iters;
+            c[1] = cnt.epa_iters;
+            c[2] = cnt.support_calls;
+            c[3] = cnt.hull_points_scanned;
+            c[4] = cnt.faces_created;
+            c[5] = cnt.epa_max_vertices;
+            c[6] = cnt.epa_max_faces;
+            c[7] = (cnt.subsolve[0] + cnt.subsolve[1] + cnt.subsolve[2] + cnt.subsolve[3]) | (cnt.epa_exit << 24);
+        }
+    }
+}
+
+template <class N, class S, class In>
+int run(const In& in, uint64_t n_pairs, int query, double param, double eps, double epa_tol, int n_threads,
+        const Outs& o) {
+    S e = eps > 0 ? S(eps) : std::numeric_limits<S>::epsilon();
+    if (eps <= 0 && sizeof(N) < sizeof(S)) e = S(std::numeric_limits<N>::epsilon());
+    Tol<S> tol(e, S(epa_tol > 0 ? epa_tol : 0.0));
+    S p = S(param);
+    if (n_threads <= 1 || n_pairs < 64) {
+        run_range<N, S>(in, query, p, tol, 0, n_pairs, o);
+        return 0;
+    }
+    std::vector<std::thread> th;
+    uint64_t chunk = (n_pairs + n_threads - 1) / n_threads;
+    for (int t = 0; t < n_threads; ++t) {
+        uint64_t lo = t * chunk, hi = std::min<uint64_t>(n_pairs, lo + chunk);
+        if (lo >= hi) break;
+        th.emplace_back([&, lo, hi] { run_range<N, S>(in, query, p, tol, lo, hi, o); });
+    }
+    for (auto& x : th) x.join();
+    return 0;
+}
+
+template <class In>
+int dispatch(int policy, const In& in, uint64_t n, int query, double param, double eps, double epa_tol, int nt,
+             const Outs& o) {
+    if (query == Q_PROXIMITY && param < 0) return NCG_EINVAL;
+    switch (policy) {
+    case POLICY_F32: return run<float, float>(in, n, query, param, eps, epa_tol, nt, o);
+    case POLICY_F64: return run<double, double>(in, n, query, param, eps, epa_tol, nt, o);
+    case POLICY_MIXED: return run<float, double>(in, n, query, param, eps, epa_tol, nt, o);
+    default: return NCG_EINVAL;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// policy: 0 = reference f32, 1 = reference f64, 2 = f32 supports + f64 sub-solve.
+// query:  0 = contact, 1 = distance, 2 = proximity, 3 = closest_points.
+// eps <= 0 selects the machine epsilon of the policy's N (the reference's
+// default_epsilon); any other value replaces it in every tolerance.
+// epa_tol > 0 replaces EPA's termination threshold (100 eps) alone.
+// out16: per pair p1[3] p2[3] dir[3] value gjk_kind, padded to 16 doubles.
+// counters8: gjk iters, epa iters, support calls, hull points scanned,
+//            faces created, EPA max vertices, EPA max faces,
+//            sub-solves | (EPA exit << 24).
+int ncgo_query(int policy, int query, double param, double eps, double epa_tol, int n_threads, const ncg_shape* shapes,
+               uint32_t n_shapes, const float* hull_points, uint64_t n_hull_points, uint64_t n_pairs,
+               const ncg_pose* m1, const uint32_t* g1, const ncg_pose* m2, const uint32_t* g2,
+               const float* init_dir, double* out16, uint8_t* tag, uint32_t* status, uint32_t* counters8) {
+    InF32 in{shapes, n_shapes, hull_points, n_hull_points, m1, g1, m2, g2, init_dir};
+    Outs o{out16, tag, status, counters8};
+    return dispatch(policy, in, n_pairs, query, param, eps, epa_tol, n_threads, o);
+}
+
+int ncgo_query_f64in(int policy, int query, double param, double eps, double epa_tol, int n_threads, const int32_t* kinds,
+                     const uint32_t* hull_off, const uint32_t* hull_n, const double* params, uint32_t n_shapes,
+                     const double* hull_points, uint64_t n_hull_points, uint64_t n_pairs, const double* m1,
+                     const uint32_t* g1, const double* m2, const uint32_t* g2, const double* init_dir,
+                     double* out16, uint8_t* tag, uint32_t* status, uint32_t* counters8) {
+    InF64 in{kinds, hull_off, hull_n, params, n_shapes, hull_points, n_hull_points, m1, g1, m2, g2, init_dir};
+    Outs o{out16, tag, status, counters8};
+    return dispatch(policy, in, n_pairs, query, param, eps, epa_tol, n_threads, o);
+}
+
+// benches/query/algorithm.rs:5-23: reset(a), add_point(b, c, d), project.
+// pts: 4 points x 3 doubles.  added[3] receives add_point's results.
+int ncgo_simplex_kat(int policy, const double* pts, int* added, double* proj, int* dim_out) {
+    auto go = [&](auto tag_n) {
+        using N = decltype(tag_n);
+        using S = N;
+        Tol<S> tol(std::numeric_limits<S>::epsilon());
+        CSOPoint<N> c[4];
+        for (int i = 0; i < 4; ++i) {
+            V3<N> p{N(pts[3 * i]), N(pts[3 * i + 1]), N(pts[3 * i + 2])};
+            c[i] = CSOPoint<N>{p, p, zero3<N>()};  // CSOPoint::single_point
+        }
+        VoronoiSimplex<N, S> s;
+        s.reset(c[0]);
+        for (int i = 1; i < 4; ++i) added[i - 1] = s.add_point(c[i], tol) ? 1 : 0;
+        V3<S> r = s.project_origin_and_reduce(tol, nullptr);
+        proj[0] = r.x; proj[1] = r.y; proj[2] = r.z;
+        *dim_out = s.dim;
+    };
+    if (policy == POLICY_F64) go(double(0));
+    else go(float(0));
+    return 0;
+}
+
+int ncgo_abi_version(void) { return NCG_ABI_VERSION; }
+
+}  // extern "C"

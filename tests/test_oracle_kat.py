@@ -1,0 +1,96 @@
+"""The oracle against the reference's own known answers (tests/golden/reference_kats.json).
+
+These pin the CPU restatement (oracle/ncg_oracle.hpp) before anything is
+compared with it.  Inputs are the reference tests' decimal literals, fed in
+f64 (the reference's tests infer f64 for float literals).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kats.json")))
+
+
+def test_epa3_cuboid_cuboid_exact():
+    k = GOLD["epa3"]
+    c = (1, tuple(k["shape"]["half_extents"]), None)
+    pairs = [(O.pose8(cs["m1_translation"]), c, O.pose8(cs["m2_translation"]), c) for cs in k["cases"]]
+    r = O.query_f64(pairs, O.CONTACT, O.F64, param=k["cases"][0]["prediction"])
+    for i, cs in enumerate(k["cases"]):
+        assert r.tag[i] == 1
+        assert r.value[i] == cs["depth"]          # assert_eq! in the reference
+        assert list(r.dir[i]) == cs["normal"]
+
+
+def test_cylinder_cuboid_issue157():
+    k = GOLD["cylinder_cuboid"]
+    cyl = (4, (k["cylinder"]["half_height"], k["cylinder"]["radius"]), None)
+    cub = (1, tuple(k["cuboid"]["half_extents"]), None)
+    pair = [(O.pose8(k["cylinder"]["translation"]), cyl, O.pose8(k["cuboid"]["translation"]), cub)]
+    for pol in (O.F64, O.F32, O.MIXED):
+        d = O.query_f64(pair, O.DISTANCE, pol)
+        p = O.query_f64(pair, O.PROXIMITY, pol, param=k["proximity_margin"])
+        c = O.query_f64(pair, O.CONTACT, pol, param=k["contact_prediction"])
+        assert d.value[0] == k["distance"]
+        assert p.tag[0] == k["proximity"]
+        assert c.tag[0] == 1
+
+
+def test_distance_example():
+    k = GOLD["distance_example"]
+    ball, cub = (0, (k["ball_radius"],), None), (1, tuple(k["cuboid_half_extents"]), None)
+    pairs = [(O.pose8(cs["ball_translation"]), ball, O.pose8(), cub) for cs in k["cases"]]
+    r = O.query_f64(pairs, O.DISTANCE, O.F64)
+    assert r.value[0] == 0.0
+    assert abs(r.value[1] - 1.0) <= k["cases"][1]["epsilon"]
+
+
+def test_proximity_example():
+    k = GOLD["proximity_example"]
+    ball, cub = (0, (k["ball_radius"],), None), (1, tuple(k["cuboid_half_extents"]), None)
+    pairs = [(O.pose8(cs["ball_translation"]), ball, O.pose8(), cub) for cs in k["cases"]]
+    for pol in (O.F64, O.F32, O.MIXED):
+        r = O.query_f64(pairs, O.PROXIMITY, pol, param=k["margin"])
+        assert list(r.tag) == [cs["proximity"] for cs in k["cases"]]
+
+
+def test_johnson_simplex_rejects_degenerate_point():
+    k = GOLD["johnson_simplex"]
+    for pol in (O.F32, O.F64):
+        added, proj, dim = O.simplex_kat(k["points"], pol)
+        assert list(added) == k["add_point_results"]
+        assert dim <= 2
+
+
+def test_touching_cuboids_no_nan():
+    k = GOLD["touching_cuboids"]
+    c = (1, tuple(k["half_extents"]), None)
+    pair = [(O.pose8(k["m1_translation"]), c, O.pose8(k["m2_translation"]), c)]
+    r = O.query_f64(pair, O.CONTACT, O.F32, param=k["prediction"])
+    assert np.all(np.isfinite(r.value)) and np.all(np.isfinite(r.dir))
+
+
+def test_coincident_cubes_equal_keys():
+    # Coincident unit cubes (tests/pipeline/contact_pairs.rs:8-85): GJK ends on
+    # a segment through the origin, EPA starts from two flat faces pushed with
+    # equal keys (epa3.rs:319-320) and the best face keeps zero barycentric
+    # coordinates, so the contact has depth 0 — the reference's pipeline test
+    # skips `contact.depth == 0.0` for exactly this configuration.  Every
+    # precision must agree, and the normal must be an axis.
+    c = (1, (1.0, 1.0, 1.0), None)
+    outs = [O.query_f64([(O.pose8(), c, O.pose8(), c)], O.CONTACT, pol, param=0.0) for pol in (O.F64, O.F32, O.MIXED)]
+    for r in outs:
+        assert r.tag[0] == 1
+        assert sorted(np.abs(r.dir[0]).tolist()) == [0.0, 0.0, 1.0]
+        assert r.value[0] == 0.0
+        assert np.all(np.isfinite(r.p1)) and np.all(np.isfinite(r.p2))
+
+
+def test_margin_negative_is_rejected():
+    c = (1, (1.0, 1.0, 1.0), None)
+    with pytest.raises(ValueError):
+        O.query_f64([(O.pose8(), c, O.pose8((5, 0, 0)), c)], O.PROXIMITY, O.F64, param=-1.0)
