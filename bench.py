@@ -1,0 +1,352 @@
+"""Benchmark: batched GJK/EPA contact pairs/s on one GB300.
+
+Workload: 1,048,576 mixed convex pairs (Ball, Cuboid, Capsule, Cone and
+ConvexHull with 8..1024 points, seeded synthetic data), query::contact with
+prediction 0 in the PRECISE tolerance set, inputs resident in HBM (1.5 GB,
+larger than L2).  One step = one contact_batch over the whole batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is device-resident throughput; `e2e` is the
+same metric through the library's host entry point with host<->device copies
+inside the timed region; `cpu_baseline` times the CPU restatement of the
+reference path (the oracle, f32) on the host cores; `roofline` describes the
+dominant kernel.  With torchrun (N > 1) every rank processes its own batch
+(weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GJK/EPA contact pairs/s on 1 GB300: warm-started vs plain at ≤1e-5 rel err"
+N_PAIRS = 1 << 20
+SEED = 1
+# Algorithmic FP32 operations per unit of work, counted from the restated
+# reference: a quaternion rotation is 30 flops and each support call rotates
+# twice (66 flops with the CSO difference), a hull point costs 5 flops in the
+# arg-max (3 mul + 2 add), a GJK sub-solve ~300 and an EPA face ~150.
+FLOPS_SUPPORT, FLOPS_HULL_POINT, FLOPS_SUBSOLVE, FLOPS_FACE = 66.0, 5.0, 300.0, 150.0
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_workload(rank):
+    from ncollide_gb300 import workloads as W
+    return W.mixed_convex(N_PAIRS, seed=SEED + rank)
+
+
+def algorithmic(batch, counters):
+    """Bytes and FP32 flops per pair (inputs read once, outputs written once)."""
+    n = batch.n_pairs
+    kinds = batch.shapes["kind"]
+    hull_bytes = 16.0 * (batch.shapes["hull_n"][batch.g1].astype(np.float64) +
+                         batch.shapes["hull_n"][batch.g2].astype(np.float64))
+    in_bytes = 2 * 32 + 2 * 32 + 2 * 4 + hull_bytes.mean()
+    out_bytes = 40 + 1 + 12 + 4
+    c = counters.astype(np.float64)
+    flops = (c[:, 2] * FLOPS_SUPPORT + c[:, 3] * FLOPS_HULL_POINT + (c[:, 7].astype(np.uint32) & 0xffffff) *
+             FLOPS_SUBSOLVE + c[:, 4] * FLOPS_FACE).mean()
+    del kinds
+    return in_bytes + out_bytes, in_bytes, out_bytes, flops
+
+
+def accuracy_report(batch, gpu_out, sample):
+    """Errors of the GPU contacts against the oracle built with f64 (the error
+    oracle), on the first `sample` pairs; classification against the oracle's
+    f32 reference path outside a 1e-6 band."""
+    from oracle import oracle as O
+    sub = batch.subset(np.arange(sample))
+    r64 = O.query(sub, O.CONTACT, O.F64, param=0.0)
+    r32 = O.query(sub, O.CONTACT, O.F32, param=0.0)
+    d64 = O.query(sub, O.DISTANCE, O.F64)
+    has = gpu_out["has_contact"][:sample]
+    c = gpu_out["contact"][:sample].astype(np.float64)
+    k1, k2 = sub.kinds()
+    curved = np.isin(k1, [0, 2, 3]) | np.isin(k2, [0, 2, 3])
+    ballball = (k1 == 0) & (k2 == 0)
+    both = (has == 1) & (r64.tag == 1) & ~ballball
+    scale = sub.scale
+    dd = np.abs(c[:, 9] - r64.value) / np.maximum(np.abs(r64.value), scale)
+    dn = np.linalg.norm(c[:, 6:9] - r64.dir, axis=1)
+    dp = np.maximum(np.linalg.norm(c[:, 0:3] - r64.p1, axis=1), np.linalg.norm(c[:, 3:6] - r64.p2, axis=1)) / scale
+    sep = np.where(r64.gjk_kind == O.GJK_INTERSECTION, -1.0, 1.0) * d64.value  # signed gap
+    band = np.abs(d64.value) <= 1e-6 * scale
+    gpu_int = (has == 1) & (c[:, 9] > 0)
+    ref_int = (r32.tag == 1) & (r32.value > 0)
+    del sep
+
+    def pct(x, m):
+        return {"p50": float(np.percentile(x[m], 50)), "p99": float(np.percentile(x[m], 99)),
+                "max": float(x[m].max()), "frac_gt_1e-5": float((x[m] > 1e-5).mean()), "n": int(m.sum())} \
+            if m.any() else None
+    return {
+        "sample_pairs": int(sample),
+        "relative_to": "max(|f64 value|, rA+rB); normals absolute",
+        "depth": {"polytope_pairs": pct(dd, both & ~curved), "curved_pairs": pct(dd, both & curved)},
+        "normal": {"polytope_pairs": pct(dn, both & ~curved), "curved_pairs": pct(dn, both & curved)},
+        "witness_points": {"polytope_pairs": pct(dp, both & ~curved), "curved_pairs": pct(dp, both & curved)},
+        "intersect_classification_mismatch_vs_f32_ref_outside_band": int(((gpu_int != ref_int) & ~band).sum()),
+        "ball_ball_pairs_excluded": int(ballball.sum()),
+    }
+
+
+def cpu_baseline(batch, threads):
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    O.query(batch, O.CONTACT, O.F32, param=0.0, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": batch.n_pairs / dt, "unit": "pairs/s", "cores": threads, "kind": "port",
+            "sample": f"all {batch.n_pairs} pairs of the workload, 1 run, contact f32 reference path "
+                      f"(oracle restatement; the Rust reference cannot be built here)", "seconds": dt}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU path (restated oracle, f32) on host cores."""
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    batch = make_workload(0)
+    threads = os.cpu_count() or 1
+    sample = batch.subset(np.arange(min(batch.n_pairs, 1 << 18)))
+    for _ in range(args.warmup):
+        O.query(sample, O.CONTACT, O.F32, param=0.0, threads=threads)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.query(sample, O.CONTACT, O.F32, param=0.0, threads=threads)
+        ts.append(time.perf_counter() - t0)
+    total = sum(ts)
+    value = sample.n_pairs * len(ts) / total
+    line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / len(ts), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "mixed_convex_1M", "n_pairs": batch.n_pairs, "query": "contact",
+                       "prediction": 0.0, "seed": SEED, "step_sample_pairs": sample.n_pairs},
+            "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": f"first {sample.n_pairs} pairs of the workload per step"},
+            "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--tolerance", default="precise", choices=["precise", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--accuracy-sample", type=int, default=32768)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import _native as Nn
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    batch = make_workload(rank)
+    db = Q.DeviceBatch.from_host(batch, device=f"cuda:{local}")
+    ctx = Q.Context(local, tolerance=args.tolerance)
+    ctx.set_profiling(True)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        out = Q.contact_batch(ctx, db, 0.0, with_iters=False)
+    torch.cuda.synchronize()
+
+    stage_sums = {}
+    launches = 0
+    with ClockSampler(local) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            out = Q.contact_batch(ctx, db, 0.0)
+            st = ctx.stage_ms()  # waits for this step's last stage event
+            for k, v in st.items():
+                stage_sums[k] = stage_sums.get(k, 0.0) + v
+            launches += ctx.stats()["kernels_launched"]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * batch.n_pairs * args.steps / (ms / 1e3)
+    stats = ctx.stats()
+
+    # ---- e2e through the host entry point (pinned host buffers)
+    e2e = None
+    if rank == 0 or True:
+        import ctypes
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        h = {"shapes": pin(batch.shapes.view(np.uint8)), "hull": pin(batch.hull_points),
+             "m1": pin(batch.m1), "g1": pin(batch.g1.view(np.int32)), "m2": pin(batch.m2),
+             "g2": pin(batch.g2.view(np.int32))}
+        n = batch.n_pairs
+        ho = {"contact": torch.empty((n, 10), dtype=torch.float32).pin_memory(),
+              "has": torch.empty(n, dtype=torch.uint8).pin_memory(),
+              "dir": torch.empty((n, 3), dtype=torch.float32).pin_memory(),
+              "status": torch.empty(n, dtype=torch.int32).pin_memory()}
+        cb = Nn.NcgBatch(h["shapes"].data_ptr(), h["hull"].data_ptr(), len(batch.shapes), 0,
+                         batch.hull_points.shape[0], h["m1"].data_ptr(), h["g1"].data_ptr(), h["m2"].data_ptr(),
+                         h["g2"].data_ptr(), n, None)
+        L = Nn.load()
+        ctx.set_profiling(False)
+
+        def host_step():
+            Nn.check(L.ncg_contact_batch_host(ctx.handle, ctypes.byref(cb), ctypes.c_float(0.0),
+                                              ho["contact"].data_ptr(), ho["has"].data_ptr(), ho["dir"].data_ptr(),
+                                              ho["status"].data_ptr()), "ncg_contact_batch_host")
+        for _ in range(2):
+            host_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            host_step()
+        dt = time.perf_counter() - t0
+        h2d = sum(int(v.numel() * v.element_size()) for v in h.values())
+        d2h = sum(int(v.numel() * v.element_size()) for v in ho.values())
+        e2e = {"value": batch.n_pairs * args.steps / dt, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "api": "ncg_contact_batch_host"}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    # ---- roofline of the dominant kernel
+    from oracle import oracle as O  # the checker: counts algorithmic work on a sample
+    pk = peaks()
+    hbm_peak = float(pk.get("hbm_gbs", 6800.0))
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = sm_count * 128 * 2 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12  # TFLOP/s
+    mean_stage = {k: v / args.steps for k, v in stage_sums.items()}
+    dom = max(mean_stage, key=mean_stage.get)
+    sample = batch.subset(np.arange(min(65536, batch.n_pairs)))
+    rs = O.query(sample, O.CONTACT, O.MIXED, param=0.0, eps=-1.0 if args.tolerance == "precise" else 0.0,
+                 epa_tol=1e-6 if args.tolerance == "precise" else 0.0)
+    bytes_pp, in_pp, out_pp, flops_pp = algorithmic(batch, rs.counters)
+    units = {"classify": batch.n_pairs, "gjk_thread": stats.get("n_pairs", 0), "gjk_warp": stats.get("n_pairs", 0),
+             "epa_tier_a": stats["n_epa"], "epa_tier_b": stats["n_epa_overflow"],
+             "epa_tier_c": stats["n_epa_overflow"]}.get(dom, batch.n_pairs)
+    dom_s = mean_stage[dom] / 1e3
+    achieved = units * bytes_pp / dom_s / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                "traffic": None, "units_per_launch": int(units), "bytes_per_unit": bytes_pp,
+                "mean_launch_ms": mean_stage[dom], "stage_ms": mean_stage,
+                "fp32": {"achieved_tflops": batch.n_pairs * flops_pp / (ms / 1e3 / args.steps) / 1e12,
+                         "peak_tflops": fp32_peak, "frac": batch.n_pairs * flops_pp / (ms / 1e3 / args.steps) /
+                         1e12 / fp32_peak, "flops_per_pair": flops_pp,
+                         "note": "whole step; peak = SMs x 128 x 2 x max SM clock"}}
+
+    cpu = None
+    acc = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(batch, os.cpu_count() or 1)
+        out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
+        acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs))
+
+    line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "mixed_convex_1M", "n_pairs": batch.n_pairs, "query": "contact",
+                       "prediction": 0.0, "tolerance": args.tolerance, "warm_start": "none (plain)",
+                       "seed": SEED, "parallelism": f"weak x{world}" if world > 1 else "1 GPU",
+                       "l2": "inputs larger than L2 (%.2f GB resident)" % (batch.nbytes_inputs() / 1e9)},
+            "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
+            "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc,
+            "epa": {"pairs": stats["n_epa"], "tier_b_pairs": stats["n_epa_overflow"],
+                    "gjk_iters_per_pair": stats["gjk_iters"] / batch.n_pairs,
+                    "epa_iters_per_epa_pair": stats["epa_iters"] / max(1, stats["n_epa"])}}
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

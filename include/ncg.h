@@ -143,6 +143,16 @@ int ncg_ctx_set_tolerance(ncg_ctx* ctx, int tolerance);
 int ncg_ctx_set_warm_start(ncg_ctx* ctx, int warm_start);
 int ncg_sync(ncg_ctx* ctx, void* stream);
 int ncg_get_stats(ncg_ctx* ctx, ncg_stats* out);
+
+/* Stage timing: when enabled, each batch call records CUDA events between its
+ * kernel launches on the caller's stream.  ncg_get_stage_ms fills up to
+ * n_max durations in milliseconds (order: classify, gjk_thread, gjk_warp,
+ * epa_tier_a, epa_tier_b, epa_tier_c) of the last call and returns how many it
+ * wrote; it synchronises on the last call's events.  No reference counterpart
+ * (the reference has no instrumentation). */
+#define NCG_N_STAGES 6
+int ncg_ctx_set_profiling(ncg_ctx* ctx, int enabled);
+int ncg_get_stage_ms(ncg_ctx* ctx, float* ms, int n_max);
 const char* ncg_last_error(void);
 int ncg_abi_version(void);
 

@@ -3,10 +3,11 @@
 //
 // Arithmetic split: support mapping and CSO points in f32; the simplex
 // sub-solve (segment / triangle / tetrahedron Voronoi projection), GJK's bound
-// tests and the search direction in f64.  The library is compiled with
-// -fmad=false and every expression keeps the reference's evaluation order, so
-// a pair's result is a deterministic function of its inputs (no contraction,
-// IEEE division and square root).
+// tests and the search direction in double-word arithmetic (`real`, see
+// ncg_dw.cuh), which gives FP64-class precision on the FP32 pipes.  The library
+// is compiled with -fmad=false and every expression keeps the reference's
+// evaluation order, so a pair's result is a deterministic function of its
+// inputs (no contraction, IEEE division and square root).
 //
 // Reference (ncollide 0.33): src/shape/support_map.rs:25-28,
 // src/shape/{ball,cuboid,capsule,cone,cylinder}.rs, src/shape/convex.rs:418-423,
@@ -23,7 +24,11 @@
 
 #define NCG_DEV __device__ __forceinline__
 
+#include "ncg_dw.cuh"
+
 namespace ncg {
+
+using real = dw;
 
 // ------------------------------------------------------------------ vectors
 template <class T> struct vec3 {
@@ -40,10 +45,10 @@ template <class T> NCG_DEV vec3<T> cross(vec3<T> a, vec3<T> b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 template <class T> NCG_DEV T norm_sq(vec3<T> a) { return dot(a, a); }
-NCG_DEV float vnorm(vec3<float> a) { return sqrtf(norm_sq(a)); }
-NCG_DEV double vnorm(vec3<double> a) { return sqrt(norm_sq(a)); }
-NCG_DEV vec3<double> to_d(vec3<float> a) { return {(double)a.x, (double)a.y, (double)a.z}; }
-NCG_DEV vec3<float> to_f(vec3<double> a) { return {(float)a.x, (float)a.y, (float)a.z}; }
+NCG_DEV float vnorm(vec3<float> a) { return __fsqrt_rn(norm_sq(a)); }
+NCG_DEV real vnorm(vec3<real> a) { return sqrt(norm_sq(a)); }
+NCG_DEV vec3<real> to_r(vec3<float> a) { return {real(a.x), real(a.y), real(a.z)}; }
+NCG_DEV vec3<float> to_f(vec3<real> a) { return {a.x.h, a.y.h, a.z.h}; }
 template <class T> NCG_DEV vec3<T> zero3() { return {T(0), T(0), T(0)}; }
 
 // Unit::try_new_and_get: None when |v| <= min_norm.
@@ -221,117 +226,118 @@ template <class Scan> NCG_DEV CSO cso_support(const PairGeom& g, vec3<float> d, 
 
 // ------------------------------------------------------------------ tolerances
 // gjk.rs:26-29, :92; epa3.rs:231-232; utils/triangle.rs:94-101.  Computed on
-// the host in f64 from the chosen epsilon.
+// the host in f64 from the chosen epsilon and split into double-words.
 struct Tol {
-    double eps, eps_tol, eps_rel, epa_eps_tol, affine_eps;
-    float init_eps;  // f32::EPSILON: Unit::try_new on the initial direction
+    dw_host eps, eps_tol, eps_rel, epa_eps_tol, affine_eps;
+    dw_host add_tol;                // VoronoiSimplex::add_point's degeneracy threshold
+    float eps_tol_f, affine_eps_f;  // the same thresholds for the f32 EPA visibility test
+    float init_eps;                 // f32::EPSILON: Unit::try_new on the initial direction
 };
 
 // ------------------------------------------------------------------ projections
 enum { LOC_VERTEX = 0, LOC_EDGE = 1, LOC_FACE = 2, LOC_SOLID = 3 };
-struct Loc {
+template <class T> struct Loc {
     int kind, i;
-    double b0, b1, b2;
+    T b0, b1, b2;
 };
 
-NCG_DEV vec3<double> proj_segment(vec3<double> a, vec3<double> b, Loc& loc) {
-    vec3<double> p = zero3<double>();
-    vec3<double> ab = b - a, ap = p - a;
-    double ab_ap = dot(ab, ap), sqnab = norm_sq(ab);
-    if (ab_ap <= 0.0) {
-        loc = Loc{LOC_VERTEX, 0, 1.0, 0.0, 0.0};
+template <class T> NCG_DEV vec3<T> proj_segment(vec3<T> a, vec3<T> b, Loc<T>& loc) {
+    vec3<T> p = zero3<T>();
+    vec3<T> ab = b - a, ap = p - a;
+    T ab_ap = dot(ab, ap), sqnab = norm_sq(ab);
+    if (ab_ap <= T(0.0f)) {
+        loc = Loc<T>{LOC_VERTEX, 0, T(1.0f), T(0.0f), T(0.0f)};
         return a;
     } else if (ab_ap >= sqnab) {
-        loc = Loc{LOC_VERTEX, 1, 1.0, 0.0, 0.0};
+        loc = Loc<T>{LOC_VERTEX, 1, T(1.0f), T(0.0f), T(0.0f)};
         return b;
     }
-    double u = ab_ap / sqnab;
-    loc = Loc{LOC_EDGE, 0, 1.0 - u, u, 0.0};
+    T u = ab_ap / sqnab;
+    loc = Loc<T>{LOC_EDGE, 0, T(1.0f) - u, u, T(0.0f)};
     return a + ab * u;
 }
 
-NCG_DEV vec3<double> proj_triangle(vec3<double> a, vec3<double> b, vec3<double> c, Loc& loc) {
-    vec3<double> p = zero3<double>();
-    vec3<double> ab = b - a, ac = c - a, ap = p - a;
-    double ab_ap = dot(ab, ap), ac_ap = dot(ac, ap);
-    if (ab_ap <= 0.0 && ac_ap <= 0.0) {
-        loc = Loc{LOC_VERTEX, 0, 1.0, 0.0, 0.0};
+template <class T> NCG_DEV vec3<T> proj_triangle(vec3<T> a, vec3<T> b, vec3<T> c, Loc<T>& loc) {
+    vec3<T> p = zero3<T>();
+    vec3<T> ab = b - a, ac = c - a, ap = p - a;
+    T ab_ap = dot(ab, ap), ac_ap = dot(ac, ap);
+    if (ab_ap <= T(0.0f) && ac_ap <= T(0.0f)) {
+        loc = Loc<T>{LOC_VERTEX, 0, T(1.0f), T(0.0f), T(0.0f)};
         return a;
     }
-    vec3<double> bp = p - b;
-    double ab_bp = dot(ab, bp), ac_bp = dot(ac, bp);
-    if (ab_bp >= 0.0 && ac_bp <= ab_bp) {
-        loc = Loc{LOC_VERTEX, 1, 1.0, 0.0, 0.0};
+    vec3<T> bp = p - b;
+    T ab_bp = dot(ab, bp), ac_bp = dot(ac, bp);
+    if (ab_bp >= T(0.0f) && ac_bp <= ab_bp) {
+        loc = Loc<T>{LOC_VERTEX, 1, T(1.0f), T(0.0f), T(0.0f)};
         return b;
     }
-    vec3<double> cp = p - c;
-    double ab_cp = dot(ab, cp), ac_cp = dot(ac, cp);
-    if (ac_cp >= 0.0 && ab_cp <= ac_cp) {
-        loc = Loc{LOC_VERTEX, 2, 1.0, 0.0, 0.0};
+    vec3<T> cp = p - c;
+    T ab_cp = dot(ab, cp), ac_cp = dot(ac, cp);
+    if (ac_cp >= T(0.0f) && ab_cp <= ac_cp) {
+        loc = Loc<T>{LOC_VERTEX, 2, T(1.0f), T(0.0f), T(0.0f)};
         return c;
     }
-    vec3<double> bc = c - b;
-    vec3<double> n = cross(ab, ac);
-    double vc = dot(n, cross(ab, ap));
-    if (vc < 0.0 && ab_ap >= 0.0 && ab_bp <= 0.0) {
-        double v = ab_ap / norm_sq(ab);
-        loc = Loc{LOC_EDGE, 0, 1.0 - v, v, 0.0};
+    vec3<T> bc = c - b;
+    vec3<T> n = cross(ab, ac);
+    T vc = dot(n, cross(ab, ap));
+    if (vc < T(0.0f) && ab_ap >= T(0.0f) && ab_bp <= T(0.0f)) {
+        T v = ab_ap / norm_sq(ab);
+        loc = Loc<T>{LOC_EDGE, 0, T(1.0f) - v, v, T(0.0f)};
         return a + ab * v;
     }
-    double vb = -dot(n, cross(ac, cp));
-    if (vb < 0.0 && ac_ap >= 0.0 && ac_cp <= 0.0) {
-        double w = ac_ap / norm_sq(ac);
-        loc = Loc{LOC_EDGE, 2, 1.0 - w, w, 0.0};
+    T vb = -dot(n, cross(ac, cp));
+    if (vb < T(0.0f) && ac_ap >= T(0.0f) && ac_cp <= T(0.0f)) {
+        T w = ac_ap / norm_sq(ac);
+        loc = Loc<T>{LOC_EDGE, 2, T(1.0f) - w, w, T(0.0f)};
         return a + ac * w;
     }
-    double va = dot(n, cross(bc, bp));
-    if (va < 0.0 && ac_bp - ab_bp >= 0.0 && ab_cp - ac_cp >= 0.0) {
-        double w = dot(bc, bp) / norm_sq(bc);
-        loc = Loc{LOC_EDGE, 1, 1.0 - w, w, 0.0};
+    T va = dot(n, cross(bc, bp));
+    if (va < T(0.0f) && ac_bp - ab_bp >= T(0.0f) && ab_cp - ac_cp >= T(0.0f)) {
+        T w = dot(bc, bp) / norm_sq(bc);
+        loc = Loc<T>{LOC_EDGE, 1, T(1.0f) - w, w, T(0.0f)};
         return b + bc * w;
     }
-    int cw = dot(n, ap) >= 0.0 ? 0 : 1;
-    if (va + vb + vc != 0.0) {
-        double denom = 1.0 / (va + vb + vc);
-        double v = vb * denom, w = vc * denom;
-        loc = Loc{LOC_FACE, cw, 1.0 - v - w, v, w};
+    int cw = dot(n, ap) >= T(0.0f) ? 0 : 1;
+    if (va + vb + vc != T(0.0f)) {
+        T denom = T(1.0f) / (va + vb + vc);
+        T v = vb * denom, w = vc * denom;
+        loc = Loc<T>{LOC_FACE, cw, T(1.0f) - v - w, v, w};
         return (a + ab * v) + ac * w;
     }
-    loc = Loc{LOC_SOLID, 0, 0.0, 0.0, 0.0};
+    loc = Loc<T>{LOC_SOLID, 0, T(0.0f), T(0.0f), T(0.0f)};
     return p;
 }
 
 struct EdgeTest {
-    double d1, d2;
+    real d1, d2;
     bool hit;
-    double u;
+    real u;
 };
-NCG_DEV EdgeTest tet_edge(vec3<double> nabc, vec3<double> nabd, vec3<double> ap, vec3<double> ab, double ap_ab,
-                          double bp_ab) {
+NCG_DEV EdgeTest tet_edge(vec3<real> nabc, vec3<real> nabd, vec3<real> ap, vec3<real> ab, real ap_ab, real bp_ab) {
     EdgeTest r;
-    double ab_ab = ap_ab - bp_ab;
-    vec3<double> x = cross(ap, ab);
+    real ab_ab = ap_ab - bp_ab;
+    vec3<real> x = cross(ap, ab);
     r.d1 = dot(x, nabc);
     r.d2 = dot(x, nabd);
-    r.hit = ab_ab != 0.0 && r.d1 >= 0.0 && r.d2 >= 0.0 && ap_ab >= 0.0 && ap_ab <= ab_ab;
-    r.u = r.hit ? ap_ab / ab_ab : 0.0;
+    r.hit = ab_ab != real(0.0f) && r.d1 >= real(0.0f) && r.d2 >= real(0.0f) && ap_ab >= real(0.0f) && ap_ab <= ab_ab;
+    r.u = r.hit ? ap_ab / ab_ab : real(0.0f);
     return r;
 }
-NCG_DEV bool tet_face(vec3<double> a, vec3<double> b, vec3<double> c, vec3<double> ap, vec3<double> bp,
-                      vec3<double> cp, vec3<double> ab, vec3<double> ac, vec3<double> ad, double dabc, double dbca,
-                      double dacb, double eps, vec3<double>& proj, double bc[3], uint32_t& status) {
-    if (dabc < 0.0 && dbca < 0.0 && dacb < 0.0) {
-        vec3<double> n = cross(ab, ac);
-        if (dot(n, ad) * dot(n, ap) < 0.0) {
-            vec3<double> nn;
-            double len;
+NCG_DEV bool tet_face(vec3<real> a, vec3<real> b, vec3<real> c, vec3<real> ap, vec3<real> bp, vec3<real> cp,
+                      vec3<real> ab, vec3<real> ac, vec3<real> ad, real dabc, real dbca, real dacb, real eps,
+                      vec3<real>& proj, real bc[3], uint32_t& status) {
+    if (dabc < real(0.0f) && dbca < real(0.0f) && dacb < real(0.0f)) {
+        vec3<real> n = cross(ab, ac);
+        if (dot(n, ad) * dot(n, ap) < real(0.0f)) {
+            vec3<real> nn;
+            real len;
             if (!try_normalize(n, eps, nn, len)) return false;
-            double vc = dot(nn, cross(ap, bp));
-            double va = dot(nn, cross(bp, cp));
-            double vb = dot(nn, cross(cp, ap));
-            double denom = va + vb + vc;
-            if (denom == 0.0) status |= NCG_STATUS_DEGENERATE;
-            double inv = 1.0 / denom;
+            real vc = dot(nn, cross(ap, bp));
+            real va = dot(nn, cross(bp, cp));
+            real vb = dot(nn, cross(cp, ap));
+            real denom = va + vb + vc;
+            if (denom == real(0.0f)) status |= NCG_STATUS_DEGENERATE;
+            real inv = real(1.0f) / denom;
             bc[0] = va * inv;
             bc[1] = vb * inv;
             bc[2] = vc * inv;
@@ -341,86 +347,86 @@ NCG_DEV bool tet_face(vec3<double> a, vec3<double> b, vec3<double> c, vec3<doubl
     }
     return false;
 }
-NCG_DEV vec3<double> proj_tetrahedron(vec3<double> a, vec3<double> b, vec3<double> c, vec3<double> d, double eps,
-                                      Loc& loc, uint32_t& status) {
-    vec3<double> p = zero3<double>();
-    vec3<double> ab = b - a, ac = c - a, ad = d - a, ap = p - a;
-    double ap_ab = dot(ap, ab), ap_ac = dot(ap, ac), ap_ad = dot(ap, ad);
-    if (ap_ab <= 0.0 && ap_ac <= 0.0 && ap_ad <= 0.0) {
-        loc = Loc{LOC_VERTEX, 0, 1.0, 0.0, 0.0};
+NCG_DEV vec3<real> proj_tetrahedron(vec3<real> a, vec3<real> b, vec3<real> c, vec3<real> d, real eps,
+                                    Loc<real>& loc, uint32_t& status) {
+    vec3<real> p = zero3<real>();
+    vec3<real> ab = b - a, ac = c - a, ad = d - a, ap = p - a;
+    real ap_ab = dot(ap, ab), ap_ac = dot(ap, ac), ap_ad = dot(ap, ad);
+    if (ap_ab <= real(0.0f) && ap_ac <= real(0.0f) && ap_ad <= real(0.0f)) {
+        loc = Loc<real>{LOC_VERTEX, 0, real(1.0f), real(0.0f), real(0.0f)};
         return a;
     }
-    vec3<double> bc = c - b, bd = d - b, bp = p - b;
-    double bp_bc = dot(bp, bc), bp_bd = dot(bp, bd), bp_ab = dot(bp, ab);
-    if (bp_bc <= 0.0 && bp_bd <= 0.0 && bp_ab >= 0.0) {
-        loc = Loc{LOC_VERTEX, 1, 1.0, 0.0, 0.0};
+    vec3<real> bc = c - b, bd = d - b, bp = p - b;
+    real bp_bc = dot(bp, bc), bp_bd = dot(bp, bd), bp_ab = dot(bp, ab);
+    if (bp_bc <= real(0.0f) && bp_bd <= real(0.0f) && bp_ab >= real(0.0f)) {
+        loc = Loc<real>{LOC_VERTEX, 1, real(1.0f), real(0.0f), real(0.0f)};
         return b;
     }
-    vec3<double> cd = d - c, cp = p - c;
-    double cp_ac = dot(cp, ac), cp_bc = dot(cp, bc), cp_cd = dot(cp, cd);
-    if (cp_cd <= 0.0 && cp_bc >= 0.0 && cp_ac >= 0.0) {
-        loc = Loc{LOC_VERTEX, 2, 1.0, 0.0, 0.0};
+    vec3<real> cd = d - c, cp = p - c;
+    real cp_ac = dot(cp, ac), cp_bc = dot(cp, bc), cp_cd = dot(cp, cd);
+    if (cp_cd <= real(0.0f) && cp_bc >= real(0.0f) && cp_ac >= real(0.0f)) {
+        loc = Loc<real>{LOC_VERTEX, 2, real(1.0f), real(0.0f), real(0.0f)};
         return c;
     }
-    vec3<double> dp = p - d;
-    double dp_cd = dot(dp, cd), dp_bd = dot(dp, bd), dp_ad = dot(dp, ad);
-    if (dp_ad >= 0.0 && dp_bd >= 0.0 && dp_cd >= 0.0) {
-        loc = Loc{LOC_VERTEX, 3, 1.0, 0.0, 0.0};
+    vec3<real> dp = p - d;
+    real dp_cd = dot(dp, cd), dp_bd = dot(dp, bd), dp_ad = dot(dp, ad);
+    if (dp_ad >= real(0.0f) && dp_bd >= real(0.0f) && dp_cd >= real(0.0f)) {
+        loc = Loc<real>{LOC_VERTEX, 3, real(1.0f), real(0.0f), real(0.0f)};
         return d;
     }
-    vec3<double> nabc = cross(ab, ac), nabd = cross(ab, ad);
+    vec3<real> nabc = cross(ab, ac), nabd = cross(ab, ad);
     EdgeTest e = tet_edge(nabc, nabd, ap, ab, ap_ab, bp_ab);
-    if (e.hit) { loc = Loc{LOC_EDGE, 0, 1.0 - e.u, e.u, 0.0}; return a + ab * e.u; }
-    double dabc = e.d1, dabd = e.d2;
-    vec3<double> nacd = cross(ac, ad);
+    if (e.hit) { loc = Loc<real>{LOC_EDGE, 0, real(1.0f) - e.u, e.u, real(0.0f)}; return a + ab * e.u; }
+    real dabc = e.d1, dabd = e.d2;
+    vec3<real> nacd = cross(ac, ad);
     e = tet_edge(nacd, -nabc, ap, ac, ap_ac, cp_ac);
-    if (e.hit) { loc = Loc{LOC_EDGE, 1, 1.0 - e.u, e.u, 0.0}; return a + ac * e.u; }
-    double dacd = e.d1, dacb = e.d2;
+    if (e.hit) { loc = Loc<real>{LOC_EDGE, 1, real(1.0f) - e.u, e.u, real(0.0f)}; return a + ac * e.u; }
+    real dacd = e.d1, dacb = e.d2;
     e = tet_edge(-nabd, -nacd, ap, ad, ap_ad, dp_ad);
-    if (e.hit) { loc = Loc{LOC_EDGE, 2, 1.0 - e.u, e.u, 0.0}; return a + ad * e.u; }
-    double dadb = e.d1, dadc = e.d2;
-    vec3<double> nbcd = cross(bc, bd);
+    if (e.hit) { loc = Loc<real>{LOC_EDGE, 2, real(1.0f) - e.u, e.u, real(0.0f)}; return a + ad * e.u; }
+    real dadb = e.d1, dadc = e.d2;
+    vec3<real> nbcd = cross(bc, bd);
     e = tet_edge(nabc, nbcd, bp, bc, bp_bc, cp_bc);
-    if (e.hit) { loc = Loc{LOC_EDGE, 3, 1.0 - e.u, e.u, 0.0}; return b + bc * e.u; }
-    double dbca = e.d1, dbcd = e.d2;
+    if (e.hit) { loc = Loc<real>{LOC_EDGE, 3, real(1.0f) - e.u, e.u, real(0.0f)}; return b + bc * e.u; }
+    real dbca = e.d1, dbcd = e.d2;
     e = tet_edge(-nbcd, nabd, bp, bd, bp_bd, dp_bd);
-    if (e.hit) { loc = Loc{LOC_EDGE, 4, 1.0 - e.u, e.u, 0.0}; return b + bd * e.u; }
-    double dbdc = e.d1, dbda = e.d2;
+    if (e.hit) { loc = Loc<real>{LOC_EDGE, 4, real(1.0f) - e.u, e.u, real(0.0f)}; return b + bd * e.u; }
+    real dbdc = e.d1, dbda = e.d2;
     e = tet_edge(nacd, nbcd, cp, cd, cp_cd, dp_cd);
-    if (e.hit) { loc = Loc{LOC_EDGE, 5, 1.0 - e.u, e.u, 0.0}; return c + cd * e.u; }
-    double dcda = e.d1, dcdb = e.d2;
+    if (e.hit) { loc = Loc<real>{LOC_EDGE, 5, real(1.0f) - e.u, e.u, real(0.0f)}; return c + cd * e.u; }
+    real dcda = e.d1, dcdb = e.d2;
 
-    vec3<double> pr;
-    double bw[3];
+    vec3<real> pr;
+    real bw[3];
     if (tet_face(a, b, c, ap, bp, cp, ab, ac, ad, dabc, dbca, dacb, eps, pr, bw, status)) {
-        loc = Loc{LOC_FACE, 0, bw[0], bw[1], bw[2]};
+        loc = Loc<real>{LOC_FACE, 0, bw[0], bw[1], bw[2]};
         return pr;
     }
     if (tet_face(a, b, d, ap, bp, dp, ab, ad, ac, dadb, dabd, dbda, eps, pr, bw, status)) {
-        loc = Loc{LOC_FACE, 1, bw[0], bw[1], bw[2]};
+        loc = Loc<real>{LOC_FACE, 1, bw[0], bw[1], bw[2]};
         return pr;
     }
     if (tet_face(a, c, d, ap, cp, dp, ac, ad, ab, dacd, dcda, dadc, eps, pr, bw, status)) {
-        loc = Loc{LOC_FACE, 2, bw[0], bw[1], bw[2]};
+        loc = Loc<real>{LOC_FACE, 2, bw[0], bw[1], bw[2]};
         return pr;
     }
     if (tet_face(b, c, d, bp, cp, dp, bc, bd, -ab, dbcd, dcdb, dbdc, eps, pr, bw, status)) {
-        loc = Loc{LOC_FACE, 3, bw[0], bw[1], bw[2]};
+        loc = Loc<real>{LOC_FACE, 3, bw[0], bw[1], bw[2]};
         return pr;
     }
-    loc = Loc{LOC_SOLID, 0, 0.0, 0.0, 0.0};
+    loc = Loc<real>{LOC_SOLID, 0, real(0.0f), real(0.0f), real(0.0f)};
     return p;
 }
 
 // ------------------------------------------------------------------ simplex
 struct Simplex {
     CSO v[4];
-    double proj[3];
-    double prev_proj[3];
+    real proj[3];
+    real prev_proj[3];
     int prev_v[4];
     int dim, prev_dim;
 
-    NCG_DEV vec3<double> pt(int i) const { return to_d(v[i].p); }
+    NCG_DEV vec3<real> pt(int i) const { return to_r(v[i].p); }
     NCG_DEV void swap(int i, int j) {
         CSO t = v[i];
         v[i] = v[j];
@@ -434,8 +440,8 @@ struct Simplex {
         prev_dim = 0;
         v[0] = c;
         prev_v[0] = 0; prev_v[1] = 1; prev_v[2] = 2; prev_v[3] = 3;
-        proj[0] = proj[1] = proj[2] = 0.0;
-        prev_proj[0] = prev_proj[1] = prev_proj[2] = 0.0;
+        proj[0] = proj[1] = proj[2] = real(0.0f);
+        prev_proj[0] = prev_proj[1] = prev_proj[2] = real(0.0f);
     }
     NCG_DEV bool add_point(const CSO& c, const Tol& tol) {
         prev_dim = dim;
@@ -443,35 +449,35 @@ struct Simplex {
         prev_proj[1] = proj[1];
         prev_proj[2] = proj[2];
         prev_v[0] = 0; prev_v[1] = 1; prev_v[2] = 2; prev_v[3] = 3;
-        vec3<double> ps = to_d(c.p);
+        vec3<real> ps = to_r(c.p);
         if (dim == 0) {
-            if (norm_sq(pt(0) - ps) < tol.eps_tol) return false;
+            if (norm_sq(pt(0) - ps) < from_host(tol.add_tol)) return false;
         } else if (dim == 1) {
-            vec3<double> ab = pt(1) - pt(0), ac = ps - pt(0);
-            if (norm_sq(cross(ab, ac)) < tol.eps_tol) return false;
+            vec3<real> ab = pt(1) - pt(0), ac = ps - pt(0);
+            if (norm_sq(cross(ab, ac)) < from_host(tol.add_tol)) return false;
         } else {
-            vec3<double> ab = pt(1) - pt(0), ac = pt(2) - pt(0), ap = ps - pt(0);
-            vec3<double> cr = cross(ab, ac);
-            vec3<double> n = cr / vnorm(cr);
-            if (fabs(dot(n, ap)) < tol.eps_tol) return false;
+            vec3<real> ab = pt(1) - pt(0), ac = pt(2) - pt(0), ap = ps - pt(0);
+            vec3<real> cr = cross(ab, ac);
+            vec3<real> n = cr / vnorm(cr);
+            if (fabs(dot(n, ap)) < from_host(tol.add_tol)) return false;
         }
         dim += 1;
         v[dim] = c;
         return true;
     }
-    NCG_DEV vec3<double> project_origin_and_reduce(const Tol& tol, uint32_t& status) {
+    NCG_DEV vec3<real> project_origin_and_reduce(const Tol& tol, uint32_t& status) {
         if (dim == 0) {
-            proj[0] = 1.0;
+            proj[0] = real(1.0f);
             return pt(0);
         } else if (dim == 1) {
-            Loc loc;
-            vec3<double> r = proj_segment(pt(0), pt(1), loc);
+            Loc<real> loc;
+            vec3<real> r = proj_segment(pt(0), pt(1), loc);
             if (loc.kind == LOC_VERTEX && loc.i == 0) {
-                proj[0] = 1.0;
+                proj[0] = real(1.0f);
                 dim = 0;
             } else if (loc.kind == LOC_VERTEX) {
                 swap(0, 1);
-                proj[0] = 1.0;
+                proj[0] = real(1.0f);
                 dim = 0;
             } else {
                 proj[0] = loc.b0;
@@ -479,11 +485,11 @@ struct Simplex {
             }
             return r;
         } else if (dim == 2) {
-            Loc loc;
-            vec3<double> r = proj_triangle(pt(0), pt(1), pt(2), loc);
+            Loc<real> loc;
+            vec3<real> r = proj_triangle(pt(0), pt(1), pt(2), loc);
             if (loc.kind == LOC_VERTEX) {
                 swap(0, loc.i);
-                proj[0] = 1.0;
+                proj[0] = real(1.0f);
                 dim = 0;
             } else if (loc.kind == LOC_EDGE) {
                 if (loc.i == 0) {
@@ -506,11 +512,11 @@ struct Simplex {
             }
             return r;
         }
-        Loc loc;
-        vec3<double> r = proj_tetrahedron(pt(0), pt(1), pt(2), pt(3), tol.eps, loc, status);
+        Loc<real> loc;
+        vec3<real> r = proj_tetrahedron(pt(0), pt(1), pt(2), pt(3), from_host(tol.eps), loc, status);
         if (loc.kind == LOC_VERTEX) {
             swap(0, loc.i);
-            proj[0] = 1.0;
+            proj[0] = real(1.0f);
             dim = 0;
         } else if (loc.kind == LOC_EDGE) {
             switch (loc.i) {
@@ -552,24 +558,24 @@ struct Simplex {
 enum { GJK_INTERSECTION = 0, GJK_CLOSEST_POINTS = 1, GJK_PROXIMITY = 2, GJK_NO_INTERSECTION = 3 };
 struct GjkOut {
     int kind;
-    vec3<double> p1, p2, dir;
+    vec3<real> p1, p2, dir;
 };
 
-NCG_DEV void gjk_result(const Simplex& s, bool prev, vec3<double>& p1, vec3<double>& p2) {
-    vec3<double> r1 = zero3<double>(), r2 = zero3<double>();
+NCG_DEV void gjk_result(const Simplex& s, bool prev, vec3<real>& p1, vec3<real>& p2) {
+    vec3<real> r1 = zero3<real>(), r2 = zero3<real>();
     if (prev) {
         for (int i = 0; i < s.prev_dim + 1; ++i) {
-            double c = s.prev_proj[i];
+            real c = s.prev_proj[i];
             const CSO& p = s.v[s.prev_v[i]];
-            r1 = r1 + to_d(p.o1) * c;
-            r2 = r2 + to_d(p.o2) * c;
+            r1 = r1 + to_r(p.o1) * c;
+            r2 = r2 + to_r(p.o2) * c;
         }
     } else {
         for (int i = 0; i < s.dim + 1; ++i) {
-            double c = s.proj[i];
+            real c = s.proj[i];
             const CSO& p = s.v[i];
-            r1 = r1 + to_d(p.o1) * c;
-            r2 = r2 + to_d(p.o2) * c;
+            r1 = r1 + to_r(p.o1) * c;
+            r2 = r2 + to_r(p.o2) * c;
         }
     }
     p1 = r1;
@@ -578,27 +584,28 @@ NCG_DEV void gjk_result(const Simplex& s, bool prev, vec3<double>& p1, vec3<doub
 
 // gjk::closest_points.  `iters` counts loop entries (one CSO support each).
 template <class Scan>
-NCG_DEV GjkOut gjk(const PairGeom& g, double max_dist, bool exact, Simplex& s, const Tol& tol, const Scan& scan,
+NCG_DEV GjkOut gjk(const PairGeom& g, real max_dist, bool exact, Simplex& s, const Tol& tol, const Scan& scan,
                    uint32_t& iters, uint32_t& status, int max_iter) {
     GjkOut r;
-    r.p1 = r.p2 = r.dir = zero3<double>();
-    vec3<double> proj = s.project_origin_and_reduce(tol, status);
-    vec3<double> old_dir, dir;
+    r.p1 = r.p2 = r.dir = zero3<real>();
+    vec3<real> proj = s.project_origin_and_reduce(tol, status);
+    vec3<real> old_dir, dir;
     {
-        vec3<double> u;
-        double n;
-        if (try_normalize(proj, 0.0, u, n)) old_dir = -u;
+        vec3<real> u;
+        real n;
+        if (try_normalize(proj, real(0.0f), u, n)) old_dir = -u;
         else { r.kind = GJK_INTERSECTION; return r; }
     }
-    double max_bound = DBL_MAX;
+    real max_bound = dw_max();
+    const real eps_tol = from_host(tol.eps_tol), eps_rel = from_host(tol.eps_rel);
     int niter = 0;
     for (;;) {
         iters++;
-        double old_max_bound = max_bound;
+        real old_max_bound = max_bound;
         {
-            vec3<double> u;
-            double n;
-            if (try_normalize(-proj, tol.eps_tol, u, n)) { dir = u; max_bound = n; }
+            vec3<real> u;
+            real n;
+            if (try_normalize(-proj, eps_tol, u, n)) { dir = u; max_bound = n; }
             else { r.kind = GJK_INTERSECTION; return r; }
         }
         if (max_bound >= old_max_bound) {
@@ -608,13 +615,13 @@ NCG_DEV GjkOut gjk(const PairGeom& g, double max_dist, bool exact, Simplex& s, c
             return r;
         }
         CSO c = cso_support(g, to_f(dir), scan);
-        double min_bound = -dot(dir, to_d(c.p));
+        real min_bound = -dot(dir, to_r(c.p));
         if (min_bound != min_bound) status |= NCG_STATUS_BAD_INPUT;
         if (min_bound > max_dist) {
             r.kind = GJK_NO_INTERSECTION; r.dir = dir; return r;
-        } else if (!exact && min_bound > 0.0 && max_bound <= max_dist) {
+        } else if (!exact && min_bound > real(0.0f) && max_bound <= max_dist) {
             r.kind = GJK_PROXIMITY; r.dir = old_dir; return r;
-        } else if (max_bound - min_bound <= tol.eps_rel * max_bound) {
+        } else if (max_bound - min_bound <= eps_rel * max_bound) {
             if (exact) { gjk_result(s, false, r.p1, r.p2); r.kind = GJK_CLOSEST_POINTS; }
             else r.kind = GJK_PROXIMITY;
             r.dir = dir;
@@ -629,7 +636,7 @@ NCG_DEV GjkOut gjk(const PairGeom& g, double max_dist, bool exact, Simplex& s, c
         old_dir = dir;
         proj = s.project_origin_and_reduce(tol, status);
         if (s.dim == 3) {
-            if (min_bound >= tol.eps_tol) {
+            if (min_bound >= eps_tol) {
                 if (exact) { gjk_result(s, true, r.p1, r.p2); r.kind = GJK_CLOSEST_POINTS; }
                 else r.kind = GJK_PROXIMITY;
                 r.dir = old_dir;
@@ -642,7 +649,7 @@ NCG_DEV GjkOut gjk(const PairGeom& g, double max_dist, bool exact, Simplex& s, c
         if (niter == max_iter) {
             status |= NCG_STATUS_GJK_MAX_ITER;
             r.kind = GJK_NO_INTERSECTION;
-            r.dir = mk(1.0, 0.0, 0.0);
+            r.dir = mk(real(1.0f), real(0.0f), real(0.0f));
             return r;
         }
     }

@@ -1,15 +1,19 @@
 // ncg_epa.cuh — warp-cooperative 3-D EPA (src/query/algorithms/epa3.rs:171-454).
 //
-// One warp expands one polytope.  The polytope (CSO vertices, faces with f64
-// normals, adjacency, deleted flags), the face heap and the silhouette live in
-// a bounded store: a slice of shared memory for the first pass, a slab of
-// global memory for the pairs whose polytope outgrew the shared one.
+// One warp expands one polytope.  The polytope (CSO vertices, faces,
+// adjacency, deleted flags), the face heap and the silhouette live in a
+// bounded store: a slice of shared memory for the first pass, a slab of global
+// memory for the pairs whose polytope outgrew the shared one.
+//
+// Arithmetic: the expansion (Face::new's projection of the origin, the
+// visibility test of the silhouette) runs in f32; each face normal is
+// computed in double-word from the f32 vertices and stored rounded to f32;
+// face distances, heap keys and the termination tests are double-word.
 //
 // Work split inside the warp:
 //   * support point along the popped face's normal: every lane (hull arg-max
 //     is warp-parallel, analytic maps are computed redundantly);
-//   * the new faces of one expansion step: one lane per silhouette edge
-//     (f64 triangle projection, f64 normal, f64 distance);
+//   * the new faces of one expansion step: one lane per silhouette edge;
 //   * heap push/pop, the silhouette flood fill and the ordered post-pass over
 //     the new faces: lane 0, because their order decides which face the
 //     reference pops next.  The heap is a restatement of Rust's BinaryHeap
@@ -35,9 +39,9 @@ enum EpaExit : int {
 // flood-fill stack entries.  All indices fit in 16 bits.
 struct EpaStore {
     float* v;         // [9][VC]: point xyz, orig1 xyz, orig2 xyz
-    double* fn;       // [3][FC] face normals
-    double* hkey;     // [FC] heap keys (neg_dist)
-    double* sdist;    // [SC] distance of the face built on silhouette edge k
+    float* fn;        // [3][FC] face normals
+    float* hkey;      // [2][FC] heap keys (neg_dist), double-word hi / lo
+    float* sdist;     // [2][SC] distance of the face built on silhouette edge k
     uint16_t* fpts;   // [3][FC]
     uint16_t* fadj;   // [3][FC]
     uint16_t* hid;    // [FC]
@@ -52,7 +56,7 @@ struct EpaStore {
     // Bytes needed for one store (each array padded to 16 bytes).
     static __host__ __device__ size_t bytes(int VC, int FC, int SC, int TC) {
         auto r = [](size_t b) { return (b + 15) & ~size_t(15); };
-        return r(9 * 4 * (size_t)VC) + r(3 * 8 * (size_t)FC) + r(8 * (size_t)FC) + r(8 * (size_t)SC) +
+        return r(9 * 4 * (size_t)VC) + r(3 * 4 * (size_t)FC) + r(8 * (size_t)FC) + r(8 * (size_t)SC) +
                r(3 * 2 * (size_t)FC) + r(3 * 2 * (size_t)FC) + r(2 * (size_t)FC) + r(2 * (size_t)SC) +
                r(2 * (size_t)TC) + r((size_t)FC) + r((size_t)SC) + r((size_t)TC) + r((size_t)SC);
     }
@@ -61,9 +65,9 @@ struct EpaStore {
         auto r = [](size_t b) { return (b + 15) & ~size_t(15); };
         char* p = base;
         v = (float*)p; p += r(9 * 4 * (size_t)VC);
-        fn = (double*)p; p += r(3 * 8 * (size_t)FC);
-        hkey = (double*)p; p += r(8 * (size_t)FC);
-        sdist = (double*)p; p += r(8 * (size_t)SC);
+        fn = (float*)p; p += r(3 * 4 * (size_t)FC);
+        hkey = (float*)p; p += r(8 * (size_t)FC);
+        sdist = (float*)p; p += r(8 * (size_t)SC);
         fpts = (uint16_t*)p; p += r(3 * 2 * (size_t)FC);
         fadj = (uint16_t*)p; p += r(3 * 2 * (size_t)FC);
         hid = (uint16_t*)p; p += r(2 * (size_t)FC);
@@ -75,9 +79,10 @@ struct EpaStore {
         sflag = (uint8_t*)p;
     }
 
-    NCG_DEV vec3<double> vp(int i) const { return {(double)v[i], (double)v[VC + i], (double)v[2 * VC + i]}; }
-    NCG_DEV vec3<double> vo1(int i) const { return {(double)v[3 * VC + i], (double)v[4 * VC + i], (double)v[5 * VC + i]}; }
-    NCG_DEV vec3<double> vo2(int i) const { return {(double)v[6 * VC + i], (double)v[7 * VC + i], (double)v[8 * VC + i]}; }
+    NCG_DEV vec3<float> vf(int i) const { return {v[i], v[VC + i], v[2 * VC + i]}; }
+    NCG_DEV vec3<real> vp(int i) const { return to_r(vf(i)); }
+    NCG_DEV vec3<real> vo1(int i) const { return {real(v[3 * VC + i]), real(v[4 * VC + i]), real(v[5 * VC + i])}; }
+    NCG_DEV vec3<real> vo2(int i) const { return {real(v[6 * VC + i]), real(v[7 * VC + i]), real(v[8 * VC + i])}; }
     NCG_DEV void put_vertex(int i, const CSO& c) {
         v[i] = c.p.x; v[VC + i] = c.p.y; v[2 * VC + i] = c.p.z;
         v[3 * VC + i] = c.o1.x; v[4 * VC + i] = c.o1.y; v[5 * VC + i] = c.o1.z;
@@ -90,33 +95,37 @@ struct EpaStore {
     NCG_DEV int pt(int f, int k) const { return fpts[k * FC + f]; }
     NCG_DEV int adj(int f, int k) const { return fadj[k * FC + f]; }
     NCG_DEV void set_adj(int f, int k, int a) { fadj[k * FC + f] = (uint16_t)a; }
-    NCG_DEV vec3<double> normal(int f) const { return {fn[f], fn[FC + f], fn[2 * FC + f]}; }
+    NCG_DEV vec3<float> normalf(int f) const { return {fn[f], fn[FC + f], fn[2 * FC + f]}; }
+    NCG_DEV vec3<real> normal(int f) const { return to_r(normalf(f)); }
+    NCG_DEV real key(int h) const { return real(hkey[h], hkey[FC + h]); }
 
     // Face::new (epa3.rs:96-115) + ccw_face_normal (utils/ccw_face_normal.rs:21-27).
     // Writes face f; returns whether the origin projects inside; dist = n . pts[0].
-    NCG_DEV bool build_face(int f, int p0, int p1, int p2, int a0, int a1, int a2, double eps, double& dist) {
-        vec3<double> A = vp(p0), B = vp(p1), C = vp(p2);
-        Loc loc;
-        (void)proj_triangle(A, B, C, loc);
-        vec3<double> n, u;
-        double len;
-        if (try_normalize(cross(B - A, C - A), eps, u, len)) n = u;
-        else n = zero3<double>();
+    NCG_DEV bool build_face(int f, int p0, int p1, int p2, int a0, int a1, int a2, real eps, real& dist) {
+        vec3<float> Af = vf(p0), Bf = vf(p1), Cf = vf(p2);
+        Loc<float> loc;
+        (void)proj_triangle(Af, Bf, Cf, loc);
+        vec3<real> A = to_r(Af);
+        vec3<real> u;
+        real len;
+        vec3<float> n;
+        if (try_normalize(cross(to_r(Bf) - A, to_r(Cf) - A), eps, u, len)) n = to_f(u);
+        else n = zero3<float>();
         fpts[f] = (uint16_t)p0; fpts[FC + f] = (uint16_t)p1; fpts[2 * FC + f] = (uint16_t)p2;
         fadj[f] = (uint16_t)a0; fadj[FC + f] = (uint16_t)a1; fadj[2 * FC + f] = (uint16_t)a2;
         fn[f] = n.x; fn[FC + f] = n.y; fn[2 * FC + f] = n.z;
         fdel[f] = 0;
-        dist = dot(n, A);
+        dist = dot(to_r(n), A);
         return loc.kind == LOC_FACE;
     }
     // Face::closest_points with the barycentric coordinates Face::new stored
     // (recomputed: the projection is a pure function of the three vertices).
-    NCG_DEV void face_points(int f, vec3<double>& p1, vec3<double>& p2) const {
+    NCG_DEV void face_points(int f, vec3<real>& p1, vec3<real>& p2) const {
         int a = pt(f, 0), b = pt(f, 1), c = pt(f, 2);
-        Loc loc;
-        (void)proj_triangle(vp(a), vp(b), vp(c), loc);
-        double b0 = 0.0, b1 = 0.0, b2 = 0.0;
-        if (loc.kind == LOC_FACE) { b0 = loc.b0; b1 = loc.b1; b2 = loc.b2; }
+        Loc<float> loc;
+        (void)proj_triangle(vf(a), vf(b), vf(c), loc);
+        real b0(0.0f), b1(0.0f), b2(0.0f);
+        if (loc.kind == LOC_FACE) { b0 = real(loc.b0); b1 = real(loc.b1); b2 = real(loc.b2); }
         p1 = (vo1(a) * b0 + vo1(b) * b1) + vo1(c) * b2;
         p2 = (vo2(a) * b0 + vo2(b) * b1) + vo2(c) * b2;
     }
@@ -125,55 +134,61 @@ struct EpaStore {
         if (pt(f, 1) == id) return 2;
         return 0;
     }
-    // epa3.rs:143-156 and utils/triangle.rs:85-102.
+    // epa3.rs:143-156 and utils/triangle.rs:85-102 (f32).
     NCG_DEV bool seen_by(int f, int point, int opp, const Tol& tol) const {
-        vec3<double> p0 = vp(pt(f, opp)), p1 = vp(pt(f, (opp + 1) % 3)), p2 = vp(pt(f, (opp + 2) % 3));
-        vec3<double> q = vp(point);
-        if (dot(q - p0, normal(f)) >= -tol.eps_tol) return true;
-        double x = norm_sq(cross(p2 - p1, q - p1));
-        return x == 0.0 || fabs(x) <= tol.affine_eps;
+        vec3<float> p0 = vf(pt(f, opp)), p1 = vf(pt(f, (opp + 1) % 3)), p2 = vf(pt(f, (opp + 2) % 3));
+        vec3<float> q = vf(point);
+        if (dot(q - p0, normalf(f)) >= -tol.eps_tol_f) return true;
+        float x = norm_sq(cross(p2 - p1, q - p1));
+        return x == 0.0f || fabsf(x) <= tol.affine_eps_f;
     }
 
     // ---- Rust BinaryHeap<FaceId> (max-heap on neg_dist) — lane 0 only.
-    NCG_DEV void heap_sift_up(int start, int pos, int id, double key) {
-        while (pos > start) {
-            int parent = (pos - 1) / 2;
-            if (key <= hkey[parent]) break;
-            hkey[pos] = hkey[parent];
-            hid[pos] = hid[parent];
-            pos = parent;
-        }
-        hkey[pos] = key;
+    NCG_DEV void hput(int pos, int id, real k) {
+        hkey[pos] = k.h;
+        hkey[FC + pos] = k.l;
         hid[pos] = (uint16_t)id;
     }
-    NCG_DEV void heap_push(int& size, int id, double key) {
-        int pos = size++;
-        heap_sift_up(0, pos, id, key);
+    NCG_DEV void hmove(int dst, int src) {
+        hkey[dst] = hkey[src];
+        hkey[FC + dst] = hkey[FC + src];
+        hid[dst] = hid[src];
     }
-    NCG_DEV bool heap_pop(int& size, int& id, double& key) {
+    NCG_DEV void heap_sift_up(int start, int pos, int id, real k) {
+        while (pos > start) {
+            int parent = (pos - 1) / 2;
+            if (k <= key(parent)) break;
+            hmove(pos, parent);
+            pos = parent;
+        }
+        hput(pos, id, k);
+    }
+    NCG_DEV void heap_push(int& size, int id, real k) {
+        int pos = size++;
+        heap_sift_up(0, pos, id, k);
+    }
+    NCG_DEV bool heap_pop(int& size, int& id, real& k) {
         if (size == 0) return false;
         size--;
         int lid = hid[size];
-        double lkey = hkey[size];
+        real lkey = key(size);
         if (size == 0) {
             id = lid;
-            key = lkey;
+            k = lkey;
             return true;
         }
         id = hid[0];
-        key = hkey[0];
+        k = key(0);
         // sift_down_to_bottom(0) with the former last element in the hole.
         int end = size, pos = 0, child = 1;
         while (end >= 2 && child <= end - 2) {
-            child += (hkey[child] <= hkey[child + 1]) ? 1 : 0;
-            hkey[pos] = hkey[child];
-            hid[pos] = hid[child];
+            child += (key(child) <= key(child + 1)) ? 1 : 0;
+            hmove(pos, child);
             pos = child;
             child = 2 * pos + 1;
         }
         if (child == end - 1) {
-            hkey[pos] = hkey[child];
-            hid[pos] = hid[child];
+            hmove(pos, child);
             pos = child;
         }
         heap_sift_up(0, pos, lid, lkey);
@@ -183,13 +198,15 @@ struct EpaStore {
 
 struct EpaResult {
     int exit;
-    vec3<double> p1, p2, n;
+    vec3<real> p1, p2, n;
     uint32_t iters;
     uint32_t status;
 };
 
 NCG_DEV int bcast(int x) { return __shfl_sync(0xffffffffu, x, 0); }
-NCG_DEV double bcastd(double x) { return __shfl_sync(0xffffffffu, x, 0); }
+NCG_DEV real bcastr(real x) {
+    return real(__shfl_sync(0xffffffffu, x.h, 0), __shfl_sync(0xffffffffu, x.l, 0));
+}
 
 // EPA::closest_points.  Called by all 32 lanes of a warp with identical
 // arguments; every lane returns the same result.
@@ -199,25 +216,26 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
     const int lane = threadIdx.x & 31;
     EpaResult res;
     res.exit = EPA_NONE;
-    res.p1 = res.p2 = res.n = zero3<double>();
+    res.p1 = res.p2 = res.n = zero3<real>();
     res.iters = 0;
     res.status = 0;
 
     if (dim == 0) {
-        res.n = mk(0.0, 1.0, 0.0);
+        res.n = mk(real(0.0f), real(1.0f), real(0.0f));
         res.exit = EPA_OK_DIM0;
         return res;
     }
     int nv = dim + 1, nf = 0, hsize = 0;
+    const real eps = from_host(tol.eps), eps_tol = from_host(tol.eps_tol), epa_tol = from_host(tol.epa_eps_tol);
     if (lane == 0)
         for (int i = 0; i < nv; ++i) st.put_vertex(i, sv[i]);
     __syncwarp();
 
     if (dim == 3) {
-        vec3<double> v0 = st.vp(0);
-        vec3<double> dp1 = st.vp(1) - v0, dp2 = st.vp(2) - v0, dp3 = st.vp(3) - v0;
+        vec3<real> v0 = st.vp(0);
+        vec3<real> dp1 = st.vp(1) - v0, dp2 = st.vp(2) - v0, dp3 = st.vp(3) - v0;
         __syncwarp();
-        if (dot(cross(dp1, dp2), dp3) > 0.0) {
+        if (dot(cross(dp1, dp2), dp3) > real(0.0f)) {
             if (lane == 0) {
                 CSO a = st.get_vertex(1), b = st.get_vertex(2);
                 st.put_vertex(1, b);
@@ -228,10 +246,10 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
         // Faces [0,1,2] [1,3,2] [0,2,3] [0,3,1], adjacency per epa3.rs:256-264; lanes 0..3.
         const int P[4][3] = {{0, 1, 2}, {1, 3, 2}, {0, 2, 3}, {0, 3, 1}};
         const int A[4][3] = {{3, 1, 2}, {3, 2, 0}, {0, 1, 3}, {2, 1, 0}};
-        double d = 0.0;
+        real d;
         bool inside = false;
         if (lane < 4) inside = st.build_face(lane, P[lane][0], P[lane][1], P[lane][2], A[lane][0], A[lane][1],
-                                             A[lane][2], tol.eps, d);
+                                             A[lane][2], eps, d);
         unsigned ins = __ballot_sync(0xffffffffu, inside);
         __syncwarp();
         int fail = 0;
@@ -239,8 +257,8 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
             for (int k = 0; k < 4; ++k) {
                 if (!(ins >> k & 1u)) continue;
                 // dist_k = normal_k . vertices[k] (epa3.rs:277,282,287,292)
-                double dk = dot(st.normal(k), st.vp(k));
-                if (-dk > tol.eps_tol) { fail = 1; break; }
+                real dk = dot(st.normal(k), st.vp(k));
+                if (-dk > eps_tol) { fail = 1; break; }
                 st.heap_push(hsize, k, -dk);
             }
         }
@@ -251,22 +269,22 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
         if (fail) { res.exit = EPA_NONE; res.status |= NCG_STATUS_EPA_FAILED; return res; }
     } else {
         if (dim == 1) {
-            vec3<double> dpt = st.vp(1) - st.vp(0);
-            vec3<double> a = fabs(dpt.x) > fabs(dpt.y) ? mk(dpt.z, 0.0, -dpt.x) : mk(0.0, -dpt.z, dpt.y);
+            vec3<real> dpt = st.vp(1) - st.vp(0);
+            vec3<real> a = fabs(dpt.x) > fabs(dpt.y) ? mk(dpt.z, real(0.0f), -dpt.x) : mk(real(0.0f), -dpt.z, dpt.y);
             a = a / vnorm(a);
-            vec3<double> dir = cross(a, dpt);
+            vec3<real> dir = cross(a, dpt);
             CSO c = cso_support(g, to_f(dir), scan);
             if (lane == 0) st.put_vertex(2, c);
             nv = 3;
             __syncwarp();
         }
-        double d;
-        if (lane == 0) (void)st.build_face(0, 0, 1, 2, 1, 1, 1, tol.eps, d);
-        if (lane == 1) (void)st.build_face(1, 0, 2, 1, 0, 0, 0, tol.eps, d);
+        real d;
+        if (lane == 0) (void)st.build_face(0, 0, 1, 2, 1, 1, 1, eps, d);
+        if (lane == 1) (void)st.build_face(1, 0, 2, 1, 0, 0, 0, eps, d);
         __syncwarp();
         if (lane == 0) {
-            st.heap_push(hsize, 0, 0.0);
-            st.heap_push(hsize, 1, 0.0);
+            st.heap_push(hsize, 0, real(0.0f));
+            st.heap_push(hsize, 1, real(0.0f));
         }
         hsize = 2;
         nf = 2;
@@ -278,22 +296,22 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
         return res;
     }
     int best = bcast(lane == 0 ? (int)st.hid[0] : 0);
-    double max_dist = DBL_MAX;
+    real max_dist = dw_max();
     int niter = 0;
 
     for (;;) {
         // ---- pop the closest non-deleted face (lane 0)
         int fid = -1;
-        double key = 0.0;
+        real key(0.0f);
         if (lane == 0) {
             int id;
-            double k;
+            real k;
             while (st.heap_pop(hsize, id, k)) {
                 if (!st.fdel[id]) { fid = id; key = k; break; }
             }
         }
         fid = bcast(fid);
-        key = bcastd(key);
+        key = bcastr(key);
         hsize = bcast(hsize);
         if (fid < 0) {
             st.face_points(best, res.p1, res.p2);
@@ -302,19 +320,20 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
             return res;
         }
         res.iters++;
-        vec3<double> fnrm = st.normal(fid);
-        CSO c = cso_support(g, to_f(fnrm), scan);
+        vec3<float> fnf = st.normalf(fid);
+        vec3<real> fnrm = to_r(fnf);
+        CSO c = cso_support(g, fnf, scan);
         if (nv >= st.VC) { res.exit = EPA_OVERFLOW; return res; }
         const int sup = nv++;
         if (lane == 0) st.put_vertex(sup, c);
-        double cand = dot(to_d(c.p), fnrm);
+        real cand = dot(to_r(c.p), fnrm);
         if (cand < max_dist) {
             best = fid;
             max_dist = cand;
         }
-        double curr = -key;
+        real curr = -key;
         __syncwarp();
-        if (max_dist - curr < tol.epa_eps_tol) {
+        if (max_dist - curr < epa_tol) {
             st.face_points(best, res.p1, res.p2);
             res.n = st.normal(best);
             res.exit = EPA_OK_CONVERGED;
@@ -385,9 +404,10 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
             if (first_new + built + __popc(m) > st.FC) { ovf = 1; }
             if (live && !ovf) {
                 int q1 = st.pt(sf, (so + 2) % 3), q2 = st.pt(sf, (so + 1) % 3);
-                double dist;
-                bool in = st.build_face(id, q1, q2, sup, sf, id + 1, id - 1, tol.eps, dist);
-                st.sdist[k] = dist;
+                real dist;
+                bool in = st.build_face(id, q1, q2, sup, sf, id + 1, id - 1, eps, dist);
+                st.sdist[k] = dist.h;
+                st.sdist[st.SC + k] = dist.l;
                 st.sflag[k] = (uint8_t)(1 | (in ? 2 : 0));
             } else if (k < nsil) {
                 st.sflag[k] = 0;
@@ -407,9 +427,9 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
                 int sf = st.sface[k], so = st.sopp[k];
                 st.set_adj(sf, (so + 1) % 3, id);
                 if (fl & 2) {
-                    double dist = st.sdist[k];
+                    real dist(st.sdist[k], st.sdist[st.SC + k]);
                     if (dist < curr) { outcome = 1; break; }
-                    if (-dist > tol.eps_tol) { outcome = 2; break; }
+                    if (-dist > eps_tol) { outcome = 2; break; }
                     st.heap_push(hsize, id, -dist);
                 }
                 id++;

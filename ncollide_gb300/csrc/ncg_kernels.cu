@@ -6,10 +6,12 @@
 //   2. gjk_thread   1 thread/pair over the analytic list (persistent grid).
 //   3. gjk_warp     1 warp/pair over the hull list (dynamic queue); the hull
 //                   arg-max is warp-parallel with coalesced 128-bit loads.
-//   4. epa_shared   contact only: 1 warp per intersecting pair, polytope in
-//                   shared memory (dynamic queue).
-//   5. epa_global   contact only: pairs whose polytope outgrew shared memory,
-//                   re-run with a polytope in a global-memory slab per warp.
+//   4. epa tier A   contact only: 1 warp per intersecting pair, polytope of up
+//                   to 128 vertices in shared memory (~9 warps per SM).
+//   5. epa tier B   pairs whose polytope outgrew tier A, re-run with up to
+//                   1024 vertices in shared memory (1 warp per SM).
+//   6. epa tier C   pairs that outgrew tier B, re-run in a global-memory slab
+//                   per warp (up to 10240 vertices).
 // Pairs are independent; the GJK stage writes its outputs directly or appends
 // the final simplex to the EPA queue.
 #include <cuda_runtime.h>
@@ -49,7 +51,7 @@ struct QueryParams {
     int use_init_dir;
     int gjk_max_iter;
     int epa_max_iter;
-    double param;  // prediction / margin (f64 copy of the f32 argument)
+    dw_host param;  // prediction / margin
     Tol tol;
 };
 
@@ -63,16 +65,18 @@ struct __align__(16) EpaItem {
 };
 
 struct DevCounters {
-    unsigned long long n_analytic, n_hull, epa_count, ovf_count;
-    unsigned long long hull_next, epa_next, ovf_next;
+    unsigned long long n_analytic, n_hull;
+    unsigned long long hull_next;
+    unsigned long long epa_count[3];  // items queued for tier A (all), B, C
+    unsigned long long epa_next[3];
     unsigned long long gjk_iters, epa_iters;
-    unsigned long long pad[7];
+    unsigned long long pad[5];
 };
 
 struct Scratch {
     uint32_t* analytic;
     uint32_t* hull;
-    uint32_t* ovf;
+    uint32_t* ovf[3];  // ovf[1]: items for tier B, ovf[2]: items for tier C
     EpaItem* items;
     DevCounters* ctr;
     char* slabs;
@@ -80,18 +84,22 @@ struct Scratch {
     int n_slabs;
 };
 
-// Global-memory EPA store capacities (overflow pass).
-constexpr int G_VC = 10240, G_FC = 65535, G_SC = 4096, G_TC = 16384;
-// Shared-memory EPA store capacities (first pass).
-constexpr int S_VC = 64, S_FC = 256, S_SC = 64, S_TC = 128;
-constexpr int EPA_WARPS = 2;  // warps per block in epa_shared
+// EPA store capacities per tier: vertices, faces, silhouette edges, flood-fill stack.
+template <int T> struct EpaTier;
+template <> struct EpaTier<0> { static constexpr int VC = 128, FC = 512, SC = 64, TC = 256; };
+template <> struct EpaTier<1> { static constexpr int VC = 1024, FC = 4096, SC = 512, TC = 2048; };
+template <> struct EpaTier<2> { static constexpr int VC = 10240, FC = 65535, SC = 4096, TC = 16384; };
+template <int T> size_t tier_bytes() {
+    return EpaStore::bytes(EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC);
+}
 
 NCG_DEV uint32_t pack_iters(uint32_t g, uint32_t e) { return (g > 0xffffu ? 0xffffu : g) | ((e > 0xffffu ? 0xffffu : e) << 16); }
 
-NCG_DEV void wr3(float* p, vec3<double> v) {
-    p[0] = (float)v.x;
-    p[1] = (float)v.y;
-    p[2] = (float)v.z;
+// Results leave the device as the high word of each double-word.
+NCG_DEV void wr3(float* p, vec3<real> v) {
+    p[0] = v.x.h;
+    p[1] = v.y.h;
+    p[2] = v.z.h;
 }
 
 // Writes the outputs of a finished pair (every query except an EPA-bound contact).
@@ -107,7 +115,7 @@ NCG_DEV void write_outputs(const QueryParams& qp, const Outputs& o, uint32_t i, 
             wr3(c.world1, r.p1);
             wr3(c.world2, r.p2);
             wr3(c.normal, r.dir);
-            c.depth = (float)(-dot(r.dir, r.p2 - r.p1));
+            c.depth = (-dot(r.dir, r.p2 - r.p1)).h;
         }
         o.contact[i] = c;
         o.tag[i] = tag;
@@ -115,7 +123,7 @@ NCG_DEV void write_outputs(const QueryParams& qp, const Outputs& o, uint32_t i, 
         break;
     }
     case Q_DISTANCE:
-        o.value[i] = r.kind == GJK_CLOSEST_POINTS ? (float)vnorm(r.p2 - r.p1) : 0.0f;
+        o.value[i] = r.kind == GJK_CLOSEST_POINTS ? vnorm(r.p2 - r.p1).h : 0.0f;
         break;
     case Q_PROXIMITY: {
         uint8_t t = r.kind == GJK_INTERSECTION ? NCG_INTERSECTING
@@ -151,7 +159,7 @@ NCG_DEV void write_outputs(const QueryParams& qp, const Outputs& o, uint32_t i, 
 NCG_DEV void write_bad(const QueryParams& qp, const Outputs& o, uint32_t i) {
     GjkOut r;
     r.kind = GJK_NO_INTERSECTION;
-    r.p1 = r.p2 = r.dir = zero3<double>();
+    r.p1 = r.p2 = r.dir = zero3<real>();
     write_outputs(qp, o, i, r, zero3<float>(), NCG_STATUS_BAD_INPUT, 0);
 }
 
@@ -190,13 +198,13 @@ NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& 
     Simplex sx;
     sx.reset(cso_support(g, d, scan));
     uint32_t iters = 0, status = 0;
-    double max_dist = qp.query == Q_DISTANCE ? DBL_MAX : qp.param;
+    real max_dist = qp.query == Q_DISTANCE ? dw_max() : from_host(qp.param);
     bool exact = qp.query != Q_PROXIMITY;
     GjkOut r = gjk(g, max_dist, exact, sx, qp.tol, scan, iters, status, qp.gjk_max_iter);
     iter_acc += iters;
     if (qp.query == Q_CONTACT && r.kind == GJK_INTERSECTION) {
         if (writer) {
-            unsigned long long slot = atomicAdd(&s.ctr->epa_count, 1ull);
+            unsigned long long slot = atomicAdd(&s.ctr->epa_count[0], 1ull);
             EpaItem& it = s.items[slot];
             it.pair = i;
             it.gjk_iters = iters;
@@ -282,13 +290,13 @@ NCG_DEV void write_epa(const Outputs& o, const EpaItem& it, const EpaResult& r, 
     ncg_contact c;
     memset(&c, 0, sizeof(c));
     uint8_t tag = 0;
-    vec3<double> dir = mk(1.0, 0.0, 0.0);
+    vec3<real> dir = mk(real(1.0f), real(0.0f), real(0.0f));
     if (r.exit >= EPA_OK_DIM0 && r.exit <= EPA_OK_HEAP_EMPTY) {
         tag = 1;
         wr3(c.world1, r.p1);
         wr3(c.world2, r.p2);
         wr3(c.normal, r.n);
-        c.depth = (float)(-dot(r.n, r.p2 - r.p1));
+        c.depth = (-dot(r.n, r.p2 - r.p1)).h;
         dir = r.n;
     }
     o.contact[i] = c;
@@ -314,66 +322,51 @@ NCG_DEV void load_simplex(const EpaItem& it, CSO* sv) {
     }
 }
 
-__global__ void __launch_bounds__(EPA_WARPS * 32) k_epa_shared(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+// EPA tier T: tiers 0 and 1 keep the polytope in dynamic shared memory (one
+// warp per block), tier 2 in a global-memory slab per warp.  A pair whose
+// polytope outgrows its tier is queued for the next tier and re-run there from
+// GJK's simplex; at tier 2 it ends with NCG_STATUS_EPA_CAPACITY.
+template <int T>
+__global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
     extern __shared__ __align__(16) char smem[];
-    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const unsigned lane = threadIdx.x & 31u;
+    using C = EpaTier<T>;
     EpaStore st;
-    const size_t bytes = EpaStore::bytes(S_VC, S_FC, S_SC, S_TC);
-    st.carve(smem + warp * bytes, S_VC, S_FC, S_SC, S_TC);
-    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count;
+    if (T < 2) {
+        st.carve(smem, C::VC, C::FC, C::SC, C::TC);
+    } else {
+        if (blockIdx.x >= (unsigned)s.n_slabs) return;
+        st.carve(s.slabs + (size_t)blockIdx.x * s.slab_bytes, C::VC, C::FC, C::SC, C::TC);
+    }
+    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[T];
     WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     unsigned long long acc = 0;
     for (;;) {
         unsigned long long k = 0;
-        if (lane == 0) k = atomicAdd(&s.ctr->epa_next, 1ull);
+        if (lane == 0) k = atomicAdd(&s.ctr->epa_next[T], 1ull);
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= n) break;
-        const EpaItem& it = s.items[k];
+        const uint32_t item = T == 0 ? (uint32_t)k : s.ovf[T][k];
+        const EpaItem& it = s.items[item];
         PairGeom g = load_geom(b, it.pair);
         CSO sv[4];
         load_simplex(it, sv);
         EpaResult r = epa_warp(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
-        if (r.exit == EPA_OVERFLOW) {
+        if (r.exit == EPA_OVERFLOW && T < 2) {
             if (lane == 0) {
-                unsigned long long q = atomicAdd(&s.ctr->ovf_count, 1ull);
-                s.ovf[q] = (uint32_t)k;
+                unsigned long long q = atomicAdd(&s.ctr->epa_count[T + 1], 1ull);
+                s.ovf[T + 1][q] = item;
             }
         } else {
             acc += r.iters;
-            if (lane == 0) write_epa(o, it, r, 0);
-        }
-        __syncwarp();
-    }
-    if (lane == 0 && acc) atomicAdd(&s.ctr->epa_iters, acc);
-}
-
-__global__ void __launch_bounds__(128) k_epa_global(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (gw >= (unsigned)s.n_slabs) return;
-    EpaStore st;
-    st.carve(s.slabs + (size_t)gw * s.slab_bytes, G_VC, G_FC, G_SC, G_TC);
-    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->ovf_count;
-    WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
-    unsigned long long acc = 0;
-    for (;;) {
-        unsigned long long k = 0;
-        if (lane == 0) k = atomicAdd(&s.ctr->ovf_next, 1ull);
-        k = __shfl_sync(0xffffffffu, k, 0);
-        if (k >= n) break;
-        const EpaItem& it = s.items[s.ovf[k]];
-        PairGeom g = load_geom(b, it.pair);
-        CSO sv[4];
-        load_simplex(it, sv);
-        EpaResult r = epa_warp(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
-        acc += r.iters;
-        if (lane == 0) {
-            if (r.exit == EPA_OVERFLOW) {
-                EpaResult none = r;
-                none.exit = EPA_NONE;
-                write_epa(o, it, none, NCG_STATUS_EPA_CAPACITY);
-            } else {
-                write_epa(o, it, r, 0);
+            if (lane == 0) {
+                if (r.exit == EPA_OVERFLOW) {
+                    EpaResult none = r;
+                    none.exit = EPA_NONE;
+                    write_epa(o, it, none, NCG_STATUS_EPA_CAPACITY);
+                } else {
+                    write_epa(o, it, r, 0);
+                }
             }
         }
         __syncwarp();
@@ -388,15 +381,31 @@ bool cuda_ok(cudaError_t e, const char* what) {
     return false;
 }
 
+// Tolerance constants in f64, split into double-words.
+// REFERENCE: the reference's own f32 constants (eps = f32::EPSILON).
+// PRECISE: the tests that classify (origin on the simplex, origin inside the
+// tetrahedron, EPA face checks and visibility) keep f32::EPSILON, the noise
+// floor of f32 support points; the tests that decide how far GJK refines
+// (add_point's degeneracy threshold, the relative gap sqrt(10 eps)) use
+// f64::EPSILON as the reference built with f64; EPA terminates at 1e-6
+// absolute (the f64 reference's 100 eps is below f32 support noise).
 Tol make_tol(int mode) {
     Tol t;
-    double e = mode == NCG_TOL_PRECISE ? (double)DBL_EPSILON : (double)FLT_EPSILON;
-    t.eps = e;
-    t.eps_tol = e * 10.0;
-    t.eps_rel = std::sqrt(t.eps_tol);
-    t.epa_eps_tol = mode == NCG_TOL_PRECISE ? 1e-6 : e * 100.0;
+    double e = (double)FLT_EPSILON;
+    t.eps = dw_split(e);
+    t.eps_tol = dw_split(e * 10.0);
+    t.eps_rel = dw_split(std::sqrt(e * 10.0));
+    t.epa_eps_tol = dw_split(e * 100.0);
     double a = e * 100.0;
-    t.affine_eps = a * a;
+    t.affine_eps = dw_split(a * a);
+    t.add_tol = t.eps_tol;
+    if (mode == NCG_TOL_PRECISE) {
+        t.eps_rel = dw_split(std::sqrt(10.0 * (double)DBL_EPSILON));
+        t.add_tol = dw_split(10.0 * (double)DBL_EPSILON);
+        t.epa_eps_tol = dw_split(1e-6);
+    }
+    t.eps_tol_f = t.eps_tol.h;
+    t.affine_eps_f = t.affine_eps.h;
     t.init_eps = FLT_EPSILON;
     return t;
 }
@@ -408,7 +417,7 @@ struct ncg_ctx {
     int num_sms = 0;
     int tol_mode = NCG_TOL_REFERENCE;
     int warm = NCG_WARM_NONE;
-    int occ_thread = 1, occ_warp = 1, occ_epa = 1, occ_classify = 1;
+    int occ_thread = 1, occ_warp = 1, occ_epa0 = 1, occ_epa1 = 1;
     char* scratch = nullptr;
     size_t scratch_cap_pairs = 0;
     char* slabs = nullptr;
@@ -421,6 +430,10 @@ struct ncg_ctx {
     char* stage = nullptr;
     size_t stage_cap = 0;
     cudaStream_t own_stream = nullptr;
+    int profiling = 0;
+    int n_marks = 0;
+    int mark_stage[NCG_N_STAGES + 1];
+    cudaEvent_t marks[NCG_N_STAGES + 1] = {};
 };
 
 namespace {
@@ -430,7 +443,7 @@ bool ensure_scratch(ncg_ctx* c, uint64_t n) {
     if (c->scratch) cudaFree(c->scratch);
     c->scratch = nullptr;
     uint64_t cap = n < 1024 ? 1024 : n;
-    size_t bytes = 3 * 4 * cap + sizeof(EpaItem) * cap + sizeof(DevCounters) + 1024;
+    size_t bytes = 4 * 4 * cap + sizeof(EpaItem) * cap + sizeof(DevCounters) + 1024;
     if (!cuda_ok(cudaMalloc(&c->scratch, bytes), "cudaMalloc(scratch)")) return false;
     c->scratch_cap_pairs = cap;
     return true;
@@ -444,7 +457,9 @@ Scratch carve_scratch(ncg_ctx* c) {
     s.items = (EpaItem*)p; p += sizeof(EpaItem) * cap;
     s.analytic = (uint32_t*)p; p += 4 * cap;
     s.hull = (uint32_t*)p; p += 4 * cap;
-    s.ovf = (uint32_t*)p;
+    s.ovf[0] = nullptr;
+    s.ovf[1] = (uint32_t*)p; p += 4 * cap;
+    s.ovf[2] = (uint32_t*)p;
     s.slabs = c->slabs;
     s.slab_bytes = c->slab_bytes;
     s.n_slabs = c->n_slabs;
@@ -467,24 +482,34 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     qp.use_init_dir = (c->warm == NCG_WARM_INIT_DIR && b->init_dir) ? 1 : 0;
     qp.gjk_max_iter = 10000;
     qp.epa_max_iter = 10000;
-    qp.param = (double)param;
+    qp.param = dw_split((double)param);
     qp.tol = make_tol(c->tol_mode);
     ncg_batch bb = *b;
     uint32_t launches = 0;
+    c->n_marks = 0;
+    auto mark = [&](int stage) {
+        if (!c->profiling) return;
+        c->mark_stage[c->n_marks] = stage;
+        cudaEventRecord(c->marks[c->n_marks++], st);
+    };
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset counters")) return NCG_ECUDA;
     unsigned n = (unsigned)b->n_pairs;
+    mark(-1);
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
-    launches++;
+    mark(0);
     k_gjk_thread<<<c->num_sms * c->occ_thread, 128, 0, st>>>(bb, qp, o, s);
-    launches++;
+    mark(1);
     k_gjk_warp<<<c->num_sms * c->occ_warp, 128, 0, st>>>(bb, qp, o, s);
-    launches++;
+    mark(2);
+    launches += 3;
     if (query == Q_CONTACT) {
-        size_t smem = EPA_WARPS * EpaStore::bytes(S_VC, S_FC, S_SC, S_TC);
-        k_epa_shared<<<c->num_sms * c->occ_epa, EPA_WARPS * 32, smem, st>>>(bb, qp, o, s);
-        launches++;
-        k_epa_global<<<(c->n_slabs * 32 + 127) / 128, 128, 0, st>>>(bb, qp, o, s);
-        launches++;
+        k_epa<0><<<c->num_sms * c->occ_epa0, 32, tier_bytes<0>(), st>>>(bb, qp, o, s);
+        mark(3);
+        k_epa<1><<<c->num_sms * c->occ_epa1, 32, tier_bytes<1>(), st>>>(bb, qp, o, s);
+        mark(4);
+        k_epa<2><<<c->n_slabs, 32, 0, st>>>(bb, qp, o, s);
+        mark(5);
+        launches += 3;
     }
     if (!cuda_ok(cudaGetLastError(), "kernel launch")) return NCG_ECUDA;
     if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st),
@@ -512,15 +537,17 @@ int ncg_ctx_create(ncg_ctx** out, int device) {
     ncg_ctx* c = new ncg_ctx();
     c->device = device;
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-    size_t smem = EPA_WARPS * EpaStore::bytes(S_VC, S_FC, S_SC, S_TC);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_epa_shared, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_epa<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<0>());
+    cudaFuncSetAttribute(k_epa<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<1>());
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_thread, k_gjk_thread, 128, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_warp, k_gjk_warp, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa, k_epa_shared, EPA_WARPS * 32, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa0, k_epa<0>, 32, tier_bytes<0>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa1, k_epa<1>, 32, tier_bytes<1>());
     if (c->occ_thread < 1) c->occ_thread = 1;
     if (c->occ_warp < 1) c->occ_warp = 1;
-    if (c->occ_epa < 1) c->occ_epa = 1;
-    c->slab_bytes = (EpaStore::bytes(G_VC, G_FC, G_SC, G_TC) + 255) & ~size_t(255);
+    if (c->occ_epa0 < 1) c->occ_epa0 = 1;
+    if (c->occ_epa1 < 1) c->occ_epa1 = 1;
+    c->slab_bytes = (tier_bytes<2>() + 255) & ~size_t(255);
     c->n_slabs = c->num_sms;
     if (!cuda_ok(cudaMalloc(&c->slabs, c->slab_bytes * c->n_slabs), "cudaMalloc(slabs)") ||
         !cuda_ok(cudaMallocHost(&c->host_ctr, sizeof(DevCounters)), "cudaMallocHost")) {
@@ -540,6 +567,8 @@ int ncg_ctx_destroy(ncg_ctx* c) {
     if (c->stage) cudaFree(c->stage);
     if (c->host_ctr) cudaFreeHost(c->host_ctr);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    for (int i = 0; i <= NCG_N_STAGES; ++i)
+        if (c->marks[i]) cudaEventDestroy(c->marks[i]);
     delete c;
     return NCG_OK;
 }
@@ -548,6 +577,34 @@ int ncg_ctx_set_tolerance(ncg_ctx* c, int tol) {
     if (!c || (tol != NCG_TOL_REFERENCE && tol != NCG_TOL_PRECISE)) return NCG_EINVAL;
     c->tol_mode = tol;
     return NCG_OK;
+}
+
+int ncg_ctx_set_profiling(ncg_ctx* c, int enabled) {
+    if (!c) return NCG_EINVAL;
+    if (enabled && !c->marks[0]) {
+        for (int i = 0; i <= NCG_N_STAGES; ++i)
+            if (!cuda_ok(cudaEventCreate(&c->marks[i]), "cudaEventCreate")) return NCG_ECUDA;
+    }
+    c->profiling = enabled ? 1 : 0;
+    return NCG_OK;
+}
+
+int ncg_get_stage_ms(ncg_ctx* c, float* ms, int n_max) {
+    if (!c || !ms) return NCG_EINVAL;
+    for (int i = 0; i < n_max; ++i) ms[i] = 0.0f;
+    if (!c->profiling || c->n_marks < 2) return 0;
+    if (!cuda_ok(cudaEventSynchronize(c->marks[c->n_marks - 1]), "cudaEventSynchronize")) return NCG_ECUDA;
+    int wrote = 0;
+    for (int i = 1; i < c->n_marks; ++i) {
+        int stage = c->mark_stage[i];
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, c->marks[i - 1], c->marks[i]);
+        if (stage >= 0 && stage < n_max) {
+            ms[stage] = t;
+            if (stage + 1 > wrote) wrote = stage + 1;
+        }
+    }
+    return wrote;
 }
 
 int ncg_ctx_set_warm_start(ncg_ctx* c, int w) {
@@ -567,8 +624,8 @@ int ncg_get_stats(ncg_ctx* c, ncg_stats* out) {
     // host_ctr was filled by an asynchronous copy at the end of the last call;
     // the caller synchronises the stream before reading the statistics.
     out->n_pairs = c->last.n_pairs;
-    out->n_epa = c->host_ctr->epa_count;
-    out->n_epa_overflow = c->host_ctr->ovf_count;
+    out->n_epa = c->host_ctr->epa_count[0];
+    out->n_epa_overflow = c->host_ctr->epa_count[1];
     out->gjk_iters = c->host_ctr->gjk_iters;
     out->epa_iters = c->host_ctr->epa_iters;
     out->kernels_launched = c->launches;

@@ -54,6 +54,19 @@ class Context:
         N.check(self._L.ncg_ctx_set_warm_start(self._p, int(mode)), "ncg_ctx_set_warm_start")
         self.warm_start = int(mode)
 
+    def set_profiling(self, on=True):
+        """Records CUDA events between the library's kernel launches."""
+        N.check(self._L.ncg_ctx_set_profiling(self._p, 1 if on else 0), "ncg_ctx_set_profiling")
+
+    def stage_ms(self):
+        """Per-kernel durations (ms) of the last call, keyed by stage name."""
+        import numpy as _np
+        buf = _np.zeros(len(N.STAGES), _np.float32)
+        n = self._L.ncg_get_stage_ms(self._p, buf.ctypes.data, len(N.STAGES))
+        if n < 0:
+            N.check(n, "ncg_get_stage_ms")
+        return {k: float(buf[i]) for i, k in enumerate(N.STAGES[:n])}
+
     def stats(self):
         s = N.NcgStats()
         N.check(self._L.ncg_get_stats(self._p, ctypes.byref(s)), "ncg_get_stats")

@@ -12,7 +12,8 @@
 //                 the termination tests.
 //   <float, float>   = the reference f32 path,
 //   <double, double> = the reference built with f64 (the FP64 error oracle),
-//   <float, double>  = the mixed split that the GPU kernels compute.
+//   <float, dw>      = the mixed split that the GPU kernels compute (dw =
+//                      double-word float-float arithmetic, dw.hpp).
 // Build with -ffp-contract=off: the reference (Rust) never fuses mul+add.
 //
 // Parity pins: the known-answer tests of the reference (tests/geometry/epa3.rs,
@@ -28,6 +29,8 @@
 #include <cstdint>
 #include <limits>
 #include <vector>
+
+#include "dw.hpp"
 
 namespace ncgo {
 
@@ -47,7 +50,10 @@ template <class T> inline V3<T> cross(V3<T> a, V3<T> b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 template <class T> inline T norm_sq(V3<T> a) { return dot(a, a); }
-template <class T> inline T norm(V3<T> a) { return std::sqrt(norm_sq(a)); }
+template <class T> inline T norm(V3<T> a) {
+    using std::sqrt;
+    return sqrt(norm_sq(a));
+}
 template <class T, class U> inline V3<T> cvt(V3<U> a) { return {T(a.x), T(a.y), T(a.z)}; }
 template <class T> inline V3<T> zero3() { return {T(0), T(0), T(0)}; }
 
@@ -214,16 +220,53 @@ inline CSOPoint<N> cso_from_shapes(const Iso<N>& m1, const Shape<N>& g1, const I
 // epa3.rs:231-232 (100 eps), utils/triangle.rs:94-101 ((100 eps)^2).
 template <class S> struct Tol {
     S eps, eps_tol, eps_rel, epa_eps_tol, affine_eps;
+    S add_tol;  // VoronoiSimplex::add_point's degeneracy threshold (gjk::eps_tol in the reference)
+    Tol() {}
+    // In S arithmetic, as the reference computes them for N = S.
     // epa_tol > 0 replaces EPA's termination threshold (100 eps) only.
     explicit Tol(S e, S epa_tol = S(0)) {
+        using std::sqrt;
         eps = e;
         eps_tol = e * S(10.0);
-        eps_rel = std::sqrt(eps_tol);
+        eps_rel = sqrt(eps_tol);
         epa_eps_tol = epa_tol > S(0) ? epa_tol : e * S(100.0);
         S t = e * S(100.0);
         affine_eps = t * t;
+        add_tol = eps_tol;
     }
 };
+template <class S> inline Tol<S> make_tol(double e, double epa_tol) { return Tol<S>(S(e), S(epa_tol)); }
+// The double-word split computes its constants in f64 and rounds them to
+// double-word (the kernels' host code does the same).
+template <> inline Tol<dw> make_tol<dw>(double e, double epa_tol) {
+    Tol<dw> t;
+    t.eps = dw::from_double(e);
+    t.eps_tol = dw::from_double(e * 10.0);
+    t.eps_rel = dw::from_double(std::sqrt(e * 10.0));
+    t.epa_eps_tol = dw::from_double(epa_tol > 0 ? epa_tol : e * 100.0);
+    double a = e * 100.0;
+    t.affine_eps = dw::from_double(a * a);
+    t.add_tol = t.eps_tol;
+    return t;
+}
+// The kernels' PRECISE tolerance set: the tests that classify (origin on the
+// simplex, origin inside the tetrahedron, EPA face checks and visibility) keep
+// the f32 machine epsilon, the noise floor of f32 support points; the tests
+// that decide how far GJK refines (add_point's degeneracy threshold and the
+// relative gap sqrt(10 eps)) use f64::EPSILON as the reference built with f64.
+template <class S> inline Tol<S> make_tol_precise(double epa_tol) {
+    Tol<S> t = make_tol<S>((double)FLT_EPSILON, epa_tol);
+    t.eps_rel = S(std::sqrt(10.0 * (double)DBL_EPSILON));
+    t.add_tol = S(10.0 * (double)DBL_EPSILON);
+    return t;
+}
+template <> inline Tol<dw> make_tol_precise<dw>(double epa_tol) {
+    Tol<dw> t = make_tol<dw>((double)FLT_EPSILON, epa_tol);
+    t.eps_rel = dw::from_double(std::sqrt(10.0 * (double)DBL_EPSILON));
+    t.add_tol = dw::from_double(10.0 * (double)DBL_EPSILON);
+    return t;
+}
+
 
 // ------------------------------------------------- point projections (solid)
 enum LocKind { ON_VERTEX, ON_EDGE, ON_FACE, ON_SOLID };
@@ -454,18 +497,19 @@ template <class N, class S> struct VoronoiSimplex {
         for (int i = 0; i < 4; ++i) prev_vertices[i] = i;
         V3<S> ps = cvt<S>(p.point);
         if (dim == 0) {
-            if (norm_sq(pt(0) - ps) < tol.eps_tol) return false;
+            if (norm_sq(pt(0) - ps) < tol.add_tol) return false;
         } else if (dim == 1) {
             V3<S> ab = pt(1) - pt(0);
             V3<S> ac = ps - pt(0);
-            if (norm_sq(cross(ab, ac)) < tol.eps_tol) return false;
+            if (norm_sq(cross(ab, ac)) < tol.add_tol) return false;
         } else {  // dim == 2
             V3<S> ab = pt(1) - pt(0);
             V3<S> ac = pt(2) - pt(0);
             V3<S> ap = ps - pt(0);
             V3<S> c = cross(ab, ac);
             V3<S> n = c / norm(c);
-            if (std::fabs(dot(n, ap)) < tol.eps_tol) return false;
+            using std::fabs;
+            if (fabs(dot(n, ap)) < tol.add_tol) return false;
         }
         dim += 1;
         vertices[dim] = p;
@@ -737,72 +781,76 @@ template <class S> struct RustBinaryHeap {
     }
 };
 
-template <class S> struct Face {
+// The polytope's expansion (triangle projection, visibility) runs in N; the
+// face normal is computed in S and stored in N; distances, heap keys and the
+// termination test are in S.  With N = S this is the reference's EPA exactly.
+template <class N> struct Face {
     size_t pts[3];
     size_t adj[3];
-    V3<S> normal;
-    V3<S> proj;
-    S bcoords[3];
+    V3<N> normal;
+    N bcoords[3];
     bool deleted;
 };
 
 template <class N, class S> struct EPA {
     std::vector<CSOPoint<N>> vertices;
-    std::vector<Face<S>> faces;
+    std::vector<Face<N>> faces;
     std::vector<std::pair<size_t, size_t>> silhouette;  // (face_id, opp_pt_id)
     RustBinaryHeap<S> heap;
     const Tol<S>* tol = nullptr;
 
     V3<S> vp(size_t i) const { return cvt<S>(vertices[i].point); }
+    V3<N> vn(size_t i) const { return vertices[i].point; }
+    V3<S> fnormal(size_t f) const { return cvt<S>(faces[f].normal); }
 
     // epa3.rs:63-94 (ccw_face_normal: utils/ccw_face_normal.rs:21-27).
-    Face<S> face_with_proj(V3<S> proj, const S b[3], size_t p0, size_t p1, size_t p2, size_t a0, size_t a1, size_t a2) {
-        Face<S> f;
+    Face<N> face_with_proj(const N b[3], size_t p0, size_t p1, size_t p2, size_t a0, size_t a1, size_t a2) {
+        Face<N> f;
         f.pts[0] = p0; f.pts[1] = p1; f.pts[2] = p2;
         f.adj[0] = a0; f.adj[1] = a1; f.adj[2] = a2;
         V3<S> ab = vp(p1) - vp(p0), ac = vp(p2) - vp(p0);
         V3<S> n;
         if (!try_normalize(cross(ab, ac), tol->eps, &n, (S*)nullptr)) n = zero3<S>();
-        f.normal = n;
-        f.proj = proj;
+        f.normal = cvt<N>(n);
         f.bcoords[0] = b[0]; f.bcoords[1] = b[1]; f.bcoords[2] = b[2];
         f.deleted = false;
         return f;
     }
-    // epa3.rs:96-115.
-    Face<S> face_new(size_t p0, size_t p1, size_t p2, size_t a0, size_t a1, size_t a2, bool* inside) {
-        Loc<S> loc;
-        V3<S> pr = project_origin_triangle(vp(p0), vp(p1), vp(p2), &loc);
+    // epa3.rs:96-115 (the projected point itself is never used).
+    Face<N> face_new(size_t p0, size_t p1, size_t p2, size_t a0, size_t a1, size_t a2, bool* inside) {
+        Loc<N> loc;
+        (void)project_origin_triangle(vn(p0), vn(p1), vn(p2), &loc);
         if (loc.kind == ON_FACE) {
             *inside = true;
-            return face_with_proj(pr, loc.b, p0, p1, p2, a0, a1, a2);
+            return face_with_proj(loc.b, p0, p1, p2, a0, a1, a2);
         }
         *inside = false;
-        S z[3] = {S(0), S(0), S(0)};
-        return face_with_proj(pr, z, p0, p1, p2, a0, a1, a2);
+        N z[3] = {N(0), N(0), N(0)};
+        return face_with_proj(z, p0, p1, p2, a0, a1, a2);
     }
     // epa3.rs:117-126.
-    void face_closest_points(const Face<S>& f, V3<S>* p1, V3<S>* p2) const {
-        *p1 = (cvt<S>(vertices[f.pts[0]].orig1) * f.bcoords[0] + cvt<S>(vertices[f.pts[1]].orig1) * f.bcoords[1]) +
-              cvt<S>(vertices[f.pts[2]].orig1) * f.bcoords[2];
-        *p2 = (cvt<S>(vertices[f.pts[0]].orig2) * f.bcoords[0] + cvt<S>(vertices[f.pts[1]].orig2) * f.bcoords[1]) +
-              cvt<S>(vertices[f.pts[2]].orig2) * f.bcoords[2];
+    void face_closest_points(const Face<N>& f, V3<S>* p1, V3<S>* p2) const {
+        S b0 = S(f.bcoords[0]), b1 = S(f.bcoords[1]), b2 = S(f.bcoords[2]);
+        *p1 = (cvt<S>(vertices[f.pts[0]].orig1) * b0 + cvt<S>(vertices[f.pts[1]].orig1) * b1) +
+              cvt<S>(vertices[f.pts[2]].orig1) * b2;
+        *p2 = (cvt<S>(vertices[f.pts[0]].orig2) * b0 + cvt<S>(vertices[f.pts[1]].orig2) * b1) +
+              cvt<S>(vertices[f.pts[2]].orig2) * b2;
     }
-    static size_t next_ccw_pt_id(const Face<S>& f, size_t id) {
+    static size_t next_ccw_pt_id(const Face<N>& f, size_t id) {
         if (f.pts[0] == id) return 1;
         if (f.pts[1] == id) return 2;
         return 0;
     }
     // epa3.rs:143-156 and utils/triangle.rs:85-102.
-    bool can_be_seen_by(const Face<S>& f, size_t point, size_t opp) const {
-        V3<S> p0 = vp(f.pts[opp]);
-        V3<S> p1 = vp(f.pts[(opp + 1) % 3]);
-        V3<S> p2 = vp(f.pts[(opp + 2) % 3]);
-        V3<S> pt = vp(point);
-        if (dot(pt - p0, f.normal) >= -tol->eps_tol) return true;
+    bool can_be_seen_by(const Face<N>& f, size_t point, size_t opp) const {
+        V3<N> p0 = vn(f.pts[opp]);
+        V3<N> p1 = vn(f.pts[(opp + 1) % 3]);
+        V3<N> p2 = vn(f.pts[(opp + 2) % 3]);
+        V3<N> pt = vn(point);
+        if (dot(pt - p0, f.normal) >= -N(tol->eps_tol)) return true;
         // relative_eq!(|p1p2 x p1p3|^2, 0, epsilon = (100 eps)^2)
-        S x = norm_sq(cross(p2 - p1, pt - p1));
-        return x == S(0) || std::fabs(x) <= tol->affine_eps;
+        N x = norm_sq(cross(p2 - p1, pt - p1));
+        return x == N(0) || std::fabs(x) <= N(tol->affine_eps);
     }
     // epa3.rs:432-454.
     void compute_silhouette(size_t point, size_t id, size_t opp) {
@@ -852,7 +900,7 @@ template <class N, class S> struct EPA {
             bool ins[4] = {in1, in2, in3, in4};
             for (size_t k = 0; k < 4; ++k) {
                 if (ins[k]) {
-                    S dist = dot(faces[k].normal, vp(k));
+                    S dist = dot(fnormal(k), vp(k));
                     if (-dist > t.eps_tol) { if (cnt) cnt->status |= ST_EPA_FAILED; return false; }
                     heap.push(FaceId<S>{k, -dist});
                 }
@@ -863,7 +911,8 @@ template <class N, class S> struct EPA {
                 // closure returns false after the first basis vector a x dpt.
                 V3<S> dpt = vp(1) - vp(0);
                 V3<S> a;
-                if (std::fabs(dpt.x) > std::fabs(dpt.y)) a = v3<S>(dpt.z, S(0), -dpt.x);
+                using std::fabs;
+                if (fabs(dpt.x) > fabs(dpt.y)) a = v3<S>(dpt.z, S(0), -dpt.x);
                 else a = v3<S>(S(0), -dpt.z, dpt.y);
                 a = a / norm(a);
                 V3<S> dir = cross(a, dpt);
@@ -887,22 +936,22 @@ template <class N, class S> struct EPA {
 
         FaceId<S> face_id;
         while (heap.pop(&face_id)) {
-            Face<S> face = faces[face_id.id];
+            Face<N> face = faces[face_id.id];
             if (face.deleted) continue;
             if (cnt) cnt->epa_iters++;
             CSOPoint<N> cso = cso_from_shapes(m1, g1, m2, g2, cvt<N>(face.normal), cnt);
             size_t support_point_id = vertices.size();
             vertices.push_back(cso);
-            S candidate_max_dist = dot(cvt<S>(cso.point), face.normal);
+            S candidate_max_dist = dot(cvt<S>(cso.point), cvt<S>(face.normal));
             if (candidate_max_dist < max_dist) {
                 best_face_id = face_id;
                 max_dist = candidate_max_dist;
             }
             S curr_dist = -face_id.neg_dist;
             if (max_dist - curr_dist < t.epa_eps_tol) {
-                const Face<S>& bf = faces[best_face_id.id];
+                const Face<N>& bf = faces[best_face_id.id];
                 face_closest_points(bf, out_p1, out_p2);
-                *out_n = bf.normal;
+                *out_n = cvt<S>(bf.normal);
                 if (cnt) cnt->epa_exit = EXIT_CONVERGED;
                 track(cnt);
                 return true;
@@ -927,16 +976,16 @@ template <class N, class S> struct EPA {
                     size_t pt_id1 = faces[edge.first].pts[(edge.second + 2) % 3];
                     size_t pt_id2 = faces[edge.first].pts[(edge.second + 1) % 3];
                     bool inside;
-                    Face<S> nf = face_new(pt_id1, pt_id2, support_point_id, edge.first, new_face_id + 1,
+                    Face<N> nf = face_new(pt_id1, pt_id2, support_point_id, edge.first, new_face_id + 1,
                                           new_face_id - 1, &inside);
                     faces[edge.first].adj[(edge.second + 1) % 3] = new_face_id;
                     faces.push_back(nf);
                     if (cnt) cnt->faces_created++;
                     if (inside) {
-                        S dist = dot(faces[new_face_id].normal, vp(faces[new_face_id].pts[0]));
+                        S dist = dot(fnormal(new_face_id), vp(faces[new_face_id].pts[0]));
                         if (dist < curr_dist) {
                             face_closest_points(face, out_p1, out_p2);
-                            *out_n = face.normal;
+                            *out_n = cvt<S>(face.normal);
                             if (cnt) cnt->epa_exit = EXIT_NUMERIC;
                             track(cnt);
                             return true;
@@ -965,9 +1014,9 @@ template <class N, class S> struct EPA {
                 return false;
             }
         }
-        const Face<S>& bf = faces[best_face_id.id];
+        const Face<N>& bf = faces[best_face_id.id];
         face_closest_points(bf, out_p1, out_p2);
-        *out_n = bf.normal;
+        *out_n = cvt<S>(bf.normal);
         if (cnt) cnt->epa_exit = EXIT_HEAP_EMPTY;
         track(cnt);
         return true;

@@ -129,10 +129,12 @@ void run_range(const In& in, int query, S param, const Tol<S>& tol, uint64_t lo,
         }
         if (o.out16) {
             double* w = o.out16 + 16 * i;
-            w[0] = r.p1.x; w[1] = r.p1.y; w[2] = r.p1.z;
-            w[3] = r.p2.x; w[4] = r.p2.y; w[5] = r.p2.z;
-            w[6] = r.dir.x; w[7] = r.dir.y; w[8] = r.dir.z;
-            w[9] = r.value;
+            // double-word values are reported by their high word (the f32
+            // the kernels write out)
+            w[0] = double(r.p1.x); w[1] = double(r.p1.y); w[2] = double(r.p1.z);
+            w[3] = double(r.p2.x); w[4] = double(r.p2.y); w[5] = double(r.p2.z);
+            w[6] = double(r.dir.x); w[7] = double(r.dir.y); w[8] = double(r.dir.z);
+            w[9] = double(r.value);
             w[10] = r.gjk_kind;
             for (int k = 11; k < 16; ++k) w[k] = 0.0;
         }
@@ -155,9 +157,9 @@ void run_range(const In& in, int query, S param, const Tol<S>& tol, uint64_t lo,
 template <class N, class S, class In>
 int run(const In& in, uint64_t n_pairs, int query, double param, double eps, double epa_tol, int n_threads,
         const Outs& o) {
-    S e = eps > 0 ? S(eps) : std::numeric_limits<S>::epsilon();
-    if (eps <= 0 && sizeof(N) < sizeof(S)) e = S(std::numeric_limits<N>::epsilon());
-    Tol<S> tol(e, S(epa_tol > 0 ? epa_tol : 0.0));
+    // eps < 0 selects the PRECISE tolerance set (make_tol_precise).
+    double e = eps > 0 ? eps : (double)std::numeric_limits<N>::epsilon();
+    Tol<S> tol = eps < 0 ? make_tol_precise<S>(epa_tol > 0 ? epa_tol : 0.0) : make_tol<S>(e, epa_tol > 0 ? epa_tol : 0.0);
     S p = S(param);
     if (n_threads <= 1 || n_pairs < 64) {
         run_range<N, S>(in, query, p, tol, 0, n_pairs, o);
@@ -181,7 +183,7 @@ int dispatch(int policy, const In& in, uint64_t n, int query, double param, doub
     switch (policy) {
     case POLICY_F32: return run<float, float>(in, n, query, param, eps, epa_tol, nt, o);
     case POLICY_F64: return run<double, double>(in, n, query, param, eps, epa_tol, nt, o);
-    case POLICY_MIXED: return run<float, double>(in, n, query, param, eps, epa_tol, nt, o);
+    case POLICY_MIXED: return run<float, dw>(in, n, query, param, eps, epa_tol, nt, o);
     default: return NCG_EINVAL;
     }
 }
@@ -190,10 +192,11 @@ int dispatch(int policy, const In& in, uint64_t n, int query, double param, doub
 
 extern "C" {
 
-// policy: 0 = reference f32, 1 = reference f64, 2 = f32 supports + f64 sub-solve.
+// policy: 0 = reference f32, 1 = reference f64, 2 = f32 supports + double-word sub-solve.
 // query:  0 = contact, 1 = distance, 2 = proximity, 3 = closest_points.
-// eps <= 0 selects the machine epsilon of the policy's N (the reference's
-// default_epsilon); any other value replaces it in every tolerance.
+// eps == 0 selects the machine epsilon of the policy's N (the reference's
+// default_epsilon); eps > 0 replaces it in every tolerance; eps < 0 selects
+// the PRECISE set (f32 zero tests, f64 relative GJK convergence).
 // epa_tol > 0 replaces EPA's termination threshold (100 eps) alone.
 // out16: per pair p1[3] p2[3] dir[3] value gjk_kind, padded to 16 doubles.
 // counters8: gjk iters, epa iters, support calls, hull points scanned,

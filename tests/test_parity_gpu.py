@@ -22,7 +22,8 @@ DBL_EPS = float(np.finfo(np.float64).eps)
 
 
 def oracle_mixed(batch, query, param, tol):
-    eps, epa_tol = (0.0, 0.0) if tol == N.TOL_REFERENCE else (DBL_EPS, 1e-6)
+    # eps < 0 selects the oracle's PRECISE tolerance set (the kernels' NCG_TOL_PRECISE)
+    eps, epa_tol = (0.0, 0.0) if tol == N.TOL_REFERENCE else (-1.0, 1e-6)
     return O.query(batch, query, O.MIXED, param=float(np.float32(param)), eps=eps, epa_tol=epa_tol)
 
 
