@@ -191,6 +191,33 @@ int ncg_distance_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float* out_dis
 int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
                              uint8_t* out_prox, float* out_sep_axis, uint32_t* status);
 
+/* ---- contact without any device allocation --------------------------------
+ * For callers that cannot allocate device memory at the moment they need
+ * contacts: code recording a CUDA graph through stream capture without a graph
+ * memory pool, real-time simulation loops whose allocator is frozen after
+ * start-up, and host runtimes (game engines, FFI hosts) that own every device
+ * allocation themselves.  This entry point needs no ncg_ctx and never calls
+ * cudaMalloc, cudaFree or any allocating routine: its scratch (pair lists, EPA
+ * work items and one global-memory EPA slab) is a fixed array of 8.1 MiB
+ * (8,528,128 bytes) compiled into the library, which every GPU that loads the
+ * library holds until the process exits.
+ * Limit: at most NCG_NOALLOC_MAX_PAIRS pairs per call; a larger batch returns
+ * NCG_EINVAL with a message in ncg_last_error().
+ * The first call on a device performs a one-time set-up with that device
+ * current (it looks up the array's device address and the launch limits):
+ * make that first call before any stream capture.  Every call on a device
+ * shares the one array and the array keeps the previous call's contents (the
+ * call clears what must start at zero), so calls that overlap on the GPU —
+ * different streams, or concurrent host threads — race and corrupt each
+ * other's results: serialise them.
+ * `tolerance` is an ncg_tolerance; batch->init_dir, when not NULL, is the
+ * first GJK direction of every pair.  Results equal ncg_contact_batch's.
+ * This entry point has no counterpart in the reference. */
+#define NCG_NOALLOC_MAX_PAIRS 32768
+int ncg_contact_batch_noalloc(const ncg_batch* batch, float prediction, int tolerance,
+                              ncg_contact* out, uint8_t* has_contact, float* out_dir,
+                              uint32_t* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,11 +54,11 @@ struct EpaStore {
     int VC, FC, SC, TC;
 
     // Bytes needed for one store (each array padded to 16 bytes).
-    static __host__ __device__ size_t bytes(int VC, int FC, int SC, int TC) {
-        auto r = [](size_t b) { return (b + 15) & ~size_t(15); };
-        return r(9 * 4 * (size_t)VC) + r(3 * 4 * (size_t)FC) + r(8 * (size_t)FC) + r(8 * (size_t)SC) +
-               r(3 * 2 * (size_t)FC) + r(3 * 2 * (size_t)FC) + r(2 * (size_t)FC) + r(2 * (size_t)SC) +
-               r(2 * (size_t)TC) + r((size_t)FC) + r((size_t)SC) + r((size_t)TC) + r((size_t)SC);
+    static constexpr __host__ __device__ size_t r16(size_t b) { return (b + 15) & ~size_t(15); }
+    static constexpr __host__ __device__ size_t bytes(int VC, int FC, int SC, int TC) {
+        return r16(9 * 4 * (size_t)VC) + r16(3 * 4 * (size_t)FC) + r16(8 * (size_t)FC) + r16(8 * (size_t)SC) +
+               r16(3 * 2 * (size_t)FC) + r16(3 * 2 * (size_t)FC) + r16(2 * (size_t)FC) + r16(2 * (size_t)SC) +
+               r16(2 * (size_t)TC) + r16((size_t)FC) + r16((size_t)SC) + r16((size_t)TC) + r16((size_t)SC);
     }
     NCG_DEV void carve(char* base, int vc, int fc, int sc, int tc) {
         VC = vc; FC = fc; SC = sc; TC = tc;

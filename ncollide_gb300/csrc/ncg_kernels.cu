@@ -781,3 +781,121 @@ int ncg_proximity_batch_host(ncg_ctx* c, const ncg_batch* b, float margin, uint8
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ no-allocation entry point
+// ncg_contact_batch_noalloc runs the contact pipeline on a fixed scratch array
+// in the library's device image instead of context-owned allocations.  Layout
+// of the array: counters (256 B), EPA work items, routing lists and tier
+// queues (4 x 4 B per pair), one tier-C EPA slab.
+namespace {
+constexpr uint64_t NA_MAX_PAIRS = NCG_NOALLOC_MAX_PAIRS;
+constexpr size_t NA_SLAB_BYTES =
+    (EpaStore::bytes(EpaTier<2>::VC, EpaTier<2>::FC, EpaTier<2>::SC, EpaTier<2>::TC) + 255) & ~size_t(255);
+constexpr size_t NA_ITEMS_BYTES = sizeof(EpaItem) * NA_MAX_PAIRS;
+constexpr size_t NA_LISTS_BYTES = 4 * 4 * NA_MAX_PAIRS;
+constexpr size_t NA_BYTES = 256 + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_SLAB_BYTES;
+static_assert(sizeof(DevCounters) <= 256, "counters must fit their slot");
+}  // namespace
+
+// Host code must not use this name as an address: it is only a host-side stand-in.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+namespace {
+struct NoallocDevice {
+    bool ready;
+    char* base;  // device address of g_noalloc_scratch on this device
+    int num_sms, occ_thread, occ_warp, occ_epa0, occ_epa1;
+};
+std::mutex g_noalloc_mu;
+constexpr int NA_MAX_DEVICES = 64;
+NoallocDevice g_noalloc[NA_MAX_DEVICES] = {};
+
+// One-time set-up for the current device: the array's device address and the
+// launch limits.  No allocation.
+int noalloc_setup(int dev, NoallocDevice& out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoallocDevice& d = g_noalloc[dev];
+    if (!d.ready) {
+        void* p = nullptr;
+        if (!cuda_ok(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(noalloc scratch)"))
+            return NCG_ECUDA;
+        d.base = (char*)p;
+        if (!cuda_ok(cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev), "device attribute"))
+            return NCG_ECUDA;
+        cudaFuncSetAttribute(k_epa<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<0>());
+        cudaFuncSetAttribute(k_epa<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<1>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_thread, k_gjk_thread, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_warp, k_gjk_warp, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_epa0, k_epa<0>, 32, tier_bytes<0>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_epa1, k_epa<1>, 32, tier_bytes<1>());
+        if (d.occ_thread < 1) d.occ_thread = 1;
+        if (d.occ_warp < 1) d.occ_warp = 1;
+        if (d.occ_epa0 < 1) d.occ_epa0 = 1;
+        if (d.occ_epa1 < 1) d.occ_epa1 = 1;
+        if (!cuda_ok(cudaGetLastError(), "noalloc set-up")) return NCG_ECUDA;
+        d.ready = true;
+    }
+    out = d;
+    return NCG_OK;
+}
+}  // namespace
+
+extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, int tolerance, ncg_contact* out,
+                                         uint8_t* has_contact, float* out_dir, uint32_t* status, void* stream) {
+    if (!b) { g_last_error = "null batch"; return NCG_EINVAL; }
+    if (b->n_pairs > NA_MAX_PAIRS) {
+        g_last_error = "ncg_contact_batch_noalloc: batch of " + std::to_string(b->n_pairs) +
+                       " pairs exceeds NCG_NOALLOC_MAX_PAIRS (" + std::to_string(NA_MAX_PAIRS) + ")";
+        return NCG_EINVAL;
+    }
+    if (tolerance != NCG_TOL_REFERENCE && tolerance != NCG_TOL_PRECISE) {
+        g_last_error = "unknown tolerance set";
+        return NCG_EINVAL;
+    }
+    if (b->n_pairs == 0) return NCG_OK;
+    if (!out || !has_contact || !status || !b->shapes || !b->m1 || !b->m2 || !b->g1 || !b->g2) {
+        g_last_error = "null required pointer";
+        return NCG_EINVAL;
+    }
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return NCG_ECUDA;
+    if (dev < 0 || dev >= NA_MAX_DEVICES) { g_last_error = "device index out of range"; return NCG_EINVAL; }
+    NoallocDevice d;
+    int rc = noalloc_setup(dev, d);
+    if (rc) return rc;
+
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch s;
+    char* p = d.base;
+    s.ctr = (DevCounters*)p; p += 256;
+    s.items = (EpaItem*)p; p += NA_ITEMS_BYTES;
+    s.analytic = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
+    s.hull = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
+    s.ovf[0] = nullptr;
+    s.ovf[1] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
+    s.ovf[2] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
+    s.slabs = p;
+    s.slab_bytes = NA_SLAB_BYTES;
+    s.n_slabs = 1;
+
+    QueryParams qp;
+    qp.query = Q_CONTACT;
+    qp.use_init_dir = b->init_dir ? 1 : 0;
+    qp.gjk_max_iter = 10000;
+    qp.epa_max_iter = 10000;
+    qp.param = dw_split((double)prediction);
+    qp.tol = make_tol(tolerance);
+    Outputs o{out, has_contact, out_dir, nullptr, nullptr, status, nullptr};
+    ncg_batch bb = *b;
+
+    // The array keeps the previous call's contents: reset the counters and queues' heads.
+    if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset noalloc counters")) return NCG_ECUDA;
+    unsigned n = (unsigned)b->n_pairs;
+    k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
+    k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s);
+    k_gjk_warp<<<d.num_sms * d.occ_warp, 128, 0, st>>>(bb, qp, o, s);
+    k_epa<0><<<d.num_sms * d.occ_epa0, 32, tier_bytes<0>(), st>>>(bb, qp, o, s);
+    k_epa<1><<<d.num_sms * d.occ_epa1, 32, tier_bytes<1>(), st>>>(bb, qp, o, s);
+    k_epa<2><<<1, 32, 0, st>>>(bb, qp, o, s);
+    return cuda_ok(cudaGetLastError(), "noalloc kernel launch") ? NCG_OK : NCG_ECUDA;
+}
