@@ -310,7 +310,7 @@ def main():
                  epa_tol=1e-6 if args.tolerance == "precise" else 0.0)
     bytes_pp, in_pp, out_pp, flops_pp = algorithmic(batch, rs.counters)
     units = {"classify": batch.n_pairs, "gjk_thread": stats.get("n_pairs", 0), "gjk_warp": stats.get("n_pairs", 0),
-             "epa_tier_a": stats["n_epa"], "epa_tier_b": stats["n_epa_overflow"],
+             "epa_thread": stats["n_epa"], "epa_tier_a": stats["n_epa"], "epa_tier_b": stats["n_epa_overflow"],
              "epa_tier_c": stats["n_epa_overflow"]}.get(dom, batch.n_pairs)
     dom_s = mean_stage[dom] / 1e3
     achieved = units * bytes_pp / dom_s / 1e9

@@ -147,10 +147,10 @@ int ncg_get_stats(ncg_ctx* ctx, ncg_stats* out);
 /* Stage timing: when enabled, each batch call records CUDA events between its
  * kernel launches on the caller's stream.  ncg_get_stage_ms fills up to
  * n_max durations in milliseconds (order: classify, gjk_thread, gjk_warp,
- * epa_tier_a, epa_tier_b, epa_tier_c) of the last call and returns how many it
- * wrote; it synchronises on the last call's events.  No reference counterpart
- * (the reference has no instrumentation). */
-#define NCG_N_STAGES 6
+ * epa_thread, epa_tier_a, epa_tier_b, epa_tier_c) of the last call and returns
+ * how many it wrote; it synchronises on the last call's events.  No reference
+ * counterpart (the reference has no instrumentation). */
+#define NCG_N_STAGES 7
 int ncg_ctx_set_profiling(ncg_ctx* ctx, int enabled);
 int ncg_get_stage_ms(ncg_ctx* ctx, float* ms, int n_max);
 const char* ncg_last_error(void);
@@ -198,8 +198,8 @@ int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
  * start-up, and host runtimes (game engines, FFI hosts) that own every device
  * allocation themselves.  This entry point needs no ncg_ctx and never calls
  * cudaMalloc, cudaFree or any allocating routine: its scratch (pair lists, EPA
- * work items and one global-memory EPA slab) is a fixed array of 8.1 MiB
- * (8,528,128 bytes) compiled into the library, which every GPU that loads the
+ * work items and one global-memory EPA slab) is a fixed array of 7.1 MiB
+ * (7,433,728 bytes) compiled into the library, which every GPU that loads the
  * library holds until the process exits.
  * Limit: at most NCG_NOALLOC_MAX_PAIRS pairs per call; a larger batch returns
  * NCG_EINVAL with a message in ncg_last_error().

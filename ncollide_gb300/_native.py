@@ -33,7 +33,7 @@ EXPORTED = [
     "ncg_proximity_batch_host", "ncg_ctx_set_profiling", "ncg_get_stage_ms", "ncg_contact_batch_noalloc",
 ]
 NOALLOC_MAX_PAIRS = 32768
-STAGES = ["classify", "gjk_thread", "gjk_warp", "epa_tier_a", "epa_tier_b", "epa_tier_c"]
+STAGES = ["classify", "gjk_thread", "gjk_warp", "epa_thread", "epa_tier_a", "epa_tier_b", "epa_tier_c"]
 
 
 class NcgBatch(ctypes.Structure):

@@ -1,24 +1,45 @@
 // ncg_epa.cuh — warp-cooperative 3-D EPA (src/query/algorithms/epa3.rs:171-454).
 //
-// One warp expands one polytope.  The polytope (CSO vertices, faces,
-// adjacency, deleted flags), the face heap and the silhouette live in a
-// bounded store: a slice of shared memory for the first pass, a slab of global
-// memory for the pairs whose polytope outgrew the shared one.
+// The algorithm is written once for two execution policies:
+//   ThreadExec  one thread expands one polytope held in its local memory (the
+//               hardware interleaves local memory per lane, so a warp runs 32
+//               independent pairs and thousands of threads hide the latency);
+//               used for pairs of analytic shapes.
+//   WarpExec    one warp expands one polytope held in shared memory (tiers A
+//               and B) or a global-memory slab (tier C); used for ConvexHull
+//               pairs (warp-parallel support scans) and for polytopes that
+//               outgrow a thread's store.
+//
+// Layout (all 16-byte records):
+//   vertex  float4 (x, y, z, 0); the two support points behind each vertex
+//           (witness data, read only at the end) in a separate 6 x f32 array
+//   face    float4 (normal xyz, p0 | p1 << 16) + uint4 (p2 | gen << 16, adj0, adj1, adj2)
+//   heap    float4 (key hi, key lo, push sequence, face reference)
+// A face reference is slot | gen << 16.  Deleting a face bumps its slot's
+// generation and frees the slot, so every reference taken before the deletion
+// (adjacency, heap entries, flood-fill stack) reads as deleted, exactly like
+// the reference's `deleted` flag, and the store only needs room for the live
+// faces (about twice the vertices) instead of every face ever created.  A
+// slot is reused at most once per iteration, so with at most 10 000
+// iterations its 16-bit generation never wraps.
+//
+// Priority order: larger neg_dist first, then the earlier push.  With this
+// strict total order the pop sequence depends only on the set of entries, not
+// on how the heap is arranged, so the entries of deleted faces can be dropped
+// whenever the heap fills up.  Equal keys (the only case where this differs
+// from Rust's BinaryHeap) pop first-in first-out.
 //
 // Arithmetic: the expansion (Face::new's projection of the origin, the
-// visibility test of the silhouette) runs in f32; each face normal is
-// computed in double-word from the f32 vertices and stored rounded to f32;
-// face distances, heap keys and the termination tests are double-word.
+// visibility test of the silhouette) runs in f32; each face normal is the
+// double-word cross product of exact double-word edge vectors, normalised in
+// f32 and stored in f32; face distances, queue keys and the termination tests
+// are double-word.
 //
-// Work split inside the warp:
-//   * support point along the popped face's normal: every lane (hull arg-max
-//     is warp-parallel, analytic maps are computed redundantly);
-//   * the new faces of one expansion step: one lane per silhouette edge;
-//   * heap push/pop, the silhouette flood fill and the ordered post-pass over
-//     the new faces: lane 0, because their order decides which face the
-//     reference pops next.  The heap is a restatement of Rust's BinaryHeap
-//     (push = sift_up; pop = move last to root, sift_down_to_bottom, sift_up)
-//     so that equal keys pop in the reference's order.
+// Work split inside a warp (WarpExec): the support point along the popped
+// face's normal uses every lane (the hull arg-max is warp-parallel); the faces
+// of one expansion step are built one lane per silhouette edge; heap
+// operations, the silhouette flood fill and the ordered post-pass run on lane
+// 0 because their order decides the result.
 #pragma once
 
 #include "ncg_core.cuh"
@@ -34,94 +55,122 @@ enum EpaExit : int {
     EPA_OVERFLOW = 6,    // store capacity exceeded (result not valid)
 };
 
-// Pointers into one warp's store.  Capacities: VC vertices, FC faces (also the
-// heap capacity, each face is pushed at most once), SC silhouette edges, TC
-// flood-fill stack entries.  All indices fit in 16 bits.
+NCG_DEV uint32_t mkref(int slot, uint32_t gen) { return (uint32_t)slot | (gen << 16); }
+NCG_DEV int rslot(uint32_t r) { return (int)(r & 0xffffu); }
+
 struct EpaStore {
-    float* v;         // [9][VC]: point xyz, orig1 xyz, orig2 xyz
-    float* fn;        // [3][FC] face normals
-    float* hkey;      // [2][FC] heap keys (neg_dist), double-word hi / lo
-    float* sdist;     // [2][SC] distance of the face built on silhouette edge k
-    uint16_t* fpts;   // [3][FC]
-    uint16_t* fadj;   // [3][FC]
-    uint16_t* hid;    // [FC]
-    uint16_t* sface;  // [SC]
-    uint16_t* tface;  // [TC]
-    uint8_t* fdel;    // [FC]
+    float4* vpt;      // [VC]
+    float* vo;        // [6][VC] orig1 xyz, orig2 xyz
+    float4* fa;       // [FC] normal xyz, pts p0 | p1 << 16
+    uint4* fb;        // [FC] p2 | gen << 16, adj0, adj1, adj2
+    float4* heap;     // [FC] key hi, key lo, seq, ref
+    uint32_t* freel;  // [FC] free slots (stack)
+    uint32_t* sref;   // [SC] silhouette face references
+    uint32_t* snew;   // [SC] reference of the face built on edge k
+    uint32_t* snext;  // [SC] reference of the next live edge's new face
+    uint32_t* sprev;  // [SC] reference of the previous live edge's new face
+    float2* sdist;    // [SC] distance of the new face (double-word)
     uint8_t* sopp;    // [SC]
-    uint8_t* topp;    // [TC]
-    uint8_t* sflag;   // [SC] bit0 = face built, bit1 = origin projects inside
+    uint8_t* sflag;   // [SC] bit0 live edge, bit1 origin projects inside
+    uint32_t* tref;   // [TC] flood-fill stack: references
+    uint8_t* topp;    // [TC] flood-fill stack: opposite vertex
     int VC, FC, SC, TC;
 
-    // Bytes needed for one store (each array padded to 16 bytes).
     static constexpr __host__ __device__ size_t r16(size_t b) { return (b + 15) & ~size_t(15); }
+    // Bytes of one store.
     static constexpr __host__ __device__ size_t bytes(int VC, int FC, int SC, int TC) {
-        return r16(9 * 4 * (size_t)VC) + r16(3 * 4 * (size_t)FC) + r16(8 * (size_t)FC) + r16(8 * (size_t)SC) +
-               r16(3 * 2 * (size_t)FC) + r16(3 * 2 * (size_t)FC) + r16(2 * (size_t)FC) + r16(2 * (size_t)SC) +
-               r16(2 * (size_t)TC) + r16((size_t)FC) + r16((size_t)SC) + r16((size_t)TC) + r16((size_t)SC);
+        return r16(16 * (size_t)VC) + r16(16 * (size_t)FC) + r16(16 * (size_t)FC) + r16(16 * (size_t)FC) +
+               r16(4 * (size_t)FC) + 4 * r16(4 * (size_t)SC) + r16(8 * (size_t)SC) + 2 * r16((size_t)SC) +
+               r16(4 * (size_t)TC) + r16((size_t)TC) + r16(24 * (size_t)VC);
     }
+
     NCG_DEV void carve(char* base, int vc, int fc, int sc, int tc) {
         VC = vc; FC = fc; SC = sc; TC = tc;
-        auto r = [](size_t b) { return (b + 15) & ~size_t(15); };
         char* p = base;
-        v = (float*)p; p += r(9 * 4 * (size_t)VC);
-        fn = (float*)p; p += r(3 * 4 * (size_t)FC);
-        hkey = (float*)p; p += r(8 * (size_t)FC);
-        sdist = (float*)p; p += r(8 * (size_t)SC);
-        fpts = (uint16_t*)p; p += r(3 * 2 * (size_t)FC);
-        fadj = (uint16_t*)p; p += r(3 * 2 * (size_t)FC);
-        hid = (uint16_t*)p; p += r(2 * (size_t)FC);
-        sface = (uint16_t*)p; p += r(2 * (size_t)SC);
-        tface = (uint16_t*)p; p += r(2 * (size_t)TC);
-        fdel = (uint8_t*)p; p += r((size_t)FC);
-        sopp = (uint8_t*)p; p += r((size_t)SC);
-        topp = (uint8_t*)p; p += r((size_t)TC);
-        sflag = (uint8_t*)p;
+        vpt = (float4*)p; p += r16(16 * (size_t)VC);
+        fa = (float4*)p; p += r16(16 * (size_t)FC);
+        fb = (uint4*)p; p += r16(16 * (size_t)FC);
+        heap = (float4*)p; p += r16(16 * (size_t)FC);
+        freel = (uint32_t*)p; p += r16(4 * (size_t)FC);
+        sref = (uint32_t*)p; p += r16(4 * (size_t)SC);
+        snew = (uint32_t*)p; p += r16(4 * (size_t)SC);
+        snext = (uint32_t*)p; p += r16(4 * (size_t)SC);
+        sprev = (uint32_t*)p; p += r16(4 * (size_t)SC);
+        sdist = (float2*)p; p += r16(8 * (size_t)SC);
+        sopp = (uint8_t*)p; p += r16((size_t)SC);
+        sflag = (uint8_t*)p; p += r16((size_t)SC);
+        tref = (uint32_t*)p; p += r16(4 * (size_t)TC);
+        topp = (uint8_t*)p; p += r16((size_t)TC);
+        vo = (float*)p;
     }
 
-    NCG_DEV vec3<float> vf(int i) const { return {v[i], v[VC + i], v[2 * VC + i]}; }
-    NCG_DEV vec3<real> vp(int i) const { return to_r(vf(i)); }
-    NCG_DEV vec3<real> vo1(int i) const { return {real(v[3 * VC + i]), real(v[4 * VC + i]), real(v[5 * VC + i])}; }
-    NCG_DEV vec3<real> vo2(int i) const { return {real(v[6 * VC + i]), real(v[7 * VC + i]), real(v[8 * VC + i])}; }
+    NCG_DEV vec3<float> vf(int i) const {
+        float4 v = vpt[i];
+        return {v.x, v.y, v.z};
+    }
+    NCG_DEV vec3<real> vo1(int i) const { return {real(vo[i]), real(vo[VC + i]), real(vo[2 * VC + i])}; }
+    NCG_DEV vec3<real> vo2(int i) const { return {real(vo[3 * VC + i]), real(vo[4 * VC + i]), real(vo[5 * VC + i])}; }
     NCG_DEV void put_vertex(int i, const CSO& c) {
-        v[i] = c.p.x; v[VC + i] = c.p.y; v[2 * VC + i] = c.p.z;
-        v[3 * VC + i] = c.o1.x; v[4 * VC + i] = c.o1.y; v[5 * VC + i] = c.o1.z;
-        v[6 * VC + i] = c.o2.x; v[7 * VC + i] = c.o2.y; v[8 * VC + i] = c.o2.z;
+        vpt[i] = make_float4(c.p.x, c.p.y, c.p.z, 0.0f);
+        vo[i] = c.o1.x; vo[VC + i] = c.o1.y; vo[2 * VC + i] = c.o1.z;
+        vo[3 * VC + i] = c.o2.x; vo[4 * VC + i] = c.o2.y; vo[5 * VC + i] = c.o2.z;
     }
     NCG_DEV CSO get_vertex(int i) const {
-        return CSO{{v[i], v[VC + i], v[2 * VC + i]}, {v[3 * VC + i], v[4 * VC + i], v[5 * VC + i]},
-                   {v[6 * VC + i], v[7 * VC + i], v[8 * VC + i]}};
+        return CSO{vf(i), {vo[i], vo[VC + i], vo[2 * VC + i]}, {vo[3 * VC + i], vo[4 * VC + i], vo[5 * VC + i]}};
     }
-    NCG_DEV int pt(int f, int k) const { return fpts[k * FC + f]; }
-    NCG_DEV int adj(int f, int k) const { return fadj[k * FC + f]; }
-    NCG_DEV void set_adj(int f, int k, int a) { fadj[k * FC + f] = (uint16_t)a; }
-    NCG_DEV vec3<float> normalf(int f) const { return {fn[f], fn[FC + f], fn[2 * FC + f]}; }
+    NCG_DEV uint32_t gen(int f) const { return fb[f].x >> 16; }
+    NCG_DEV bool live(uint32_t ref) const { return gen(rslot(ref)) == (ref >> 16); }
+    NCG_DEV void pts(int f, int& a, int& b, int& c) const {
+        uint32_t ab = __float_as_uint(fa[f].w);
+        a = (int)(ab & 0xffffu);
+        b = (int)(ab >> 16);
+        c = (int)(fb[f].x & 0xffffu);
+    }
+    NCG_DEV int pt(int f, int k) const {
+        int a, b, c;
+        pts(f, a, b, c);
+        return k == 0 ? a : (k == 1 ? b : c);
+    }
+    NCG_DEV uint32_t adj(int f, int k) const {
+        uint4 b = fb[f];
+        return k == 0 ? b.y : (k == 1 ? b.z : b.w);
+    }
+    NCG_DEV void set_adj(int f, int k, uint32_t r) {
+        if (k == 0) fb[f].y = r;
+        else if (k == 1) fb[f].z = r;
+        else fb[f].w = r;
+    }
+    NCG_DEV vec3<float> normalf(int f) const {
+        float4 a = fa[f];
+        return {a.x, a.y, a.z};
+    }
     NCG_DEV vec3<real> normal(int f) const { return to_r(normalf(f)); }
-    NCG_DEV real key(int h) const { return real(hkey[h], hkey[FC + h]); }
+    // Deletes a face: bumps its slot's generation (all references go stale) and frees the slot.
+    NCG_DEV void kill(int f, int& nfree) {
+        fb[f].x += 1u << 16;
+        freel[nfree++] = (uint32_t)f;
+    }
 
     // Face::new (epa3.rs:96-115) + ccw_face_normal (utils/ccw_face_normal.rs:21-27).
-    // Writes face f; returns whether the origin projects inside; dist = n . pts[0].
-    NCG_DEV bool build_face(int f, int p0, int p1, int p2, int a0, int a1, int a2, real eps, real& dist) {
+    // Writes face f (generation g); returns whether the origin projects inside;
+    // dist = n . pts[0].
+    __device__ __noinline__ bool build_face(int f, uint32_t g, int p0, int p1, int p2, uint32_t a0, uint32_t a1,
+                                            uint32_t a2, float eps, real& dist) {
         vec3<float> Af = vf(p0), Bf = vf(p1), Cf = vf(p2);
         Loc<float> loc;
         (void)proj_triangle(Af, Bf, Cf, loc);
         vec3<real> A = to_r(Af);
-        vec3<real> u;
-        real len;
         vec3<float> n;
-        if (try_normalize(cross(to_r(Bf) - A, to_r(Cf) - A), eps, u, len)) n = to_f(u);
-        else n = zero3<float>();
-        fpts[f] = (uint16_t)p0; fpts[FC + f] = (uint16_t)p1; fpts[2 * FC + f] = (uint16_t)p2;
-        fadj[f] = (uint16_t)a0; fadj[FC + f] = (uint16_t)a1; fadj[2 * FC + f] = (uint16_t)a2;
-        fn[f] = n.x; fn[FC + f] = n.y; fn[2 * FC + f] = n.z;
-        fdel[f] = 0;
+        float len;
+        if (!try_normalize(to_f(cross(to_r(Bf) - A, to_r(Cf) - A)), eps, n, len)) n = zero3<float>();
+        fa[f] = make_float4(n.x, n.y, n.z, __uint_as_float((uint32_t)p0 | ((uint32_t)p1 << 16)));
+        fb[f] = make_uint4((uint32_t)p2 | (g << 16), a0, a1, a2);
         dist = dot(to_r(n), A);
         return loc.kind == LOC_FACE;
     }
-    // Face::closest_points with the barycentric coordinates Face::new stored
-    // (recomputed: the projection is a pure function of the three vertices).
-    NCG_DEV void face_points(int f, vec3<real>& p1, vec3<real>& p2) const {
-        int a = pt(f, 0), b = pt(f, 1), c = pt(f, 2);
+    // Face::closest_points: the barycentric coordinates Face::new stored are
+    // recomputed from the three vertices (a pure function of them).
+    __device__ __noinline__ void face_points(int a, int b, int c, vec3<real>& p1, vec3<real>& p2) const {
         Loc<float> loc;
         (void)proj_triangle(vf(a), vf(b), vf(c), loc);
         real b0(0.0f), b1(0.0f), b2(0.0f);
@@ -130,70 +179,113 @@ struct EpaStore {
         p2 = (vo2(a) * b0 + vo2(b) * b1) + vo2(c) * b2;
     }
     NCG_DEV int next_ccw(int f, int id) const {
-        if (pt(f, 0) == id) return 1;
-        if (pt(f, 1) == id) return 2;
+        int a, b, c;
+        pts(f, a, b, c);
+        if (a == id) return 1;
+        if (b == id) return 2;
         return 0;
     }
     // epa3.rs:143-156 and utils/triangle.rs:85-102 (f32).
     NCG_DEV bool seen_by(int f, int point, int opp, const Tol& tol) const {
-        vec3<float> p0 = vf(pt(f, opp)), p1 = vf(pt(f, (opp + 1) % 3)), p2 = vf(pt(f, (opp + 2) % 3));
-        vec3<float> q = vf(point);
-        if (dot(q - p0, normalf(f)) >= -tol.eps_tol_f) return true;
-        float x = norm_sq(cross(p2 - p1, q - p1));
-        return x == 0.0f || fabsf(x) <= tol.affine_eps_f;
+        int a, b, c;
+        pts(f, a, b, c);
+        int i0 = opp == 0 ? a : (opp == 1 ? b : c);
+        int i1 = opp == 0 ? b : (opp == 1 ? c : a);
+        int i2 = opp == 0 ? c : (opp == 1 ? a : b);
+        vec3<float> p0 = vf(i0), p1 = vf(i1), p2 = vf(i2);
+        vec3<float> x = vf(point);
+        if (dot(x - p0, normalf(f)) >= -tol.eps_tol_f) return true;
+        float s = norm_sq(cross(p2 - p1, x - p1));
+        return s == 0.0f || fabsf(s) <= tol.affine_eps_f;
     }
 
-    // ---- Rust BinaryHeap<FaceId> (max-heap on neg_dist) — lane 0 only.
-    NCG_DEV void hput(int pos, int id, real k) {
-        hkey[pos] = k.h;
-        hkey[FC + pos] = k.l;
-        hid[pos] = (uint16_t)id;
+    // ---- binary heap on (neg_dist, earlier push) — one thread only.
+    NCG_DEV static bool before(float4 a, float4 b) {
+        real ka(a.x, a.y), kb(b.x, b.y);
+        if (ka > kb) return true;
+        if (kb > ka) return false;
+        return __float_as_uint(a.z) < __float_as_uint(b.z);
     }
-    NCG_DEV void hmove(int dst, int src) {
-        hkey[dst] = hkey[src];
-        hkey[FC + dst] = hkey[FC + src];
-        hid[dst] = hid[src];
-    }
-    NCG_DEV void heap_sift_up(int start, int pos, int id, real k) {
-        while (pos > start) {
-            int parent = (pos - 1) / 2;
-            if (k <= key(parent)) break;
-            hmove(pos, parent);
+    NCG_DEV void sift_up(int pos, float4 e) {
+        while (pos > 0) {
+            int parent = (pos - 1) >> 1;
+            float4 p = heap[parent];
+            if (!before(e, p)) break;
+            heap[pos] = p;
             pos = parent;
         }
-        hput(pos, id, k);
+        heap[pos] = e;
     }
-    NCG_DEV void heap_push(int& size, int id, real k) {
-        int pos = size++;
-        heap_sift_up(0, pos, id, k);
+    NCG_DEV void sift_down(int pos, int size, float4 e) {
+        for (;;) {
+            int c = 2 * pos + 1;
+            if (c >= size) break;
+            float4 ce = heap[c];
+            if (c + 1 < size) {
+                float4 c2 = heap[c + 1];
+                if (before(c2, ce)) { ce = c2; c = c + 1; }
+            }
+            if (!before(ce, e)) break;
+            heap[pos] = ce;
+            pos = c;
+        }
+        heap[pos] = e;
     }
-    NCG_DEV bool heap_pop(int& size, int& id, real& k) {
-        if (size == 0) return false;
-        size--;
-        int lid = hid[size];
-        real lkey = key(size);
-        if (size == 0) {
-            id = lid;
-            k = lkey;
-            return true;
+    // Drops the entries of deleted faces (the pop order does not change).
+    NCG_DEV void purge(int& size) {
+        int j = 0;
+        for (int i = 0; i < size; ++i) {
+            float4 e = heap[i];
+            if (live(__float_as_uint(e.w))) heap[j++] = e;
         }
-        id = hid[0];
-        k = key(0);
-        // sift_down_to_bottom(0) with the former last element in the hole.
-        int end = size, pos = 0, child = 1;
-        while (end >= 2 && child <= end - 2) {
-            child += (key(child) <= key(child + 1)) ? 1 : 0;
-            hmove(pos, child);
-            pos = child;
-            child = 2 * pos + 1;
+        size = j;
+        for (int i = size / 2 - 1; i >= 0; --i) sift_down(i, size, heap[i]);
+    }
+    // Returns false when the heap is full even after purging.
+    NCG_DEV bool push(int& size, uint32_t& seq, uint32_t ref, real key) {
+        if (size >= FC) {
+            purge(size);
+            if (size >= FC) return false;
         }
-        if (child == end - 1) {
-            hmove(pos, child);
-            pos = child;
-        }
-        heap_sift_up(0, pos, lid, lkey);
+        float4 e = make_float4(key.h, key.l, __uint_as_float(seq++), __uint_as_float(ref));
+        sift_up(size++, e);
         return true;
     }
+    // Pops the first live entry; false when none is left.
+    NCG_DEV bool pop_live(int& size, int& fid, real& key) {
+        while (size > 0) {
+            float4 e = heap[0];
+            size--;
+            if (size > 0) sift_down(0, size, heap[size]);
+            uint32_t r = __float_as_uint(e.w);
+            if (live(r)) {
+                fid = rslot(r);
+                key = real(e.x, e.y);
+                return true;
+            }
+        }
+        return false;
+    }
+};
+
+// Execution policies.
+struct WarpExec {
+    static constexpr int W = 32;
+    NCG_DEV static int lane() { return threadIdx.x & 31; }
+    NCG_DEV static void sync() { __syncwarp(); }
+    NCG_DEV static int bcast(int x) { return __shfl_sync(0xffffffffu, x, 0); }
+    NCG_DEV static uint32_t bcast(uint32_t x) { return __shfl_sync(0xffffffffu, x, 0); }
+    NCG_DEV static real bcast(real x) {
+        return real(__shfl_sync(0xffffffffu, x.h, 0), __shfl_sync(0xffffffffu, x.l, 0));
+    }
+};
+struct ThreadExec {
+    static constexpr int W = 1;
+    NCG_DEV static int lane() { return 0; }
+    NCG_DEV static void sync() {}
+    NCG_DEV static int bcast(int x) { return x; }
+    NCG_DEV static uint32_t bcast(uint32_t x) { return x; }
+    NCG_DEV static real bcast(real x) { return x; }
 };
 
 struct EpaResult {
@@ -203,123 +295,126 @@ struct EpaResult {
     uint32_t status;
 };
 
-NCG_DEV int bcast(int x) { return __shfl_sync(0xffffffffu, x, 0); }
-NCG_DEV real bcastr(real x) {
-    return real(__shfl_sync(0xffffffffu, x.h, 0), __shfl_sync(0xffffffffu, x.l, 0));
-}
-
-// EPA::closest_points.  Called by all 32 lanes of a warp with identical
-// arguments; every lane returns the same result.
-template <class Scan>
-NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol& tol, const Scan& scan, EpaStore& st,
-                           int max_iter) {
-    const int lane = threadIdx.x & 31;
+// EPA::closest_points.  With WarpExec all 32 lanes of a warp call it with
+// identical arguments and every lane returns the same result; with ThreadExec
+// one thread runs it alone.
+template <class E, class Scan>
+NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& tol, const Scan& scan, EpaStore& st,
+                          int max_iter) {
+    const int lane = E::lane();
     EpaResult res;
     res.exit = EPA_NONE;
     res.p1 = res.p2 = res.n = zero3<real>();
     res.iters = 0;
     res.status = 0;
-
     if (dim == 0) {
         res.n = mk(real(0.0f), real(1.0f), real(0.0f));
         res.exit = EPA_OK_DIM0;
         return res;
     }
-    int nv = dim + 1, nf = 0, hsize = 0;
-    const real eps = from_host(tol.eps), eps_tol = from_host(tol.eps_tol), epa_tol = from_host(tol.epa_eps_tol);
+    const real eps_tol = from_host(tol.eps_tol), epa_tol = from_host(tol.epa_eps_tol);
+    const float eps = tol.eps.h;
+    int nv = dim + 1, nfresh = 0, nfree = 0, hsize = 0;
+    uint32_t seq = 0;
     if (lane == 0)
         for (int i = 0; i < nv; ++i) st.put_vertex(i, sv[i]);
-    __syncwarp();
+    E::sync();
 
     if (dim == 3) {
-        vec3<real> v0 = st.vp(0);
-        vec3<real> dp1 = st.vp(1) - v0, dp2 = st.vp(2) - v0, dp3 = st.vp(3) - v0;
-        __syncwarp();
+        vec3<real> v0 = to_r(st.vf(0));
+        vec3<real> dp1 = to_r(st.vf(1)) - v0, dp2 = to_r(st.vf(2)) - v0, dp3 = to_r(st.vf(3)) - v0;
+        E::sync();
         if (dot(cross(dp1, dp2), dp3) > real(0.0f)) {
             if (lane == 0) {
                 CSO a = st.get_vertex(1), b = st.get_vertex(2);
                 st.put_vertex(1, b);
                 st.put_vertex(2, a);
             }
-            __syncwarp();
+            E::sync();
         }
         // Faces [0,1,2] [1,3,2] [0,2,3] [0,3,1], adjacency per epa3.rs:256-264; lanes 0..3.
         const int P[4][3] = {{0, 1, 2}, {1, 3, 2}, {0, 2, 3}, {0, 3, 1}};
         const int A[4][3] = {{3, 1, 2}, {3, 2, 0}, {0, 1, 3}, {2, 1, 0}};
         real d;
-        bool inside = false;
-        if (lane < 4) inside = st.build_face(lane, P[lane][0], P[lane][1], P[lane][2], A[lane][0], A[lane][1],
-                                             A[lane][2], eps, d);
-        unsigned ins = __ballot_sync(0xffffffffu, inside);
-        __syncwarp();
+        unsigned ins = 0;
+        for (int k = lane; k < 4; k += E::W)
+            if (st.build_face(k, 0, P[k][0], P[k][1], P[k][2], mkref(A[k][0], 0), mkref(A[k][1], 0),
+                              mkref(A[k][2], 0), eps, d))
+                ins |= 1u << k;
+        if (E::W > 1) ins = __reduce_or_sync(0xffffffffu, ins);
+        E::sync();
         int fail = 0;
         if (lane == 0) {
             for (int k = 0; k < 4; ++k) {
                 if (!(ins >> k & 1u)) continue;
                 // dist_k = normal_k . vertices[k] (epa3.rs:277,282,287,292)
-                real dk = dot(st.normal(k), st.vp(k));
+                real dk = dot(st.normal(k), to_r(st.vf(k)));
                 if (-dk > eps_tol) { fail = 1; break; }
-                st.heap_push(hsize, k, -dk);
+                st.push(hsize, seq, mkref(k, 0), -dk);
             }
         }
-        (void)d;
-        fail = bcast(fail);
-        hsize = bcast(hsize);
-        nf = 4;
-        if (fail) { res.exit = EPA_NONE; res.status |= NCG_STATUS_EPA_FAILED; return res; }
+        fail = E::bcast(fail);
+        hsize = E::bcast(hsize);
+        seq = E::bcast(seq);
+        nfresh = 4;
+        if (fail) { res.status |= NCG_STATUS_EPA_FAILED; return res; }
     } else {
         if (dim == 1) {
-            vec3<real> dpt = st.vp(1) - st.vp(0);
+            vec3<real> dpt = to_r(st.vf(1)) - to_r(st.vf(0));
             vec3<real> a = fabs(dpt.x) > fabs(dpt.y) ? mk(dpt.z, real(0.0f), -dpt.x) : mk(real(0.0f), -dpt.z, dpt.y);
             a = a / vnorm(a);
             vec3<real> dir = cross(a, dpt);
             CSO c = cso_support(g, to_f(dir), scan);
             if (lane == 0) st.put_vertex(2, c);
             nv = 3;
-            __syncwarp();
+            E::sync();
         }
         real d;
-        if (lane == 0) (void)st.build_face(0, 0, 1, 2, 1, 1, 1, eps, d);
-        if (lane == 1) (void)st.build_face(1, 0, 2, 1, 0, 0, 0, eps, d);
-        __syncwarp();
+        if (lane == 0) (void)st.build_face(0, 0, 0, 1, 2, mkref(1, 0), mkref(1, 0), mkref(1, 0), eps, d);
+        if (lane == (E::W > 1 ? 1 : 0))
+            (void)st.build_face(1, 0, 0, 2, 1, mkref(0, 0), mkref(0, 0), mkref(0, 0), eps, d);
+        E::sync();
         if (lane == 0) {
-            st.heap_push(hsize, 0, real(0.0f));
-            st.heap_push(hsize, 1, real(0.0f));
+            st.push(hsize, seq, mkref(0, 0), real(0.0f));
+            st.push(hsize, seq, mkref(1, 0), real(0.0f));
         }
         hsize = 2;
-        nf = 2;
-        __syncwarp();
+        seq = 2;
+        nfresh = 2;
+        E::sync();
     }
     if (hsize == 0) {  // the reference panics on heap.peek().unwrap()
-        res.exit = EPA_NONE;
         res.status |= NCG_STATUS_EPA_NO_FACE;
         return res;
     }
-    int best = bcast(lane == 0 ? (int)st.hid[0] : 0);
+    // best face (its points and normal are kept: its slot may be recycled)
+    int bslot = rslot(__float_as_uint(st.heap[0].w));
+    int b0, b1, b2;
+    st.pts(bslot, b0, b1, b2);
+    vec3<float> bn = st.normalf(bslot);
     real max_dist = dw_max();
     int niter = 0;
 
     for (;;) {
-        // ---- pop the closest non-deleted face (lane 0)
+        // ---- pop the closest live face (lane 0)
         int fid = -1;
         real key(0.0f);
         if (lane == 0) {
-            int id;
-            real k;
-            while (st.heap_pop(hsize, id, k)) {
-                if (!st.fdel[id]) { fid = id; key = k; break; }
-            }
+            if (!st.pop_live(hsize, fid, key)) fid = -1;
         }
-        fid = bcast(fid);
-        key = bcastr(key);
-        hsize = bcast(hsize);
+        fid = E::bcast(fid);
+        key = E::bcast(key);
+        hsize = E::bcast(hsize);
+        E::sync();
         if (fid < 0) {
-            st.face_points(best, res.p1, res.p2);
-            res.n = st.normal(best);
+            st.face_points(b0, b1, b2, res.p1, res.p2);
+            res.n = to_r(bn);
             res.exit = EPA_OK_HEAP_EMPTY;
             return res;
         }
         res.iters++;
+        int f0, f1, f2;
+        st.pts(fid, f0, f1, f2);
         vec3<float> fnf = st.normalf(fid);
         vec3<real> fnrm = to_r(fnf);
         CSO c = cso_support(g, fnf, scan);
@@ -328,14 +423,15 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
         if (lane == 0) st.put_vertex(sup, c);
         real cand = dot(to_r(c.p), fnrm);
         if (cand < max_dist) {
-            best = fid;
+            b0 = f0; b1 = f1; b2 = f2;
+            bn = fnf;
             max_dist = cand;
         }
         real curr = -key;
-        __syncwarp();
+        E::sync();
         if (max_dist - curr < epa_tol) {
-            st.face_points(best, res.p1, res.p2);
-            res.n = st.normal(best);
+            st.face_points(b0, b1, b2, res.p1, res.p2);
+            res.n = to_r(bn);
             res.exit = EPA_OK_CONVERGED;
             return res;
         }
@@ -343,121 +439,134 @@ NCG_DEV EpaResult epa_warp(const PairGeom& g, int dim, const CSO* sv, const Tol&
         // ---- silhouette flood fill (lane 0), recursion order kept with a stack
         int nsil = 0, ovf = 0;
         if (lane == 0) {
-            st.fdel[fid] = 1;
-            int a0 = st.adj(fid, 0), a1 = st.adj(fid, 1), a2 = st.adj(fid, 2);
-            int o0 = st.next_ccw(a0, st.pt(fid, 0));
-            int o1 = st.next_ccw(a1, st.pt(fid, 1));
-            int o2 = st.next_ccw(a2, st.pt(fid, 2));
+            uint32_t a0 = st.adj(fid, 0), a1 = st.adj(fid, 1), a2 = st.adj(fid, 2);
+            int o0 = st.next_ccw(rslot(a0), f0);
+            int o1 = st.next_ccw(rslot(a1), f1);
+            int o2 = st.next_ccw(rslot(a2), f2);
+            st.kill(fid, nfree);
             int top = 0;
             if (st.TC < 3) ovf = 1;
             else {
-                st.tface[top] = (uint16_t)a2; st.topp[top++] = (uint8_t)o2;
-                st.tface[top] = (uint16_t)a1; st.topp[top++] = (uint8_t)o1;
-                st.tface[top] = (uint16_t)a0; st.topp[top++] = (uint8_t)o0;
+                st.tref[top] = a2; st.topp[top++] = (uint8_t)o2;
+                st.tref[top] = a1; st.topp[top++] = (uint8_t)o1;
+                st.tref[top] = a0; st.topp[top++] = (uint8_t)o0;
             }
             while (top > 0 && !ovf) {
                 --top;
-                int id = st.tface[top], opp = st.topp[top];
-                if (st.fdel[id]) continue;
+                uint32_t r = st.tref[top];
+                int opp = st.topp[top];
+                if (!st.live(r)) continue;
+                int id = rslot(r);
                 if (!st.seen_by(id, sup, opp, tol)) {
                     if (nsil >= st.SC) { ovf = 1; break; }
-                    st.sface[nsil] = (uint16_t)id;
+                    st.sref[nsil] = r;
                     st.sopp[nsil] = (uint8_t)opp;
                     nsil++;
                 } else {
-                    st.fdel[id] = 1;
                     int k1 = (opp + 2) % 3, k2 = opp;
-                    int b1 = st.adj(id, k1), b2 = st.adj(id, k2);
-                    int q1 = st.next_ccw(b1, st.pt(id, k1));
-                    int q2 = st.next_ccw(b2, st.pt(id, k2));
+                    uint32_t r1 = st.adj(id, k1), r2 = st.adj(id, k2);
+                    int q1 = st.next_ccw(rslot(r1), st.pt(id, k1));
+                    int q2 = st.next_ccw(rslot(r2), st.pt(id, k2));
+                    st.kill(id, nfree);
                     if (top + 2 > st.TC) { ovf = 1; break; }
-                    st.tface[top] = (uint16_t)b2; st.topp[top++] = (uint8_t)q2;
-                    st.tface[top] = (uint16_t)b1; st.topp[top++] = (uint8_t)q1;
+                    st.tref[top] = r2; st.topp[top++] = (uint8_t)q2;
+                    st.tref[top] = r1; st.topp[top++] = (uint8_t)q1;
                 }
             }
         }
-        nsil = bcast(nsil);
-        ovf = bcast(ovf);
-        __syncwarp();
+        nsil = E::bcast(nsil);
+        ovf = E::bcast(ovf);
+        nfree = E::bcast(nfree);
+        E::sync();
         if (ovf) { res.exit = EPA_OVERFLOW; return res; }
         if (nsil == 0) {
-            res.exit = EPA_NONE;
             res.status |= NCG_STATUS_EPA_FAILED;
             return res;
         }
 
-        // ---- new faces, one lane per surviving silhouette edge
-        const int first_new = nf;
+        // ---- which silhouette edges still border a live face (after the whole fill)
+        for (int k = lane; k < nsil; k += E::W) st.sflag[k] = st.live(st.sref[k]) ? 1 : 0;
+        E::sync();
+        // ---- slots for the new faces, in silhouette order (lane 0)
         int built = 0;
-        for (int base = 0; base < nsil; base += 32) {
-            int k = base + lane;
-            bool live = false;
-            int sf = 0, so = 0;
-            if (k < nsil) {
-                sf = st.sface[k];
-                so = st.sopp[k];
-                live = !st.fdel[sf];
+        if (lane == 0) {
+            int first = -1, prev = -1;
+            for (int k = 0; k < nsil; ++k) {
+                if (!(st.sflag[k] & 1)) continue;
+                int slot;
+                uint32_t gg;
+                if (nfree > 0) { slot = (int)st.freel[--nfree]; gg = st.gen(slot); }
+                else if (nfresh < st.FC) { slot = nfresh++; gg = 0; }
+                else { ovf = 1; break; }
+                uint32_t r = mkref(slot, gg);
+                st.snew[k] = r;
+                if (prev >= 0) { st.snext[prev] = r; st.sprev[k] = st.snew[prev]; }
+                if (first < 0) first = k;
+                prev = k;
+                built++;
             }
-            unsigned m = __ballot_sync(0xffffffffu, live);
-            int rank = __popc(m & ((1u << lane) - 1u));
-            int id = first_new + built + rank;
-            if (first_new + built + __popc(m) > st.FC) { ovf = 1; }
-            if (live && !ovf) {
-                int q1 = st.pt(sf, (so + 2) % 3), q2 = st.pt(sf, (so + 1) % 3);
-                real dist;
-                bool in = st.build_face(id, q1, q2, sup, sf, id + 1, id - 1, eps, dist);
-                st.sdist[k] = dist.h;
-                st.sdist[st.SC + k] = dist.l;
-                st.sflag[k] = (uint8_t)(1 | (in ? 2 : 0));
-            } else if (k < nsil) {
-                st.sflag[k] = 0;
+            if (!ovf && built > 0) {  // close the ring (epa3.rs:415-416)
+                st.snext[prev] = st.snew[first];
+                st.sprev[first] = st.snew[prev];
             }
-            built += __popc(m);
         }
-        __syncwarp();
+        ovf = E::bcast(ovf);
+        built = E::bcast(built);
+        nfree = E::bcast(nfree);
+        nfresh = E::bcast(nfresh);
+        E::sync();
         if (ovf) { res.exit = EPA_OVERFLOW; return res; }
+        if (built == 0) {  // epa3.rs:409-413
+            res.status |= NCG_STATUS_EPA_FAILED;
+            return res;
+        }
+        // ---- build the new faces, one lane per live edge
+        for (int k = lane; k < nsil; k += E::W) {
+            if (!(st.sflag[k] & 1)) continue;
+            uint32_t sr = st.sref[k];
+            int sf = rslot(sr), so = st.sopp[k];
+            int q1 = st.pt(sf, (so + 2) % 3), q2 = st.pt(sf, (so + 1) % 3);
+            uint32_t r = st.snew[k];
+            real dist;
+            bool in = st.build_face(rslot(r), r >> 16, q1, q2, sup, sr, st.snext[k], st.sprev[k], eps, dist);
+            st.sdist[k] = make_float2(dist.h, dist.l);
+            st.sflag[k] = (uint8_t)(1 | (in ? 2 : 0));
+        }
+        E::sync();
 
         // ---- ordered post-pass (lane 0): adjacency, checks, heap pushes
-        int outcome = 0;  // 0 continue, 1 numeric return, 2 None
+        int outcome = 0;  // 0 continue, 1 numeric return, 2 None, 3 overflow
         if (lane == 0) {
-            int id = first_new;
             for (int k = 0; k < nsil; ++k) {
                 uint8_t fl = st.sflag[k];
                 if (!(fl & 1)) continue;
-                int sf = st.sface[k], so = st.sopp[k];
-                st.set_adj(sf, (so + 1) % 3, id);
+                int sf = rslot(st.sref[k]), so = st.sopp[k];
+                st.set_adj(sf, (so + 1) % 3, st.snew[k]);
                 if (fl & 2) {
-                    real dist(st.sdist[k], st.sdist[st.SC + k]);
+                    real dist(st.sdist[k].x, st.sdist[k].y);
                     if (dist < curr) { outcome = 1; break; }
                     if (-dist > eps_tol) { outcome = 2; break; }
-                    st.heap_push(hsize, id, -dist);
+                    if (!st.push(hsize, seq, st.snew[k], -dist)) { outcome = 3; break; }
                 }
-                id++;
             }
         }
-        outcome = bcast(outcome);
-        hsize = bcast(hsize);
-        __syncwarp();
+        outcome = E::bcast(outcome);
+        hsize = E::bcast(hsize);
+        seq = E::bcast(seq);
+        E::sync();
         if (outcome == 1) {
-            st.face_points(fid, res.p1, res.p2);
+            st.face_points(f0, f1, f2, res.p1, res.p2);
             res.n = fnrm;
             res.exit = EPA_OK_NUMERIC;
             return res;
         }
-        if (outcome == 2 || built == 0) {
-            res.exit = EPA_NONE;
+        if (outcome == 2) {
             res.status |= NCG_STATUS_EPA_FAILED;
             return res;
         }
-        nf = first_new + built;
-        if (lane == 0) {
-            st.set_adj(first_new, 2, nf - 1);
-            st.set_adj(nf - 1, 1, first_new);
-        }
-        __syncwarp();
+        if (outcome == 3) { res.exit = EPA_OVERFLOW; return res; }
         niter += 1;
         if (niter > max_iter) {
-            res.exit = EPA_NONE;
             res.status |= NCG_STATUS_EPA_MAX_ITER;
             return res;
         }

@@ -6,12 +6,16 @@
 //   2. gjk_thread   1 thread/pair over the analytic list (persistent grid).
 //   3. gjk_warp     1 warp/pair over the hull list (dynamic queue); the hull
 //                   arg-max is warp-parallel with coalesced 128-bit loads.
-//   4. epa tier A   contact only: 1 warp per intersecting pair, polytope of up
-//                   to 128 vertices in shared memory (~9 warps per SM).
-//   5. epa tier B   pairs whose polytope outgrew tier A, re-run with up to
-//                   1024 vertices in shared memory (1 warp per SM).
-//   6. epa tier C   pairs that outgrew tier B, re-run in a global-memory slab
-//                   per warp (up to 10240 vertices).
+//   4. epa_thread   contact only, intersecting pairs of analytic shapes: one
+//                   thread per pair, polytope of up to 48 vertices in the
+//                   thread's local memory.
+//   5. epa tier A   ConvexHull pairs and pairs that outgrew epa_thread: one warp
+//                   per pair, up to 128 vertices in shared memory.
+//   6. epa tier B   pairs that outgrew tier A: up to 1280 vertices in shared
+//                   memory (1 warp per SM).
+//   7. epa tier C   pairs that outgrew tier B: a global-memory slab per warp
+//                   (up to 10240 vertices).
+// A pair that outgrows a stage is re-run by the next one from GJK's simplex.
 // Pairs are independent; the GJK stage writes its outputs directly or appends
 // the final simplex to the EPA queue.
 #include <cuda_runtime.h>
@@ -67,16 +71,16 @@ struct __align__(16) EpaItem {
 struct DevCounters {
     unsigned long long n_analytic, n_hull;
     unsigned long long hull_next;
-    unsigned long long epa_count[3];  // items queued for tier A (all), B, C
-    unsigned long long epa_next[3];
+    unsigned long long n_items;       // EPA work items written
+    unsigned long long epa_count[4];  // items queued for: thread stage, tier A, B, C
+    unsigned long long epa_next[4];
     unsigned long long gjk_iters, epa_iters;
-    unsigned long long pad[5];
 };
 
 struct Scratch {
     uint32_t* analytic;
     uint32_t* hull;
-    uint32_t* ovf[3];  // ovf[1]: items for tier B, ovf[2]: items for tier C
+    uint32_t* queue[4];  // item indices per EPA stage
     EpaItem* items;
     DevCounters* ctr;
     char* slabs;
@@ -84,11 +88,15 @@ struct Scratch {
     int n_slabs;
 };
 
-// EPA store capacities per tier: vertices, faces, silhouette edges, flood-fill stack.
+// EPA store capacities per stage: vertices, live face slots (about twice the
+// vertices), silhouette edges, flood-fill stack.  Stage 0 is the per-thread
+// store, 1-3 the warp tiers A, B, C.
 template <int T> struct EpaTier;
-template <> struct EpaTier<0> { static constexpr int VC = 128, FC = 512, SC = 64, TC = 256; };
-template <> struct EpaTier<1> { static constexpr int VC = 1024, FC = 4096, SC = 512, TC = 2048; };
-template <> struct EpaTier<2> { static constexpr int VC = 10240, FC = 65535, SC = 4096, TC = 16384; };
+template <> struct EpaTier<0> { static constexpr int VC = 48, FC = 2 * 48 + 16, SC = 32, TC = 96; };
+template <> struct EpaTier<1> { static constexpr int VC = 128, FC = 2 * 128 + 64, SC = 64, TC = 256; };
+template <> struct EpaTier<2> { static constexpr int VC = 1280, FC = 2 * 1280 + 64, SC = 512, TC = 2048; };
+template <> struct EpaTier<3> { static constexpr int VC = 10240, FC = 2 * 10240 + 64, SC = 4096, TC = 16384; };
+static_assert(EpaTier<3>::FC < 65536 && EpaTier<3>::VC < 65536, "16-bit face and vertex indices");
 template <int T> size_t tier_bytes() {
     return EpaStore::bytes(EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC);
 }
@@ -186,9 +194,10 @@ NCG_DEV vec3<float> initial_dir(const QueryParams& qp, const ncg_batch& b, uint3
 
 // Runs one pair through GJK; writes its outputs or its EPA work item.
 // All lanes of a warp call this with the same pair when Scan is WarpScan.
+// epa_queue: the EPA stage the pair starts in (0 = thread stage, 1 = warp tier A).
 template <class Scan>
 NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, uint32_t i,
-                      const Scan& scan, bool writer, unsigned long long& iter_acc) {
+                      const Scan& scan, bool writer, unsigned long long& iter_acc, int epa_queue) {
     PairGeom g;
     load_shape(b, b.g1[i], g.g1);
     load_shape(b, b.g2[i], g.g2);
@@ -204,7 +213,9 @@ NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& 
     iter_acc += iters;
     if (qp.query == Q_CONTACT && r.kind == GJK_INTERSECTION) {
         if (writer) {
-            unsigned long long slot = atomicAdd(&s.ctr->epa_count[0], 1ull);
+            unsigned long long slot = atomicAdd(&s.ctr->n_items, 1ull);
+            unsigned long long pos = atomicAdd(&s.ctr->epa_count[epa_queue], 1ull);
+            s.queue[epa_queue][pos] = (uint32_t)slot;
             EpaItem& it = s.items[slot];
             it.pair = i;
             it.gjk_iters = iters;
@@ -262,7 +273,7 @@ __global__ void __launch_bounds__(128) k_gjk_thread(ncg_batch b, QueryParams qp,
     const unsigned long long rounds = (n + stride - 1) / stride;
     for (unsigned long long r = 0; r < rounds; ++r) {
         unsigned long long k = start + r * stride;
-        if (k < n) gjk_pair(b, qp, o, s, s.analytic[k], scan, true, acc);
+        if (k < n) gjk_pair(b, qp, o, s, s.analytic[k], scan, true, acc, 0);
     }
     warp_add(&s.ctr->gjk_iters, acc);
 }
@@ -278,7 +289,7 @@ __global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, O
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= n) break;
         unsigned long long a = 0;
-        gjk_pair(b, qp, o, s, s.hull[k], scan, lane == 0, a);
+        gjk_pair(b, qp, o, s, s.hull[k], scan, lane == 0, a, 1);
         if (lane == 0) acc += a;
     }
     warp_add(&s.ctr->gjk_iters, acc);
@@ -322,21 +333,24 @@ NCG_DEV void load_simplex(const EpaItem& it, CSO* sv) {
     }
 }
 
-// EPA tier T: tiers 0 and 1 keep the polytope in dynamic shared memory (one
+// EPA tier t: tiers 0 and 1 keep the polytope in dynamic shared memory (one
 // warp per block), tier 2 in a global-memory slab per warp.  A pair whose
 // polytope outgrows its tier is queued for the next tier and re-run there from
-// GJK's simplex; at tier 2 it ends with NCG_STATUS_EPA_CAPACITY.
-template <int T>
-__global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+// GJK's simplex; at tier 2 it ends with NCG_STATUS_EPA_CAPACITY.  One kernel
+// serves the three tiers (runtime capacities) to keep the code footprint small.
+struct TierCaps {
+    int tier, VC, FC, SC, TC;
+};
+__global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs o, Scratch s, TierCaps tc) {
     extern __shared__ __align__(16) char smem[];
     const unsigned lane = threadIdx.x & 31u;
-    using C = EpaTier<T>;
+    const int T = tc.tier;  // 1, 2 or 3
     EpaStore st;
-    if (T < 2) {
-        st.carve(smem, C::VC, C::FC, C::SC, C::TC);
+    if (T < 3) {
+        st.carve(smem, tc.VC, tc.FC, tc.SC, tc.TC);
     } else {
         if (blockIdx.x >= (unsigned)s.n_slabs) return;
-        st.carve(s.slabs + (size_t)blockIdx.x * s.slab_bytes, C::VC, C::FC, C::SC, C::TC);
+        st.carve(s.slabs + (size_t)blockIdx.x * s.slab_bytes, tc.VC, tc.FC, tc.SC, tc.TC);
     }
     const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[T];
     WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
@@ -346,16 +360,16 @@ __global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs
         if (lane == 0) k = atomicAdd(&s.ctr->epa_next[T], 1ull);
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= n) break;
-        const uint32_t item = T == 0 ? (uint32_t)k : s.ovf[T][k];
+        const uint32_t item = s.queue[T][k];
         const EpaItem& it = s.items[item];
         PairGeom g = load_geom(b, it.pair);
         CSO sv[4];
         load_simplex(it, sv);
-        EpaResult r = epa_warp(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
-        if (r.exit == EPA_OVERFLOW && T < 2) {
+        EpaResult r = epa_run<WarpExec>(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
+        if (r.exit == EPA_OVERFLOW && T < 3) {
             if (lane == 0) {
                 unsigned long long q = atomicAdd(&s.ctr->epa_count[T + 1], 1ull);
-                s.ovf[T + 1][q] = item;
+                s.queue[T + 1][q] = item;
             }
         } else {
             acc += r.iters;
@@ -372,6 +386,37 @@ __global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs
         __syncwarp();
     }
     if (lane == 0 && acc) atomicAdd(&s.ctr->epa_iters, acc);
+}
+template <int T> TierCaps caps() { return TierCaps{T, EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC}; }
+
+// Thread stage: one thread per pair of analytic shapes, the polytope in the
+// thread's local memory.  A pair that outgrows it goes to warp tier A.
+constexpr size_t THREAD_STORE_BYTES =
+    EpaStore::bytes(EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
+__global__ void __launch_bounds__(128) k_epa_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+    __align__(16) char buf[THREAD_STORE_BYTES];
+    EpaStore st;
+    st.carve(buf, EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
+    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[0];
+    ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
+    unsigned long long acc = 0;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const uint32_t item = s.queue[0][k];
+        const EpaItem& it = s.items[item];
+        PairGeom g = load_geom(b, it.pair);
+        CSO sv[4];
+        load_simplex(it, sv);
+        EpaResult r = epa_run<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
+        if (r.exit == EPA_OVERFLOW) {
+            unsigned long long q = atomicAdd(&s.ctr->epa_count[1], 1ull);
+            s.queue[1][q] = item;
+        } else {
+            acc += r.iters;
+            write_epa(o, it, r, 0);
+        }
+    }
+    warp_add(&s.ctr->epa_iters, acc);
 }
 
 // ------------------------------------------------------------------ host side
@@ -417,7 +462,7 @@ struct ncg_ctx {
     int num_sms = 0;
     int tol_mode = NCG_TOL_REFERENCE;
     int warm = NCG_WARM_NONE;
-    int occ_thread = 1, occ_warp = 1, occ_epa0 = 1, occ_epa1 = 1;
+    int occ_thread = 1, occ_warp = 1, occ_epa0 = 1, occ_epa1 = 1, occ_ethread = 1;
     char* scratch = nullptr;
     size_t scratch_cap_pairs = 0;
     char* slabs = nullptr;
@@ -443,7 +488,7 @@ bool ensure_scratch(ncg_ctx* c, uint64_t n) {
     if (c->scratch) cudaFree(c->scratch);
     c->scratch = nullptr;
     uint64_t cap = n < 1024 ? 1024 : n;
-    size_t bytes = 4 * 4 * cap + sizeof(EpaItem) * cap + sizeof(DevCounters) + 1024;
+    size_t bytes = 6 * 4 * cap + sizeof(EpaItem) * cap + sizeof(DevCounters) + 1024;
     if (!cuda_ok(cudaMalloc(&c->scratch, bytes), "cudaMalloc(scratch)")) return false;
     c->scratch_cap_pairs = cap;
     return true;
@@ -457,9 +502,7 @@ Scratch carve_scratch(ncg_ctx* c) {
     s.items = (EpaItem*)p; p += sizeof(EpaItem) * cap;
     s.analytic = (uint32_t*)p; p += 4 * cap;
     s.hull = (uint32_t*)p; p += 4 * cap;
-    s.ovf[0] = nullptr;
-    s.ovf[1] = (uint32_t*)p; p += 4 * cap;
-    s.ovf[2] = (uint32_t*)p;
+    for (int q = 0; q < 4; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * cap; }
     s.slabs = c->slabs;
     s.slab_bytes = c->slab_bytes;
     s.n_slabs = c->n_slabs;
@@ -503,13 +546,15 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     mark(2);
     launches += 3;
     if (query == Q_CONTACT) {
-        k_epa<0><<<c->num_sms * c->occ_epa0, 32, tier_bytes<0>(), st>>>(bb, qp, o, s);
+        k_epa_thread<<<c->num_sms * c->occ_ethread, 128, 0, st>>>(bb, qp, o, s);
         mark(3);
-        k_epa<1><<<c->num_sms * c->occ_epa1, 32, tier_bytes<1>(), st>>>(bb, qp, o, s);
+        k_epa<<<c->num_sms * c->occ_epa0, 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>());
         mark(4);
-        k_epa<2><<<c->n_slabs, 32, 0, st>>>(bb, qp, o, s);
+        k_epa<<<c->num_sms * c->occ_epa1, 32, tier_bytes<2>(), st>>>(bb, qp, o, s, caps<2>());
         mark(5);
-        launches += 3;
+        k_epa<<<c->n_slabs, 32, 0, st>>>(bb, qp, o, s, caps<3>());
+        mark(6);
+        launches += 4;
     }
     if (!cuda_ok(cudaGetLastError(), "kernel launch")) return NCG_ECUDA;
     if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st),
@@ -537,17 +582,18 @@ int ncg_ctx_create(ncg_ctx** out, int device) {
     ncg_ctx* c = new ncg_ctx();
     c->device = device;
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-    cudaFuncSetAttribute(k_epa<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<0>());
-    cudaFuncSetAttribute(k_epa<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<1>());
+    cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<2>());
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_thread, k_gjk_thread, 128, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_warp, k_gjk_warp, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa0, k_epa<0>, 32, tier_bytes<0>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa1, k_epa<1>, 32, tier_bytes<1>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa0, k_epa, 32, tier_bytes<1>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa1, k_epa, 32, tier_bytes<2>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_ethread, k_epa_thread, 128, 0);
+    if (c->occ_ethread < 1) c->occ_ethread = 1;
     if (c->occ_thread < 1) c->occ_thread = 1;
     if (c->occ_warp < 1) c->occ_warp = 1;
     if (c->occ_epa0 < 1) c->occ_epa0 = 1;
     if (c->occ_epa1 < 1) c->occ_epa1 = 1;
-    c->slab_bytes = (tier_bytes<2>() + 255) & ~size_t(255);
+    c->slab_bytes = (tier_bytes<3>() + 255) & ~size_t(255);
     c->n_slabs = c->num_sms;
     if (!cuda_ok(cudaMalloc(&c->slabs, c->slab_bytes * c->n_slabs), "cudaMalloc(slabs)") ||
         !cuda_ok(cudaMallocHost(&c->host_ctr, sizeof(DevCounters)), "cudaMallocHost")) {
@@ -624,8 +670,8 @@ int ncg_get_stats(ncg_ctx* c, ncg_stats* out) {
     // host_ctr was filled by an asynchronous copy at the end of the last call;
     // the caller synchronises the stream before reading the statistics.
     out->n_pairs = c->last.n_pairs;
-    out->n_epa = c->host_ctr->epa_count[0];
-    out->n_epa_overflow = c->host_ctr->epa_count[1];
+    out->n_epa = c->host_ctr->n_items;
+    out->n_epa_overflow = c->host_ctr->epa_count[2];
     out->gjk_iters = c->host_ctr->gjk_iters;
     out->epa_iters = c->host_ctr->epa_iters;
     out->kernels_launched = c->launches;
@@ -785,14 +831,14 @@ int ncg_proximity_batch_host(ncg_ctx* c, const ncg_batch* b, float margin, uint8
 // ------------------------------------------------------------------ no-allocation entry point
 // ncg_contact_batch_noalloc runs the contact pipeline on a fixed scratch array
 // in the library's device image instead of context-owned allocations.  Layout
-// of the array: counters (256 B), EPA work items, routing lists and tier
-// queues (4 x 4 B per pair), one tier-C EPA slab.
+// of the array: counters (256 B), EPA work items, routing lists and stage
+// queues (6 x 4 B per pair), one tier-C EPA slab.
 namespace {
 constexpr uint64_t NA_MAX_PAIRS = NCG_NOALLOC_MAX_PAIRS;
 constexpr size_t NA_SLAB_BYTES =
-    (EpaStore::bytes(EpaTier<2>::VC, EpaTier<2>::FC, EpaTier<2>::SC, EpaTier<2>::TC) + 255) & ~size_t(255);
+    (EpaStore::bytes(EpaTier<3>::VC, EpaTier<3>::FC, EpaTier<3>::SC, EpaTier<3>::TC) + 255) & ~size_t(255);
 constexpr size_t NA_ITEMS_BYTES = sizeof(EpaItem) * NA_MAX_PAIRS;
-constexpr size_t NA_LISTS_BYTES = 4 * 4 * NA_MAX_PAIRS;
+constexpr size_t NA_LISTS_BYTES = 6 * 4 * NA_MAX_PAIRS;
 constexpr size_t NA_BYTES = 256 + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_SLAB_BYTES;
 static_assert(sizeof(DevCounters) <= 256, "counters must fit their slot");
 }  // namespace
@@ -804,7 +850,7 @@ namespace {
 struct NoallocDevice {
     bool ready;
     char* base;  // device address of g_noalloc_scratch on this device
-    int num_sms, occ_thread, occ_warp, occ_epa0, occ_epa1;
+    int num_sms, occ_thread, occ_warp, occ_epa0, occ_epa1, occ_ethread;
 };
 std::mutex g_noalloc_mu;
 constexpr int NA_MAX_DEVICES = 64;
@@ -822,12 +868,13 @@ int noalloc_setup(int dev, NoallocDevice& out) {
         d.base = (char*)p;
         if (!cuda_ok(cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev), "device attribute"))
             return NCG_ECUDA;
-        cudaFuncSetAttribute(k_epa<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<0>());
-        cudaFuncSetAttribute(k_epa<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<1>());
+        cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<2>());
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_thread, k_gjk_thread, 128, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_warp, k_gjk_warp, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_epa0, k_epa<0>, 32, tier_bytes<0>());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_epa1, k_epa<1>, 32, tier_bytes<1>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_epa0, k_epa, 32, tier_bytes<1>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_epa1, k_epa, 32, tier_bytes<2>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_ethread, k_epa_thread, 128, 0);
+        if (d.occ_ethread < 1) d.occ_ethread = 1;
         if (d.occ_thread < 1) d.occ_thread = 1;
         if (d.occ_warp < 1) d.occ_warp = 1;
         if (d.occ_epa0 < 1) d.occ_epa0 = 1;
@@ -871,9 +918,7 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     s.items = (EpaItem*)p; p += NA_ITEMS_BYTES;
     s.analytic = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
     s.hull = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
-    s.ovf[0] = nullptr;
-    s.ovf[1] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
-    s.ovf[2] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
+    for (int q = 0; q < 4; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS; }
     s.slabs = p;
     s.slab_bytes = NA_SLAB_BYTES;
     s.n_slabs = 1;
@@ -894,8 +939,9 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
     k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s);
     k_gjk_warp<<<d.num_sms * d.occ_warp, 128, 0, st>>>(bb, qp, o, s);
-    k_epa<0><<<d.num_sms * d.occ_epa0, 32, tier_bytes<0>(), st>>>(bb, qp, o, s);
-    k_epa<1><<<d.num_sms * d.occ_epa1, 32, tier_bytes<1>(), st>>>(bb, qp, o, s);
-    k_epa<2><<<1, 32, 0, st>>>(bb, qp, o, s);
+    k_epa_thread<<<d.num_sms * d.occ_ethread, 128, 0, st>>>(bb, qp, o, s);
+    k_epa<<<d.num_sms * d.occ_epa0, 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>());
+    k_epa<<<d.num_sms * d.occ_epa1, 32, tier_bytes<2>(), st>>>(bb, qp, o, s, caps<2>());
+    k_epa<<<1, 32, 0, st>>>(bb, qp, o, s, caps<3>());
     return cuda_ok(cudaGetLastError(), "noalloc kernel launch") ? NCG_OK : NCG_ECUDA;
 }

@@ -781,6 +781,50 @@ template <class S> struct RustBinaryHeap {
     }
 };
 
+// Priority queue with a strict total order: larger neg_dist first, then the
+// earlier push (FIFO among equal keys).  The pop order is then a function of
+// the set of entries alone, whatever the container; the kernels use this order
+// (their heap recycles face slots and purges deleted entries).  Equal keys are
+// the only case where it differs from Rust's BinaryHeap, whose tie order is an
+// implementation detail of the Rust version.
+template <class S> struct SeqHeap {
+    struct E {
+        size_t id;
+        S neg_dist;
+        uint64_t seq;
+    };
+    std::vector<E> data;
+    uint64_t next_seq = 0;
+    static bool before(const E& a, const E& b) {  // a pops before b
+        if (a.neg_dist > b.neg_dist) return true;
+        if (b.neg_dist > a.neg_dist) return false;
+        return a.seq < b.seq;
+    }
+    void clear() { data.clear(); next_seq = 0; }
+    size_t size() const { return data.size(); }
+    void push(FaceId<S> f) { data.push_back(E{f.id, f.neg_dist, next_seq++}); }
+    size_t best() const {
+        size_t b = 0;
+        for (size_t i = 1; i < data.size(); ++i)
+            if (before(data[i], data[b])) b = i;
+        return b;
+    }
+    FaceId<S> top() const { return FaceId<S>{data[best()].id, data[best()].neg_dist}; }
+    bool pop(FaceId<S>* out) {
+        if (data.empty()) return false;
+        size_t b = best();
+        *out = FaceId<S>{data[b].id, data[b].neg_dist};
+        data.erase(data.begin() + (long)b);
+        return true;
+    }
+};
+template <class S> inline FaceId<S> heap_top(const RustBinaryHeap<S>& h) { return h.data[0]; }
+template <class S> inline FaceId<S> heap_top(const SeqHeap<S>& h) { return h.top(); }
+
+// The reference instantiations (N == S) keep Rust's heap; the kernels' split uses SeqHeap.
+template <class N, class S> struct HeapFor { using type = SeqHeap<S>; };
+template <class T> struct HeapFor<T, T> { using type = RustBinaryHeap<T>; };
+
 // The polytope's expansion (triangle projection, visibility) runs in N; the
 // face normal is computed in S and stored in N; distances, heap keys and the
 // termination test are in S.  With N = S this is the reference's EPA exactly.
@@ -796,7 +840,7 @@ template <class N, class S> struct EPA {
     std::vector<CSOPoint<N>> vertices;
     std::vector<Face<N>> faces;
     std::vector<std::pair<size_t, size_t>> silhouette;  // (face_id, opp_pt_id)
-    RustBinaryHeap<S> heap;
+    typename HeapFor<N, S>::type heap;
     const Tol<S>* tol = nullptr;
 
     V3<S> vp(size_t i) const { return cvt<S>(vertices[i].point); }
@@ -809,9 +853,11 @@ template <class N, class S> struct EPA {
         f.pts[0] = p0; f.pts[1] = p1; f.pts[2] = p2;
         f.adj[0] = a0; f.adj[1] = a1; f.adj[2] = a2;
         V3<S> ab = vp(p1) - vp(p0), ac = vp(p2) - vp(p0);
-        V3<S> n;
-        if (!try_normalize(cross(ab, ac), tol->eps, &n, (S*)nullptr)) n = zero3<S>();
-        f.normal = cvt<N>(n);
+        // The cross product in S; its normalisation in N (the result is stored
+        // in N).  With N = S this is ccw_face_normal exactly.
+        V3<N> n;
+        if (!try_normalize(cvt<N>(cross(ab, ac)), N(tol->eps), &n, (N*)nullptr)) n = zero3<N>();
+        f.normal = n;
         f.bcoords[0] = b[0]; f.bcoords[1] = b[1]; f.bcoords[2] = b[2];
         f.deleted = false;
         return f;
@@ -932,7 +978,7 @@ template <class N, class S> struct EPA {
         }
         int niter = 0;
         S max_dist = std::numeric_limits<S>::max();
-        FaceId<S> best_face_id = heap.data[0];
+        FaceId<S> best_face_id = heap_top(heap);
 
         FaceId<S> face_id;
         while (heap.pop(&face_id)) {
