@@ -4,6 +4,9 @@ Workload: 1,048,576 mixed convex pairs (Ball, Cuboid, Capsule, Cone and
 ConvexHull with 8..1024 points, seeded synthetic data), query::contact with
 prediction 0 in the PRECISE tolerance set, inputs resident in HBM (1.5 GB,
 larger than L2).  One step = one contact_batch over the whole batch.
+`--dispatch query` (default) routes Ball pairs as query::contact does;
+`--dispatch support_map` sends every pair through GJK/EPA; the line reports
+the other dispatch's throughput too.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -111,14 +114,14 @@ def algorithmic(batch, counters):
     return in_bytes + out_bytes, in_bytes, out_bytes, flops
 
 
-def accuracy_report(batch, gpu_out, sample):
+def accuracy_report(batch, gpu_out, sample, query):
     """Errors of the GPU contacts against the oracle built with f64 (the error
     oracle), on the first `sample` pairs; classification against the oracle's
     f32 reference path outside a 1e-6 band."""
     from oracle import oracle as O
     sub = batch.subset(np.arange(sample))
-    r64 = O.query(sub, O.CONTACT, O.F64, param=0.0)
-    r32 = O.query(sub, O.CONTACT, O.F32, param=0.0)
+    r64 = O.query(sub, query, O.F64, param=0.0)
+    r32 = O.query(sub, query, O.F32, param=0.0)
     d64 = O.query(sub, O.DISTANCE, O.F64)
     has = gpu_out["has_contact"][:sample]
     c = gpu_out["contact"][:sample].astype(np.float64)
@@ -151,10 +154,10 @@ def accuracy_report(batch, gpu_out, sample):
     }
 
 
-def cpu_baseline(batch, threads):
+def cpu_baseline(batch, threads, query):
     from oracle import oracle as O
     t0 = time.perf_counter()
-    O.query(batch, O.CONTACT, O.F32, param=0.0, threads=threads)
+    O.query(batch, query, O.F32, param=0.0, threads=threads)
     dt = time.perf_counter() - t0
     return {"value": batch.n_pairs / dt, "unit": "pairs/s", "cores": threads, "kind": "port",
             "sample": f"all {batch.n_pairs} pairs of the workload, 1 run, contact f32 reference path "
@@ -168,13 +171,14 @@ def run_reference(args, rank, world):
     from oracle import oracle as O
     batch = make_workload(0)
     threads = os.cpu_count() or 1
+    q = O.CONTACT_QUERY if args.dispatch == "query" else O.CONTACT
     sample = batch.subset(np.arange(min(batch.n_pairs, 1 << 18)))
     for _ in range(args.warmup):
-        O.query(sample, O.CONTACT, O.F32, param=0.0, threads=threads)
+        O.query(sample, q, O.F32, param=0.0, threads=threads)
     ts = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        O.query(sample, O.CONTACT, O.F32, param=0.0, threads=threads)
+        O.query(sample, q, O.F32, param=0.0, threads=threads)
         ts.append(time.perf_counter() - t0)
     total = sum(ts)
     value = sample.n_pairs * len(ts) / total
@@ -183,7 +187,8 @@ def run_reference(args, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": "mixed_convex_1M", "n_pairs": batch.n_pairs, "query": "contact",
-                       "prediction": 0.0, "seed": SEED, "step_sample_pairs": sample.n_pairs},
+                       "dispatch": args.dispatch, "prediction": 0.0, "seed": SEED,
+                       "step_sample_pairs": sample.n_pairs},
             "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
                              "sample": f"first {sample.n_pairs} pairs of the workload per step"},
             "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -198,6 +203,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tolerance", default="precise", choices=["precise", "reference"])
+    ap.add_argument("--dispatch", default="query", choices=["query", "support_map"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--accuracy-sample", type=int, default=32768)
     args = ap.parse_args()
@@ -221,7 +227,7 @@ def main():
 
     batch = make_workload(rank)
     db = Q.DeviceBatch.from_host(batch, device=f"cuda:{local}")
-    ctx = Q.Context(local, tolerance=args.tolerance)
+    ctx = Q.Context(local, tolerance=args.tolerance, dispatch=args.dispatch)
     ctx.set_profiling(True)
     stream = torch.cuda.current_stream()
 
@@ -251,6 +257,25 @@ def main():
         torch.cuda.synchronize()
         barrier()
     ms = e0.elapsed_time(e1)
+    # the other dispatch, same batch (outside the headline's timed region)
+    other = "support_map" if args.dispatch == "query" else "query"
+    ctx.set_dispatch(other)
+    for _ in range(2):
+        Q.contact_batch(ctx, db, 0.0)
+    torch.cuda.synchronize()
+    o0 = torch.cuda.Event(enable_timing=True)
+    o1 = torch.cuda.Event(enable_timing=True)
+    other_stage = {}
+    o0.record(stream)
+    n_other = max(2, args.steps // 2)
+    for _ in range(n_other):
+        Q.contact_batch(ctx, db, 0.0)
+        for k, v in ctx.stage_ms().items():
+            other_stage[k] = other_stage.get(k, 0.0) + v / n_other
+    o1.record(stream)
+    torch.cuda.synchronize()
+    other_ms = o0.elapsed_time(o1) / n_other
+    ctx.set_dispatch(args.dispatch)
     if dist is not None:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -306,7 +331,8 @@ def main():
     mean_stage = {k: v / args.steps for k, v in stage_sums.items()}
     dom = max(mean_stage, key=mean_stage.get)
     sample = batch.subset(np.arange(min(65536, batch.n_pairs)))
-    rs = O.query(sample, O.CONTACT, O.MIXED, param=0.0, eps=-1.0 if args.tolerance == "precise" else 0.0,
+    rs = O.query(sample, O.CONTACT_QUERY if args.dispatch == "query" else O.CONTACT, O.MIXED, param=0.0,
+                 eps=-1.0 if args.tolerance == "precise" else 0.0,
                  epa_tol=1e-6 if args.tolerance == "precise" else 0.0)
     bytes_pp, in_pp, out_pp, flops_pp = algorithmic(batch, rs.counters)
     units = {"classify": batch.n_pairs, "gjk_thread": stats.get("n_pairs", 0), "gjk_warp": stats.get("n_pairs", 0),
@@ -326,19 +352,23 @@ def main():
     cpu = None
     acc = None
     if not args.no_cpu_baseline:
-        cpu = cpu_baseline(batch, os.cpu_count() or 1)
+        qo = O.CONTACT_QUERY if args.dispatch == "query" else O.CONTACT
+        cpu = cpu_baseline(batch, os.cpu_count() or 1, qo)
         out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
-        acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs))
+        acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs), qo)
 
     line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "mixed_convex_1M", "n_pairs": batch.n_pairs, "query": "contact",
-                       "prediction": 0.0, "tolerance": args.tolerance, "warm_start": "none (plain)",
+                       "dispatch": args.dispatch, "prediction": 0.0, "tolerance": args.tolerance,
+                       "warm_start": "none (plain)",
                        "seed": SEED, "parallelism": f"weak x{world}" if world > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (%.2f GB resident)" % (batch.nbytes_inputs() / 1e9)},
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc,
+            "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
+                               "stage_ms": other_stage},
             "epa": {"pairs": stats["n_epa"], "tier_b_pairs": stats["n_epa_overflow"],
                     "gjk_iters_per_pair": stats["gjk_iters"] / batch.n_pairs,
                     "epa_iters_per_epa_pair": stats["epa_iters"] / max(1, stats["n_epa"])}}

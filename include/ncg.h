@@ -100,6 +100,8 @@ enum ncg_closest_points { NCG_CP_INTERSECTING = 0, NCG_CP_WITHIN_MARGIN = 1, NCG
 #define NCG_STATUS_EPA_NO_FACE   (1u << 4) /* reference panics at epa3.rs:325        */
 #define NCG_STATUS_DEGENERATE    (1u << 5) /* reference asserts (point_tetrahedron.rs:295) */
 #define NCG_STATUS_BAD_INPUT     (1u << 6) /* shape index out of range, bad hull slice */
+#define NCG_STATUS_UNSUPPORTED_FEATURE (1u << 7) /* query dispatch: ball centre on a ConvexHull's
+                                                    surface needs the hull's face topology */
 
 /* Return codes. */
 #define NCG_OK          0
@@ -113,6 +115,16 @@ enum ncg_closest_points { NCG_CP_INTERSECTING = 0, NCG_CP_WITHIN_MARGIN = 1, NCG
  * termination 100 eps).  NCG_TOL_PRECISE tightens the termination tests so
  * that results land within 1e-5 relative of the f64 reference. */
 enum ncg_tolerance { NCG_TOL_REFERENCE = 0, NCG_TOL_PRECISE = 1 };
+
+/* Pair dispatch of ncg_contact_batch.
+ * NCG_DISPATCH_SUPPORT_MAP: every pair through contact_support_map_support_map
+ *   (GJK, then EPA) — the (&dyn SupportMap, &dyn SupportMap) semantics.
+ * NCG_DISPATCH_QUERY: query::contact's routing (contact_shape_shape.rs:10-47):
+ *   Ball-Ball by contact_ball_ball, Ball against Cuboid or ConvexHull by
+ *   contact_ball_convex_polyhedron (point projection), every other pair by
+ *   contact_support_map_support_map.  `out_dir` then holds the contact normal
+ *   (zeros for no contact) for the first two routes. */
+enum ncg_dispatch { NCG_DISPATCH_SUPPORT_MAP = 0, NCG_DISPATCH_QUERY = 1 };
 
 /* Warm-start sources for the first GJK direction. */
 enum ncg_warm_start {
@@ -141,6 +153,7 @@ int ncg_ctx_create(ncg_ctx** out, int device);
 int ncg_ctx_destroy(ncg_ctx* ctx);
 int ncg_ctx_set_tolerance(ncg_ctx* ctx, int tolerance);
 int ncg_ctx_set_warm_start(ncg_ctx* ctx, int warm_start);
+int ncg_ctx_set_dispatch(ncg_ctx* ctx, int dispatch);
 int ncg_sync(ncg_ctx* ctx, void* stream);
 int ncg_get_stats(ncg_ctx* ctx, ncg_stats* out);
 

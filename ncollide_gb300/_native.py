@@ -31,7 +31,10 @@ EXPORTED = [
     "ncg_get_stats", "ncg_last_error", "ncg_abi_version", "ncg_contact_batch", "ncg_distance_batch",
     "ncg_proximity_batch", "ncg_closest_points_batch", "ncg_contact_batch_host", "ncg_distance_batch_host",
     "ncg_proximity_batch_host", "ncg_ctx_set_profiling", "ncg_get_stage_ms", "ncg_contact_batch_noalloc",
+    "ncg_ctx_set_dispatch",
 ]
+DISPATCH_SUPPORT_MAP, DISPATCH_QUERY = 0, 1
+STATUS_UNSUPPORTED_FEATURE = 1 << 7
 NOALLOC_MAX_PAIRS = 32768
 STAGES = ["classify", "gjk_thread", "gjk_warp", "epa_thread", "epa_tier_a", "epa_tier_b", "epa_tier_c"]
 
@@ -83,6 +86,7 @@ def load(build_if_missing=True):
     L.ncg_distance_batch_host.argtypes = [vp, P(NcgBatch), vp, vp]
     L.ncg_proximity_batch_host.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp]
     L.ncg_ctx_set_profiling.argtypes = [vp, i32]
+    L.ncg_ctx_set_dispatch.argtypes = [vp, i32]
     L.ncg_get_stage_ms.argtypes = [vp, vp, i32]
     L.ncg_contact_batch_noalloc.argtypes = [P(NcgBatch), f32, i32, vp, vp, vp, vp, vp]
     for name in EXPORTED:

@@ -82,6 +82,9 @@ struct Shape {
     uint32_t kind, off, n;
     float p0, p1, p2;
 };
+// Internal shape kind: ConstantOrigin (special_support_maps.rs:7-30), whose
+// support point is the origin whatever the pose (point projection).
+constexpr uint32_t KIND_CONSTANT_ORIGIN = 7;
 
 // Validates and loads a shape record; returns false on a bad index or hull slice.
 NCG_DEV bool load_shape(const ncg_batch& b, uint32_t id, Shape& s) {
@@ -181,6 +184,8 @@ template <class Scan> NCG_DEV vec3<float> local_support(const Shape& s, vec3<flo
         if (dot(d, v) < d.y * s.p0) return {0.0f, s.p0, 0.0f};
         return v;
     }
+    case KIND_CONSTANT_ORIGIN:
+        return zero3<float>();
     case NCG_CYLINDER: {
         vec3<float> v{d.x, 0.0f, d.z};
         float n = vnorm(v);
@@ -201,6 +206,7 @@ template <class Scan> NCG_DEV vec3<float> local_support(const Shape& s, vec3<flo
 // World-space support point (Ball overrides the default transform).
 template <class Scan>
 NCG_DEV vec3<float> support_point(const Pose& m, const Shape& s, vec3<float> d, const Scan& scan) {
+    if (s.kind == KIND_CONSTANT_ORIGIN) return zero3<float>();
     if (s.kind == NCG_BALL) {
         vec3<float> u = d / vnorm(d);
         return m.t + u * s.p0;

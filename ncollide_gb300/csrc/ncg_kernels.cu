@@ -6,11 +6,11 @@
 //   2. gjk_thread   1 thread/pair over the analytic list (persistent grid).
 //   3. gjk_warp     1 warp/pair over the hull list (dynamic queue); the hull
 //                   arg-max is warp-parallel with coalesced 128-bit loads.
-//   4. epa_thread   contact only, intersecting pairs of analytic shapes: one
-//                   thread per pair, polytope of up to 48 vertices in the
-//                   thread's local memory.
-//   5. epa tier A   ConvexHull pairs and pairs that outgrew epa_thread: one warp
-//                   per pair, up to 128 vertices in shared memory.
+//   4. epa_thread   contact only, intersecting pairs: one thread per pair,
+//                   polytope of up to 96 vertices in the thread's local memory.
+//   5. epa tier A   pairs that outgrew epa_thread (and the EPA of hull pairs
+//                   when their GJK ran one warp per pair): one warp per pair,
+//                   up to 128 vertices in shared memory.
 //   6. epa tier B   pairs that outgrew tier A: up to 1280 vertices in shared
 //                   memory (1 warp per SM).
 //   7. epa tier C   pairs that outgrew tier B: a global-memory slab per warp
@@ -31,6 +31,7 @@
 #include "../../include/ncg.h"
 #include "ncg_core.cuh"
 #include "ncg_epa.cuh"
+#include "ncg_query.cuh"
 
 using namespace ncg;
 
@@ -52,6 +53,7 @@ struct Outputs {
 
 struct QueryParams {
     int query;
+    int dispatch;  // ncg_dispatch (contact only)
     int use_init_dir;
     int gjk_max_iter;
     int epa_max_iter;
@@ -60,11 +62,14 @@ struct QueryParams {
 };
 
 // EPA work item: the pair and GJK's final simplex (dim + 1 CSO points).
+// `mode` 0: contact_support_map_support_map; 1: point projection of a ball's
+// centre on a ConvexHull (query::contact dispatch), `flip` when the ball is
+// the second shape.
 struct __align__(16) EpaItem {
     uint32_t pair;
     uint32_t gjk_iters;
     uint32_t status;
-    int32_t dim;
+    uint8_t dim, mode, flip, pad;
     float v[4][9];
 };
 
@@ -92,7 +97,7 @@ struct Scratch {
 // vertices), silhouette edges, flood-fill stack.  Stage 0 is the per-thread
 // store, 1-3 the warp tiers A, B, C.
 template <int T> struct EpaTier;
-template <> struct EpaTier<0> { static constexpr int VC = 48, FC = 2 * 48 + 16, SC = 32, TC = 96; };
+template <> struct EpaTier<0> { static constexpr int VC = 96, FC = 2 * 96 + 16, SC = 48, TC = 160; };
 template <> struct EpaTier<1> { static constexpr int VC = 128, FC = 2 * 128 + 64, SC = 64, TC = 256; };
 template <> struct EpaTier<2> { static constexpr int VC = 1280, FC = 2 * 1280 + 64, SC = 512, TC = 2048; };
 template <> struct EpaTier<3> { static constexpr int VC = 10240, FC = 2 * 10240 + 64, SC = 4096, TC = 16384; };
@@ -162,6 +167,24 @@ NCG_DEV void write_outputs(const QueryParams& qp, const Outputs& o, uint32_t i, 
     if (o.iters) o.iters[i] = iters;
 }
 
+// Writes a contact of the query::contact routes (explicit depth; the normal as
+// the returned direction, zeros when there is no contact).
+NCG_DEV void write_qcontact(const Outputs& o, uint32_t i, const QContact& q, uint32_t status, uint32_t iters) {
+    ncg_contact c;
+    memset(&c, 0, sizeof(c));
+    if (q.tag) {
+        wr3(c.world1, q.p1);
+        wr3(c.world2, q.p2);
+        wr3(c.normal, q.n);
+        c.depth = q.depth.h;
+    }
+    o.contact[i] = c;
+    o.tag[i] = (uint8_t)q.tag;
+    if (o.dir) wr3(o.dir + 3 * (size_t)i, q.n);
+    o.status[i] = status | q.status;
+    if (o.iters) o.iters[i] = iters;
+}
+
 // A pair with an invalid shape index or hull slice: no contact, distance 0,
 // Disjoint, and NCG_STATUS_BAD_INPUT (the reference would index out of bounds).
 NCG_DEV void write_bad(const QueryParams& qp, const Outputs& o, uint32_t i) {
@@ -203,6 +226,70 @@ NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& 
     load_shape(b, b.g2[i], g.g2);
     g.m1 = load_pose(b.m1 + i);
     g.m2 = load_pose(b.m2 + i);
+    if (qp.query == Q_CONTACT && qp.dispatch == NCG_DISPATCH_QUERY) {
+        const bool b1 = g.g1.kind == NCG_BALL, b2 = g.g2.kind == NCG_BALL;
+        const bool p1 = g.g1.kind == NCG_CUBOID || g.g1.kind == NCG_CONVEX_HULL;
+        const bool p2 = g.g2.kind == NCG_CUBOID || g.g2.kind == NCG_CONVEX_HULL;
+        const real pred = from_host(qp.param);
+        if (b1 && b2) {
+            QContact q = contact_ball_ball(g.m1.t, g.g1.p0, g.m2.t, g.g2.p0, pred);
+            if (writer) write_qcontact(o, i, q, 0, 0);
+            return;
+        }
+        if ((b1 && p2) || (p1 && b2)) {
+            const bool flip = !b1;
+            const Pose& pb = flip ? g.m2 : g.m1;
+            const Shape& sb = flip ? g.g2 : g.g1;
+            const Pose& pp = flip ? g.m1 : g.m2;
+            const Shape& sp = flip ? g.g1 : g.g2;
+            if (sp.kind == NCG_CUBOID) {
+                bool inside;
+                vec3<float> pr;
+                int fk, fi;
+                aabb_project_with_feature(pp, mk(sp.p0, sp.p1, sp.p2), pb.t, inside, pr, fk, fi);
+                QContact q = ball_polyhedron_assemble(pb.t, sb.p0, inside, to_r(pr), fk, fi, true, pred, flip);
+                if (writer) write_qcontact(o, i, q, 0, 0);
+                return;
+            }
+            // point_projection_on_support_map: GJK on the translated hull
+            PairGeom pg = projection_geom(pp, sp, pb.t);
+            vec3<float> dir;
+            float dn;
+            if (!try_normalize(-pg.m1.t, FLT_EPSILON, dir, dn)) dir = mk(1.0f, 0.0f, 0.0f);
+            Simplex ps;
+            ps.reset(cso_support(pg, dir, scan));
+            uint32_t it = 0, st = 0;
+            GjkOut r = gjk(pg, dw_max(), true, ps, qp.tol, scan, it, st, qp.gjk_max_iter);
+            iter_acc += it;
+            if (r.kind == GJK_INTERSECTION) {
+                if (writer) {
+                    unsigned long long slot = atomicAdd(&s.ctr->n_items, 1ull);
+                    unsigned long long pos = atomicAdd(&s.ctr->epa_count[epa_queue], 1ull);
+                    s.queue[epa_queue][pos] = (uint32_t)slot;
+                    EpaItem& e = s.items[slot];
+                    e.pair = i;
+                    e.gjk_iters = it;
+                    e.status = st;
+                    e.dim = (uint8_t)ps.dim;
+                    e.mode = 1;
+                    e.flip = flip ? 1 : 0;
+                    for (int k = 0; k <= ps.dim; ++k) {
+                        const CSO& c = ps.v[k];
+                        float* w = e.v[k];
+                        w[0] = c.p.x; w[1] = c.p.y; w[2] = c.p.z;
+                        w[3] = c.o1.x; w[4] = c.o1.y; w[5] = c.o1.z;
+                        w[6] = c.o2.x; w[7] = c.o2.y; w[8] = c.o2.z;
+                    }
+                }
+                return;
+            }
+            bool inside = r.kind != GJK_CLOSEST_POINTS;  // the iteration cap: unreachable!() in gjk.rs:57
+            vec3<real> w2 = inside ? to_r(pb.t) : r.p1 + to_r(pb.t);
+            QContact q = ball_polyhedron_assemble(pb.t, sb.p0, inside, w2, F_UNKNOWN, 0, false, pred, flip);
+            if (writer) write_qcontact(o, i, q, st, pack_iters(it, 0));
+            return;
+        }
+    }
     vec3<float> d = initial_dir(qp, b, i, g);
     Simplex sx;
     sx.reset(cso_support(g, d, scan));
@@ -220,7 +307,9 @@ NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& 
             it.pair = i;
             it.gjk_iters = iters;
             it.status = status;
-            it.dim = sx.dim;
+            it.dim = (uint8_t)sx.dim;
+            it.mode = 0;
+            it.flip = 0;
             for (int k = 0; k <= sx.dim; ++k) {
                 const CSO& c = sx.v[k];
                 float* w = it.v[k];
@@ -264,8 +353,12 @@ NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
     if ((threadIdx.x & 31u) == 0 && v) atomicAdd(dst, v);
 }
 
-__global__ void __launch_bounds__(128) k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
-    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->n_analytic;
+// One thread per pair over a pair list (list 0: analytic pairs, list 1:
+// ConvexHull pairs, whose points the thread scans itself); EPA starts in the
+// thread stage.
+__global__ void __launch_bounds__(128) k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list) {
+    const unsigned long long n = *(volatile unsigned long long*)(list == 0 ? &s.ctr->n_analytic : &s.ctr->n_hull);
+    const uint32_t* ids = list == 0 ? s.analytic : s.hull;
     ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     unsigned long long acc = 0;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
@@ -273,7 +366,7 @@ __global__ void __launch_bounds__(128) k_gjk_thread(ncg_batch b, QueryParams qp,
     const unsigned long long rounds = (n + stride - 1) / stride;
     for (unsigned long long r = 0; r < rounds; ++r) {
         unsigned long long k = start + r * stride;
-        if (k < n) gjk_pair(b, qp, o, s, s.analytic[k], scan, true, acc, 0);
+        if (k < n) gjk_pair(b, qp, o, s, ids[k], scan, true, acc, 0);
     }
     warp_add(&s.ctr->gjk_iters, acc);
 }
@@ -326,6 +419,34 @@ NCG_DEV PairGeom load_geom(const ncg_batch& b, uint32_t i) {
     return g;
 }
 
+// The geometry an EPA work item runs on (mode 1: the translated hull against
+// ConstantOrigin).
+NCG_DEV PairGeom item_geom(const ncg_batch& b, const EpaItem& it) {
+    PairGeom g = load_geom(b, it.pair);
+    if (it.mode == 0) return g;
+    const Pose& pb = it.flip ? g.m2 : g.m1;
+    const Pose& pp = it.flip ? g.m1 : g.m2;
+    const Shape& sp = it.flip ? g.g1 : g.g2;
+    return projection_geom(pp, sp, pb.t);
+}
+
+// Finishes an EPA work item: a contact (mode 0) or the ball-hull contact from
+// the EPA projection of the ball's centre (mode 1).
+NCG_DEV void finish_epa(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const EpaItem& it,
+                        const EpaResult& r, uint32_t extra_status) {
+    if (it.mode == 0) {
+        write_epa(o, it, r, extra_status);
+        return;
+    }
+    PairGeom g = load_geom(b, it.pair);
+    const Pose& pb = it.flip ? g.m2 : g.m1;
+    const Shape& sb = it.flip ? g.g2 : g.g1;
+    const bool ok = r.exit >= EPA_OK_DIM0 && r.exit <= EPA_OK_HEAP_EMPTY;
+    vec3<real> w2 = ok ? r.p1 + to_r(pb.t) : to_r(pb.t);
+    QContact q = ball_polyhedron_assemble(pb.t, sb.p0, true, w2, F_UNKNOWN, 0, false, from_host(qp.param), it.flip != 0);
+    write_qcontact(o, it.pair, q, it.status | r.status | extra_status, pack_iters(it.gjk_iters, r.iters));
+}
+
 NCG_DEV void load_simplex(const EpaItem& it, CSO* sv) {
     for (int k = 0; k <= it.dim; ++k) {
         const float* w = it.v[k];
@@ -362,7 +483,7 @@ __global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs
         if (k >= n) break;
         const uint32_t item = s.queue[T][k];
         const EpaItem& it = s.items[item];
-        PairGeom g = load_geom(b, it.pair);
+        PairGeom g = item_geom(b, it);
         CSO sv[4];
         load_simplex(it, sv);
         EpaResult r = epa_run<WarpExec>(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
@@ -377,9 +498,9 @@ __global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs
                 if (r.exit == EPA_OVERFLOW) {
                     EpaResult none = r;
                     none.exit = EPA_NONE;
-                    write_epa(o, it, none, NCG_STATUS_EPA_CAPACITY);
+                    finish_epa(b, qp, o, it, none, NCG_STATUS_EPA_CAPACITY);
                 } else {
-                    write_epa(o, it, r, 0);
+                    finish_epa(b, qp, o, it, r, 0);
                 }
             }
         }
@@ -404,7 +525,7 @@ __global__ void __launch_bounds__(128) k_epa_thread(ncg_batch b, QueryParams qp,
     for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         const uint32_t item = s.queue[0][k];
         const EpaItem& it = s.items[item];
-        PairGeom g = load_geom(b, it.pair);
+        PairGeom g = item_geom(b, it);
         CSO sv[4];
         load_simplex(it, sv);
         EpaResult r = epa_run<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
@@ -413,7 +534,7 @@ __global__ void __launch_bounds__(128) k_epa_thread(ncg_batch b, QueryParams qp,
             s.queue[1][q] = item;
         } else {
             acc += r.iters;
-            write_epa(o, it, r, 0);
+            finish_epa(b, qp, o, it, r, 0);
         }
     }
     warp_add(&s.ctr->epa_iters, acc);
@@ -462,6 +583,8 @@ struct ncg_ctx {
     int num_sms = 0;
     int tol_mode = NCG_TOL_REFERENCE;
     int warm = NCG_WARM_NONE;
+    int dispatch = NCG_DISPATCH_SUPPORT_MAP;
+    int hull_gjk_warp = 0;  // GJK of ConvexHull pairs: 0 one thread per pair, 1 one warp per pair
     int occ_thread = 1, occ_warp = 1, occ_epa0 = 1, occ_epa1 = 1, occ_ethread = 1;
     char* scratch = nullptr;
     size_t scratch_cap_pairs = 0;
@@ -522,6 +645,7 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     Scratch s = carve_scratch(c);
     QueryParams qp;
     qp.query = query;
+    qp.dispatch = c->dispatch;
     qp.use_init_dir = (c->warm == NCG_WARM_INIT_DIR && b->init_dir) ? 1 : 0;
     qp.gjk_max_iter = 10000;
     qp.epa_max_iter = 10000;
@@ -540,9 +664,10 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     mark(-1);
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
     mark(0);
-    k_gjk_thread<<<c->num_sms * c->occ_thread, 128, 0, st>>>(bb, qp, o, s);
+    k_gjk_thread<<<c->num_sms * c->occ_thread, 128, 0, st>>>(bb, qp, o, s, 0);
     mark(1);
-    k_gjk_warp<<<c->num_sms * c->occ_warp, 128, 0, st>>>(bb, qp, o, s);
+    if (c->hull_gjk_warp) k_gjk_warp<<<c->num_sms * c->occ_warp, 128, 0, st>>>(bb, qp, o, s);
+    else k_gjk_thread<<<c->num_sms * c->occ_thread, 128, 0, st>>>(bb, qp, o, s, 1);
     mark(2);
     launches += 3;
     if (query == Q_CONTACT) {
@@ -622,6 +747,12 @@ int ncg_ctx_destroy(ncg_ctx* c) {
 int ncg_ctx_set_tolerance(ncg_ctx* c, int tol) {
     if (!c || (tol != NCG_TOL_REFERENCE && tol != NCG_TOL_PRECISE)) return NCG_EINVAL;
     c->tol_mode = tol;
+    return NCG_OK;
+}
+
+int ncg_ctx_set_dispatch(ncg_ctx* c, int dispatch) {
+    if (!c || (dispatch != NCG_DISPATCH_SUPPORT_MAP && dispatch != NCG_DISPATCH_QUERY)) return NCG_EINVAL;
+    c->dispatch = dispatch;
     return NCG_OK;
 }
 
@@ -925,6 +1056,7 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
 
     QueryParams qp;
     qp.query = Q_CONTACT;
+    qp.dispatch = NCG_DISPATCH_SUPPORT_MAP;
     qp.use_init_dir = b->init_dir ? 1 : 0;
     qp.gjk_max_iter = 10000;
     qp.epa_max_iter = 10000;
@@ -937,8 +1069,8 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset noalloc counters")) return NCG_ECUDA;
     unsigned n = (unsigned)b->n_pairs;
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
-    k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s);
-    k_gjk_warp<<<d.num_sms * d.occ_warp, 128, 0, st>>>(bb, qp, o, s);
+    k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s, 0);
+    k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s, 1);
     k_epa_thread<<<d.num_sms * d.occ_ethread, 128, 0, st>>>(bb, qp, o, s);
     k_epa<<<d.num_sms * d.occ_epa0, 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>());
     k_epa<<<d.num_sms * d.occ_epa1, 32, tier_bytes<2>(), st>>>(bb, qp, o, s, caps<2>());

@@ -30,7 +30,7 @@ from .shapes import CONTACT_DTYPE, PairBatch
 class Context:
     """Owns an ncg_ctx: scratch memory, EPA slabs and settings for one device."""
 
-    def __init__(self, device=0, tolerance=N.TOL_REFERENCE, warm_start=N.WARM_NONE):
+    def __init__(self, device=0, tolerance=N.TOL_REFERENCE, warm_start=N.WARM_NONE, dispatch=N.DISPATCH_SUPPORT_MAP):
         self._L = N.load()
         self._p = ctypes.c_void_p()
         if isinstance(device, torch.device):
@@ -39,6 +39,7 @@ class Context:
         N.check(self._L.ncg_ctx_create(ctypes.byref(self._p), self.device), "ncg_ctx_create")
         self.set_tolerance(tolerance)
         self.set_warm_start(warm_start)
+        self.set_dispatch(dispatch)
 
     @property
     def handle(self):
@@ -49,6 +50,14 @@ class Context:
             mode = {"reference": N.TOL_REFERENCE, "precise": N.TOL_PRECISE}[mode]
         N.check(self._L.ncg_ctx_set_tolerance(self._p, int(mode)), "ncg_ctx_set_tolerance")
         self.tolerance = int(mode)
+
+    def set_dispatch(self, mode):
+        """NCG_DISPATCH_SUPPORT_MAP (every pair by GJK/EPA) or NCG_DISPATCH_QUERY
+        (query::contact's routing of Ball pairs)."""
+        if isinstance(mode, str):
+            mode = {"support_map": N.DISPATCH_SUPPORT_MAP, "query": N.DISPATCH_QUERY}[mode]
+        N.check(self._L.ncg_ctx_set_dispatch(self._p, int(mode)), "ncg_ctx_set_dispatch")
+        self.dispatch = int(mode)
 
     def set_warm_start(self, mode):
         N.check(self._L.ncg_ctx_set_warm_start(self._p, int(mode)), "ncg_ctx_set_warm_start")

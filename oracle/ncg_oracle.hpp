@@ -89,7 +89,7 @@ template <class T> inline V3<T> transform_point(const Iso<T>& m, V3<T> p) { retu
 template <class T> inline V3<T> inverse_transform_vector(const Iso<T>& m, V3<T> v) { return inv_rotate(m.q, v); }
 
 // ---------------------------------------------------------------- shapes
-enum Kind { BALL = 0, CUBOID = 1, CAPSULE = 2, CONE = 3, CYLINDER = 4, CONVEX_HULL = 5 };
+enum Kind { BALL = 0, CUBOID = 1, CAPSULE = 2, CONE = 3, CYLINDER = 4, CONVEX_HULL = 5, CONSTANT_ORIGIN = 7 };
 
 template <class N> struct Shape {
     int kind;
@@ -134,6 +134,7 @@ enum StatusBits : uint32_t {
     ST_EPA_NO_FACE = 1u << 4,
     ST_DEGENERATE = 1u << 5,
     ST_BAD_INPUT = 1u << 6,
+    ST_UNSUPPORTED_FEATURE = 1u << 7,
 };
 
 // src/utils/point_cloud_support_point.rs:6-33 — first maximum wins.
@@ -187,6 +188,8 @@ template <class N> inline V3<N> local_support_point(const Shape<N>& s, V3<N> dir
         v.y = std::copysign(s.p0, dir.y);
         return v;
     }
+    case CONSTANT_ORIGIN:
+        return zero3<N>();
     case CONVEX_HULL:
     default:
         return s.point(point_cloud_support_point_id(dir, s, c));
@@ -196,6 +199,7 @@ template <class N> inline V3<N> local_support_point(const Shape<N>& s, V3<N> dir
 // SupportMap::support_point (support_map.rs:25-28); Ball overrides it (ball.rs:31-39).
 template <class N> inline V3<N> support_point(const Iso<N>& m, const Shape<N>& s, V3<N> dir, Counters* c) {
     if (c) c->support_calls++;
+    if (s.kind == CONSTANT_ORIGIN) return zero3<N>();  // special_support_maps.rs:9-30
     if (s.kind == BALL) {
         V3<N> d = dir / norm(dir);
         return m.t + d * s.p0;
@@ -1173,6 +1177,202 @@ QueryOut<S> closest_points(const Iso<N>& m1, const Shape<N>& g1, const Iso<N>& m
     else if (r.kind == GJK_NO_INTERSECTION) { o.tag = 2; }
     else { o.tag = 0; }
     return o;
+}
+
+}  // namespace ncgo
+
+namespace ncgo {
+
+// ---------------------------------------------------- query::contact dispatch
+// contact_shape_shape.rs:10-47 for the shapes of this library: Ball-Ball is
+// analytic, Ball against a ConvexPolyhedron with PointQuery (Cuboid,
+// ConvexHull) goes through point projection, every other pair (Capsule, Cone,
+// Cylinder included) through contact_support_map_support_map.
+
+// contact_ball_ball.rs:8-38 (Contact::new with the explicit depth).
+template <class N, class S>
+QueryOut<S> contact_ball_ball(V3<N> c1, N r1, V3<N> c2, N r2, S prediction) {
+    QueryOut<S> o{};
+    V3<S> a = cvt<S>(c1), b = cvt<S>(c2);
+    V3<S> delta = b - a;
+    S d2 = norm_sq(delta);
+    S sum = S(r1) + S(r2);
+    S se = sum + prediction;
+    o.gjk_kind = -1;
+    if (d2 < se * se) {
+        using std::sqrt;
+        V3<S> n = d2 != S(0) ? delta / norm(delta) : v3<S>(S(1), S(0), S(0));
+        o.tag = 1;
+        o.p1 = a + n * S(r1);
+        o.p2 = b + n * (-S(r2));
+        o.dir = n;
+        o.value = sum - sqrt(d2);
+    } else {
+        o.tag = 0;
+        o.dir = zero3<S>();
+    }
+    return o;
+}
+
+// Cuboid features (FeatureId): faces 0..5, edges, vertices.
+enum FeatKind { F_UNKNOWN = 0, F_FACE = 1, F_EDGE = 2, F_VERTEX = 3 };
+
+// point_aabb.rs:9-135 for the cuboid [-h, h] (solid = false), in N.
+template <class N>
+void aabb_project_with_feature(const Iso<N>& m, V3<N> h, V3<N> pt, bool* inside, V3<N>* proj, int* fkind,
+                               int* fid) {
+    V3<N> mins = zero3<N>() - h, maxs = zero3<N>() + h;
+    V3<N> ls = inv_rotate(m.q, pt - m.t);  // Isometry::inverse_transform_point
+    V3<N> mins_pt = mins - ls, pt_maxs = ls - maxs;
+    auto sup0 = [](N x) { return x > N(0) ? x : N(0); };  // Vector::sup with zero
+    N mp[3] = {mins_pt.x, mins_pt.y, mins_pt.z}, pm[3] = {pt_maxs.x, pt_maxs.y, pt_maxs.z};
+    N shift[3] = {sup0(mp[0]) - sup0(pm[0]), sup0(mp[1]) - sup0(pm[1]), sup0(mp[2]) - sup0(pm[2])};
+    bool in = shift[0] == N(0) && shift[1] == N(0) && shift[2] == N(0);
+    if (in) {
+        N best = -std::numeric_limits<N>::max();
+        bool is_mins = false;
+        int best_id = 0;
+        for (int i = 0; i < 3; ++i) {
+            if (mp[i] < pm[i]) {
+                if (pm[i] > best) { best_id = i; is_mins = false; best = pm[i]; }
+            } else if (mp[i] > best) {
+                best_id = i; is_mins = true; best = mp[i];
+            }
+        }
+        shift[0] = shift[1] = shift[2] = N(0);
+        shift[best_id] = is_mins ? best : -best;
+    }
+    V3<N> lp{ls.x + shift[0], ls.y + shift[1], ls.z + shift[2]};
+    *inside = in;
+    *proj = transform_point(m, lp);
+    N l[3] = {lp.x, lp.y, lp.z}, mx[3] = {maxs.x, maxs.y, maxs.z}, mn[3] = {mins.x, mins.y, mins.z};
+    int nzero = 0, last_zero = 0, last_nonzero = 0;
+    for (int i = 0; i < 3; ++i) {
+        if (shift[i] == N(0)) { nzero++; last_zero = i; }
+        else last_nonzero = i;
+    }
+    N eps = std::numeric_limits<N>::epsilon();
+    N center[3] = {(mn[0] + mx[0]) * N(0.5), (mn[1] + mx[1]) * N(0.5), (mn[2] + mx[2]) * N(0.5)};
+    if (nzero == 3) {
+        for (int i = 0; i < 3; ++i) {
+            if (l[i] > mx[i] - eps) { *fkind = F_FACE; *fid = i; return; }
+            if (l[i] <= mn[i] + eps) { *fkind = F_FACE; *fid = i + 3; return; }
+        }
+        *fkind = F_UNKNOWN; *fid = 0;
+    } else if (nzero == 2) {
+        *fkind = F_FACE;
+        *fid = l[last_nonzero] < center[last_nonzero] ? last_nonzero + 3 : last_nonzero;
+    } else {
+        int id = 0;
+        for (int i = 0; i < 3; ++i)
+            if (l[i] < center[i]) id |= 1 << i;
+        if (nzero == 0) { *fkind = F_VERTEX; *fid = id; }
+        else { *fkind = F_EDGE; *fid = (id << 2) | last_zero; }
+    }
+}
+
+// cuboid.rs feature_normal (3-D), in the cuboid's local frame.
+template <class N> V3<N> cuboid_feature_normal(int kind, int id) {
+    N c[3] = {N(0), N(0), N(0)};
+    if (kind == F_FACE) {
+        if (id < 3) c[id] = N(1);
+        else c[id - 3] = N(-1);
+        return {c[0], c[1], c[2]};
+    }
+    if (kind == F_EDGE) {
+        int edge = id & 3, f1 = (edge + 1) % 3, f2 = (edge + 2) % 3, signs = id >> 2;
+        c[f1] = (signs & (1 << f1)) ? N(-1) : N(1);
+        c[f2] = (signs & (1 << f2)) ? N(-1) : N(1);
+    } else {
+        for (int i = 0; i < 3; ++i) c[i] = (id & (1 << i)) ? N(-1) : N(1);
+    }
+    V3<N> v{c[0], c[1], c[2]};
+    return v / norm(v);
+}
+
+// point_support_map.rs:15-53 (solid = false): GJK projection of the origin on
+// the shape translated by -point, EPA when the point is inside.
+template <class N, class S>
+bool point_projection_on_support_map(const Iso<N>& m2, const Shape<N>& g, V3<N> point, const Tol<S>& tol,
+                                     Counters* cnt, V3<S>* proj) {
+    Iso<N> m{m2.q, (zero3<N>() - point) + m2.t};
+    Iso<N> id{Quat<N>{N(0), N(0), N(0), N(1)}, zero3<N>()};
+    Shape<N> origin{};
+    origin.kind = CONSTANT_ORIGIN;
+    V3<N> dir;
+    if (!try_normalize(-m.t, std::numeric_limits<N>::epsilon(), &dir, (N*)nullptr)) dir = v3<N>(N(1), N(0), N(0));
+    VoronoiSimplex<N, S> simplex;
+    simplex.reset(cso_from_shapes(m, g, id, origin, dir, cnt));
+    GJKResult<S> r = gjk_closest_points(m, g, id, origin, std::numeric_limits<S>::max(), true, simplex, tol, cnt);
+    if (r.kind == GJK_CLOSEST_POINTS) {
+        *proj = r.p1 + cvt<S>(point);
+        return false;
+    }
+    if (r.kind != GJK_INTERSECTION && cnt) cnt->status |= ST_GJK_MAX_ITER;  // unreachable!() in gjk.rs:57
+    EPA<N, S> epa;
+    V3<S> p1, p2, n;
+    if (r.kind == GJK_INTERSECTION && epa.closest_points(m, g, id, origin, simplex, tol, &p1, &p2, &n, cnt)) {
+        *proj = p1 + cvt<S>(point);
+        return true;
+    }
+    *proj = cvt<S>(point);
+    return true;
+}
+
+// contact_ball_convex_polyhedron.rs:11-58 (and the flip of :65-77).
+template <class N, class S>
+QueryOut<S> contact_ball_polyhedron(V3<N> c, N r, const Iso<N>& m2, const Shape<N>& g2, S prediction,
+                                    const Tol<S>& tol, Counters* cnt, bool flip) {
+    QueryOut<S> o{};
+    o.gjk_kind = -1;
+    bool inside;
+    V3<S> world2;
+    int fkind = F_UNKNOWN, fid = 0;
+    if (g2.kind == CUBOID) {
+        V3<N> pr;
+        aabb_project_with_feature(m2, v3<N>(g2.p0, g2.p1, g2.p2), c, &inside, &pr, &fkind, &fid);
+        world2 = cvt<S>(pr);
+    } else {
+        inside = point_projection_on_support_map(m2, g2, c, tol, cnt, &world2);
+    }
+    V3<S> cs = cvt<S>(c);
+    V3<S> dpt = world2 - cs;
+    V3<S> dir, normal;
+    S dist, depth;
+    if (try_normalize(dpt, S(std::numeric_limits<N>::epsilon()), &dir, &dist)) {
+        if (inside) { depth = dist + S(r); normal = -dir; }
+        else { depth = -dist + S(r); normal = dir; }
+    } else {
+        // ConvexHull::project_point_with_feature needs the hull's face topology,
+        // which this library does not build: the ball centre on the hull's
+        // surface is reported as unsupported.
+        if (g2.kind != CUBOID) { if (cnt) cnt->status |= ST_UNSUPPORTED_FEATURE; fkind = F_UNKNOWN; }
+        if (fkind == F_UNKNOWN) { o.tag = 0; o.dir = zero3<S>(); return o; }
+        depth = S(r);
+        normal = -cvt<S>(cuboid_feature_normal<N>(fkind, fid));  // local normal, as the reference does
+    }
+    if (depth >= -prediction) {
+        V3<S> world1 = cs + normal * S(r);
+        o.tag = 1;
+        o.value = depth;
+        if (flip) { o.p1 = world2; o.p2 = world1; o.dir = -normal; }
+        else { o.p1 = world1; o.p2 = world2; o.dir = normal; }
+        return o;
+    }
+    o.tag = 0;
+    o.dir = zero3<S>();
+    return o;
+}
+
+template <class N, class S>
+QueryOut<S> contact_query(const Iso<N>& m1, const Shape<N>& g1, const Iso<N>& m2, const Shape<N>& g2, S prediction,
+                          const V3<N>* init_dir, const Tol<S>& tol, Counters* cnt) {
+    bool b1 = g1.kind == BALL, b2 = g2.kind == BALL;
+    bool p1 = g1.kind == CUBOID || g1.kind == CONVEX_HULL, p2 = g2.kind == CUBOID || g2.kind == CONVEX_HULL;
+    if (b1 && b2) return contact_ball_ball<N, S>(m1.t, g1.p0, m2.t, g2.p0, prediction);
+    if (b1 && p2) return contact_ball_polyhedron<N, S>(m1.t, g1.p0, m2, g2, prediction, tol, cnt, false);
+    if (p1 && b2) return contact_ball_polyhedron<N, S>(m2.t, g2.p0, m1, g1, prediction, tol, cnt, true);
+    return contact<N, S>(m1, g1, m2, g2, prediction, init_dir, tol, cnt);
 }
 
 }  // namespace ncgo

@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libncg_oracle.so")
 
 F32, F64, MIXED = 0, 1, 2
-CONTACT, DISTANCE, PROXIMITY, CLOSEST = 0, 1, 2, 3
+CONTACT, DISTANCE, PROXIMITY, CLOSEST, CONTACT_QUERY = 0, 1, 2, 3, 4
 GJK_INTERSECTION, GJK_CLOSEST_POINTS, GJK_PROXIMITY, GJK_NO_INTERSECTION = 0, 1, 2, 3
 
 _lib = None

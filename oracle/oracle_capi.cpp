@@ -14,7 +14,7 @@ using namespace ncgo;
 namespace {
 
 enum Policy { POLICY_F32 = 0, POLICY_F64 = 1, POLICY_MIXED = 2 };
-enum Query { Q_CONTACT = 0, Q_DISTANCE = 1, Q_PROXIMITY = 2, Q_CLOSEST = 3 };
+enum Query { Q_CONTACT = 0, Q_DISTANCE = 1, Q_PROXIMITY = 2, Q_CLOSEST = 3, Q_CONTACT_QUERY = 4 };
 
 // Inputs either in the library's f32 layout or as f64 arrays (known-answer tests
 // use decimal literals that f32 cannot hold; the f64 oracle must see them exactly).
@@ -124,6 +124,7 @@ void run_range(const In& in, int query, S param, const Tol<S>& tol, uint64_t lo,
             case Q_CONTACT: r = contact<N, S>(m1, s1, m2, s2, param, dp, tol, &cnt); break;
             case Q_DISTANCE: r = distance<N, S>(m1, s1, m2, s2, dp, tol, &cnt); break;
             case Q_PROXIMITY: r = proximity<N, S>(m1, s1, m2, s2, param, dp, tol, &cnt); break;
+            case Q_CONTACT_QUERY: r = contact_query<N, S>(m1, s1, m2, s2, param, dp, tol, &cnt); break;
             default: r = closest_points<N, S>(m1, s1, m2, s2, param, dp, tol, &cnt); break;
             }
         }
@@ -193,7 +194,8 @@ int dispatch(int policy, const In& in, uint64_t n, int query, double param, doub
 extern "C" {
 
 // policy: 0 = reference f32, 1 = reference f64, 2 = f32 supports + double-word sub-solve.
-// query:  0 = contact, 1 = distance, 2 = proximity, 3 = closest_points.
+// query:  0 = contact (support-map pairs), 1 = distance, 2 = proximity,
+//         3 = closest_points, 4 = contact with query::contact's dispatch.
 // eps == 0 selects the machine epsilon of the policy's N (the reference's
 // default_epsilon); eps > 0 replaces it in every tolerance; eps < 0 selects
 // the PRECISE set (f32 zero tests, f64 relative GJK convergence).

@@ -58,6 +58,27 @@ def test_proximity_example():
         assert list(r.tag) == [cs["proximity"] for cs in k["cases"]]
 
 
+def test_contact_example_query_dispatch():
+    k = GOLD["contact_example"]
+    ball, cub = (0, (k["ball_radius"],), None), (1, tuple(k["cuboid_half_extents"]), None)
+    pairs = [(O.pose8(cs["ball_translation"]), ball, O.pose8(), cub) for cs in k["cases"]]
+    for pol in (O.F64, O.F32, O.MIXED):
+        r = O.query_f64(pairs, O.CONTACT_QUERY, pol, param=k["prediction"])
+        assert r.tag[0] == 1 and r.value[0] > 0
+        assert r.tag[1] == 1 and r.value[1] < 0
+        assert r.tag[2] == 0
+
+
+def test_query_dispatch_ball_ball_is_analytic():
+    # contact_ball_ball.rs: depth = r1 + r2 - |c2 - c1|, normal along c2 - c1
+    ball = (0, (1.0,), None)
+    r = O.query_f64([(O.pose8((0, 0, 0)), ball, O.pose8((1.5, 0, 0)), ball)], O.CONTACT_QUERY, O.F64, param=0.0)
+    assert r.tag[0] == 1 and r.value[0] == 0.5
+    assert list(r.dir[0]) == [1.0, 0.0, 0.0]
+    assert list(r.p1[0]) == [1.0, 0.0, 0.0] and list(r.p2[0]) == [0.5, 0.0, 0.0]
+    assert r.counters[0, 1] == 0  # no EPA
+
+
 def test_johnson_simplex_rejects_degenerate_point():
     k = GOLD["johnson_simplex"]
     for pol in (O.F32, O.F64):

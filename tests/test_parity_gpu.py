@@ -29,7 +29,8 @@ def oracle_mixed(batch, query, param, tol):
 
 def run_gpu(ctx, batch, query, param):
     db = Q.DeviceBatch.from_host(batch)
-    if query == O.CONTACT:
+    if query in (O.CONTACT, O.CONTACT_QUERY):
+        ctx.set_dispatch(N.DISPATCH_QUERY if query == O.CONTACT_QUERY else N.DISPATCH_SUPPORT_MAP)
         o = Q.contact_batch(ctx, db, prediction=param, with_iters=True)
     elif query == O.DISTANCE:
         o = Q.distance_batch(ctx, db, with_iters=True)
@@ -71,7 +72,7 @@ def check_query(ctx, batch, query, param, tol):
     assert_same("status", g["status"].view(np.uint32), r.status, batch)
     it = g["iters"].view(np.uint32)
     assert_same("gjk iterations", it & 0xffff, np.minimum(r.counters[:, 0], 0xffff), batch)
-    if query == O.CONTACT:
+    if query in (O.CONTACT, O.CONTACT_QUERY):
         assert_same("epa iterations", it >> 16, np.minimum(r.counters[:, 1], 0xffff), batch)
         assert_same("has_contact", g["has_contact"], r.tag, batch)
         m = r.tag == 1
@@ -109,6 +110,26 @@ def test_cuboid_pairs_contact_bit_exact(ctx_factory, tol):
 def test_mixed_convex_bit_exact(ctx_factory, tol, query, param):
     ctx = ctx_factory(tolerance=tol)
     check_query(ctx, W.mixed_convex(8192, seed=11), query, param, tol)
+
+
+@pytest.mark.parametrize("tol", TOLS)
+@pytest.mark.parametrize("param", [0.0, 0.3])
+def test_query_dispatch_bit_exact(ctx_factory, tol, param):
+    # query::contact routing: Ball-Ball analytic, Ball-Cuboid/ConvexHull by point projection
+    ctx = ctx_factory(tolerance=tol)
+    check_query(ctx, W.mixed_convex(8192, seed=18), O.CONTACT_QUERY, param, tol)
+    b = W.mixed_convex(4096, seed=19, kinds=(S.BALL, S.CUBOID, S.CONVEX_HULL))
+    check_query(ctx, b, O.CONTACT_QUERY, param, tol)
+
+
+def test_query_dispatch_contact_example(ctx_factory):
+    pairs = [(S.isometry(t), S.Ball(1.0), S.isometry(), S.Cuboid((1, 1, 1))) for t in ((1, 1, 1), (2, 2, 2), (3, 3, 3))]
+    pairs += [(S.isometry(), S.Cuboid((1, 1, 1)), S.isometry(t), S.Ball(1.0)) for t in ((1, 1, 1), (2, 2, 2), (3, 3, 3))]
+    ctx = ctx_factory()
+    g, _ = check_query(ctx, S.pack_pairs(pairs), O.CONTACT_QUERY, 1.0, N.TOL_REFERENCE)
+    has, depth = g["has_contact"], g["contact"][:, 9]
+    assert has[0] and depth[0] > 0 and has[1] and depth[1] < 0 and not has[2]   # examples/contact_query3d.rs
+    assert has[3] and depth[3] > 0 and has[4] and depth[4] < 0 and not has[5]   # flipped
 
 
 def test_epa_overflow_pass_is_exercised_and_exact(ctx_factory):
