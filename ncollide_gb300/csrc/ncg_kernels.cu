@@ -7,12 +7,16 @@
 //   3. gjk_warp     1 warp/pair over the hull list (dynamic queue); the hull
 //                   arg-max is warp-parallel with coalesced 128-bit loads.
 //   4. epa_thread   contact only, intersecting pairs: one thread per pair,
-//                   polytope of up to 96 vertices in the thread's local memory.
+//                   polytope of up to 48 vertices in the thread's local memory
+//                   (the median pair needs 13 iterations).
 //   5. epa tier A   pairs that outgrew epa_thread (and the EPA of hull pairs
 //                   when their GJK ran one warp per pair): one warp per pair,
 //                   up to 128 vertices in shared memory.
-//   6. epa tier B   pairs that outgrew tier A: up to 1280 vertices in shared
-//                   memory (1 warp per SM).
+//   6. epa tier B   pairs that outgrew tier A: up to 1280 vertices in a
+//                   global-memory slab per warp, as many warps per SM as
+//                   registers allow (the tail pairs run hundreds of
+//                   latency-bound iterations each, so concurrency wins over
+//                   shared-memory latency).
 //   7. epa tier C   pairs that outgrew tier B: a global-memory slab per warp
 //                   (up to 10240 vertices).
 // A pair that outgrows a stage is re-run by the next one from GJK's simplex.
@@ -88,16 +92,16 @@ struct Scratch {
     uint32_t* queue[4];  // item indices per EPA stage
     EpaItem* items;
     DevCounters* ctr;
-    char* slabs;
-    size_t slab_bytes;
-    int n_slabs;
+    char* slabs[2];  // global EPA stores of tiers B and C
+    size_t slab_bytes[2];
+    int n_slabs[2];
 };
 
 // EPA store capacities per stage: vertices, live face slots (about twice the
 // vertices), silhouette edges, flood-fill stack.  Stage 0 is the per-thread
 // store, 1-3 the warp tiers A, B, C.
 template <int T> struct EpaTier;
-template <> struct EpaTier<0> { static constexpr int VC = 96, FC = 2 * 96 + 16, SC = 48, TC = 160; };
+template <> struct EpaTier<0> { static constexpr int VC = 48, FC = 2 * 48 + 16, SC = 32, TC = 96; };
 template <> struct EpaTier<1> { static constexpr int VC = 128, FC = 2 * 128 + 64, SC = 64, TC = 256; };
 template <> struct EpaTier<2> { static constexpr int VC = 1280, FC = 2 * 1280 + 64, SC = 512, TC = 2048; };
 template <> struct EpaTier<3> { static constexpr int VC = 10240, FC = 2 * 10240 + 64, SC = 4096, TC = 16384; };
@@ -454,10 +458,10 @@ NCG_DEV void load_simplex(const EpaItem& it, CSO* sv) {
     }
 }
 
-// EPA tier t: tiers 0 and 1 keep the polytope in dynamic shared memory (one
-// warp per block), tier 2 in a global-memory slab per warp.  A pair whose
-// polytope outgrows its tier is queued for the next tier and re-run there from
-// GJK's simplex; at tier 2 it ends with NCG_STATUS_EPA_CAPACITY.  One kernel
+// EPA warp tier T: tier A (T = 1) keeps the polytope in dynamic shared memory
+// (one warp per block), tiers B and C in a global-memory slab per block.  A
+// pair whose polytope outgrows its tier is queued for the next tier and re-run
+// there from GJK's simplex; at tier C it ends with NCG_STATUS_EPA_CAPACITY.  One kernel
 // serves the three tiers (runtime capacities) to keep the code footprint small.
 struct TierCaps {
     int tier, VC, FC, SC, TC;
@@ -467,11 +471,11 @@ __global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs
     const unsigned lane = threadIdx.x & 31u;
     const int T = tc.tier;  // 1, 2 or 3
     EpaStore st;
-    if (T < 3) {
+    if (T == 1) {
         st.carve(smem, tc.VC, tc.FC, tc.SC, tc.TC);
     } else {
-        if (blockIdx.x >= (unsigned)s.n_slabs) return;
-        st.carve(s.slabs + (size_t)blockIdx.x * s.slab_bytes, tc.VC, tc.FC, tc.SC, tc.TC);
+        if (blockIdx.x >= (unsigned)s.n_slabs[T - 2]) return;
+        st.carve(s.slabs[T - 2] + (size_t)blockIdx.x * s.slab_bytes[T - 2], tc.VC, tc.FC, tc.SC, tc.TC);
     }
     const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[T];
     WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
@@ -508,6 +512,8 @@ __global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs
     }
     if (lane == 0 && acc) atomicAdd(&s.ctr->epa_iters, acc);
 }
+// Tier B runs at most this many warps per SM: 8 x 152 slabs of 206 KiB.
+constexpr int TIER_B_WARPS_PER_SM = 8;
 template <int T> TierCaps caps() { return TierCaps{T, EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC}; }
 
 // Thread stage: one thread per pair of analytic shapes, the polytope in the
@@ -585,12 +591,12 @@ struct ncg_ctx {
     int warm = NCG_WARM_NONE;
     int dispatch = NCG_DISPATCH_SUPPORT_MAP;
     int hull_gjk_warp = 0;  // GJK of ConvexHull pairs: 0 one thread per pair, 1 one warp per pair
-    int occ_thread = 1, occ_warp = 1, occ_epa0 = 1, occ_epa1 = 1, occ_ethread = 1;
+    int occ_thread = 1, occ_warp = 1, occ_epa0 = 1, occ_ethread = 1;
     char* scratch = nullptr;
     size_t scratch_cap_pairs = 0;
-    char* slabs = nullptr;
-    int n_slabs = 0;
-    size_t slab_bytes = 0;
+    char* slabs = nullptr;  // tier B slabs, then tier C slabs
+    int n_slabs[2] = {0, 0};
+    size_t slab_bytes[2] = {0, 0};
     DevCounters* host_ctr = nullptr;  // pinned
     ncg_stats last{};
     uint32_t launches = 0;
@@ -626,9 +632,12 @@ Scratch carve_scratch(ncg_ctx* c) {
     s.analytic = (uint32_t*)p; p += 4 * cap;
     s.hull = (uint32_t*)p; p += 4 * cap;
     for (int q = 0; q < 4; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * cap; }
-    s.slabs = c->slabs;
-    s.slab_bytes = c->slab_bytes;
-    s.n_slabs = c->n_slabs;
+    s.slabs[0] = c->slabs;
+    s.slabs[1] = c->slabs + c->slab_bytes[0] * c->n_slabs[0];
+    for (int t = 0; t < 2; ++t) {
+        s.slab_bytes[t] = c->slab_bytes[t];
+        s.n_slabs[t] = c->n_slabs[t];
+    }
     return s;
 }
 
@@ -675,9 +684,9 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
         mark(3);
         k_epa<<<c->num_sms * c->occ_epa0, 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>());
         mark(4);
-        k_epa<<<c->num_sms * c->occ_epa1, 32, tier_bytes<2>(), st>>>(bb, qp, o, s, caps<2>());
+        k_epa<<<c->n_slabs[0], 32, 0, st>>>(bb, qp, o, s, caps<2>());
         mark(5);
-        k_epa<<<c->n_slabs, 32, 0, st>>>(bb, qp, o, s, caps<3>());
+        k_epa<<<c->n_slabs[1], 32, 0, st>>>(bb, qp, o, s, caps<3>());
         mark(6);
         launches += 4;
     }
@@ -707,20 +716,25 @@ int ncg_ctx_create(ncg_ctx** out, int device) {
     ncg_ctx* c = new ncg_ctx();
     c->device = device;
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-    cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<2>());
+    cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<1>());
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_thread, k_gjk_thread, 128, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_warp, k_gjk_warp, 128, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa0, k_epa, 32, tier_bytes<1>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa1, k_epa, 32, tier_bytes<2>());
+    int occ_global = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_global, k_epa, 32, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_ethread, k_epa_thread, 128, 0);
     if (c->occ_ethread < 1) c->occ_ethread = 1;
     if (c->occ_thread < 1) c->occ_thread = 1;
     if (c->occ_warp < 1) c->occ_warp = 1;
     if (c->occ_epa0 < 1) c->occ_epa0 = 1;
-    if (c->occ_epa1 < 1) c->occ_epa1 = 1;
-    c->slab_bytes = (tier_bytes<3>() + 255) & ~size_t(255);
-    c->n_slabs = c->num_sms;
-    if (!cuda_ok(cudaMalloc(&c->slabs, c->slab_bytes * c->n_slabs), "cudaMalloc(slabs)") ||
+    if (occ_global < 1) occ_global = 1;
+    if (occ_global > TIER_B_WARPS_PER_SM) occ_global = TIER_B_WARPS_PER_SM;
+    c->slab_bytes[0] = (tier_bytes<2>() + 255) & ~size_t(255);
+    c->slab_bytes[1] = (tier_bytes<3>() + 255) & ~size_t(255);
+    c->n_slabs[0] = c->num_sms * occ_global;
+    c->n_slabs[1] = c->num_sms;
+    if (!cuda_ok(cudaMalloc(&c->slabs, c->slab_bytes[0] * c->n_slabs[0] + c->slab_bytes[1] * c->n_slabs[1]),
+                 "cudaMalloc(slabs)") ||
         !cuda_ok(cudaMallocHost(&c->host_ctr, sizeof(DevCounters)), "cudaMallocHost")) {
         ncg_ctx_destroy(c);
         return NCG_ENOMEM;
@@ -963,14 +977,17 @@ int ncg_proximity_batch_host(ncg_ctx* c, const ncg_batch* b, float margin, uint8
 // ncg_contact_batch_noalloc runs the contact pipeline on a fixed scratch array
 // in the library's device image instead of context-owned allocations.  Layout
 // of the array: counters (256 B), EPA work items, routing lists and stage
-// queues (6 x 4 B per pair), one tier-C EPA slab.
+// queues (6 x 4 B per pair), NA_TIER_B_SLABS tier-B EPA slabs, one tier-C slab.
 namespace {
 constexpr uint64_t NA_MAX_PAIRS = NCG_NOALLOC_MAX_PAIRS;
+constexpr int NA_TIER_B_SLABS = 32;
+constexpr size_t NA_SLAB_B_BYTES =
+    (EpaStore::bytes(EpaTier<2>::VC, EpaTier<2>::FC, EpaTier<2>::SC, EpaTier<2>::TC) + 255) & ~size_t(255);
 constexpr size_t NA_SLAB_BYTES =
     (EpaStore::bytes(EpaTier<3>::VC, EpaTier<3>::FC, EpaTier<3>::SC, EpaTier<3>::TC) + 255) & ~size_t(255);
 constexpr size_t NA_ITEMS_BYTES = sizeof(EpaItem) * NA_MAX_PAIRS;
 constexpr size_t NA_LISTS_BYTES = 6 * 4 * NA_MAX_PAIRS;
-constexpr size_t NA_BYTES = 256 + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_SLAB_BYTES;
+constexpr size_t NA_BYTES = 256 + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_TIER_B_SLABS * NA_SLAB_B_BYTES + NA_SLAB_BYTES;
 static_assert(sizeof(DevCounters) <= 256, "counters must fit their slot");
 }  // namespace
 
@@ -981,7 +998,7 @@ namespace {
 struct NoallocDevice {
     bool ready;
     char* base;  // device address of g_noalloc_scratch on this device
-    int num_sms, occ_thread, occ_warp, occ_epa0, occ_epa1, occ_ethread;
+    int num_sms, occ_thread, occ_warp, occ_epa0, occ_ethread;
 };
 std::mutex g_noalloc_mu;
 constexpr int NA_MAX_DEVICES = 64;
@@ -999,17 +1016,15 @@ int noalloc_setup(int dev, NoallocDevice& out) {
         d.base = (char*)p;
         if (!cuda_ok(cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev), "device attribute"))
             return NCG_ECUDA;
-        cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<2>());
+        cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<1>());
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_thread, k_gjk_thread, 128, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_warp, k_gjk_warp, 128, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_epa0, k_epa, 32, tier_bytes<1>());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_epa1, k_epa, 32, tier_bytes<2>());
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_ethread, k_epa_thread, 128, 0);
         if (d.occ_ethread < 1) d.occ_ethread = 1;
         if (d.occ_thread < 1) d.occ_thread = 1;
         if (d.occ_warp < 1) d.occ_warp = 1;
         if (d.occ_epa0 < 1) d.occ_epa0 = 1;
-        if (d.occ_epa1 < 1) d.occ_epa1 = 1;
         if (!cuda_ok(cudaGetLastError(), "noalloc set-up")) return NCG_ECUDA;
         d.ready = true;
     }
@@ -1050,9 +1065,13 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     s.analytic = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
     s.hull = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
     for (int q = 0; q < 4; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS; }
-    s.slabs = p;
-    s.slab_bytes = NA_SLAB_BYTES;
-    s.n_slabs = 1;
+    s.slabs[0] = p;
+    s.slab_bytes[0] = NA_SLAB_B_BYTES;
+    s.n_slabs[0] = NA_TIER_B_SLABS;
+    p += NA_TIER_B_SLABS * NA_SLAB_B_BYTES;
+    s.slabs[1] = p;
+    s.slab_bytes[1] = NA_SLAB_BYTES;
+    s.n_slabs[1] = 1;
 
     QueryParams qp;
     qp.query = Q_CONTACT;
@@ -1073,7 +1092,7 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s, 1);
     k_epa_thread<<<d.num_sms * d.occ_ethread, 128, 0, st>>>(bb, qp, o, s);
     k_epa<<<d.num_sms * d.occ_epa0, 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>());
-    k_epa<<<d.num_sms * d.occ_epa1, 32, tier_bytes<2>(), st>>>(bb, qp, o, s, caps<2>());
+    k_epa<<<NA_TIER_B_SLABS, 32, 0, st>>>(bb, qp, o, s, caps<2>());
     k_epa<<<1, 32, 0, st>>>(bb, qp, o, s, caps<3>());
     return cuda_ok(cudaGetLastError(), "noalloc kernel launch") ? NCG_OK : NCG_ECUDA;
 }
