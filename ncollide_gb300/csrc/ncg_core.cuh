@@ -23,6 +23,10 @@
 #include "../../include/ncg.h"
 
 #define NCG_DEV __device__ __forceinline__
+// Large double-word sub-solvers are kept out of line: inlined at every call
+// site they overflow the instruction cache (warps of a thread-per-pair kernel
+// sit in different sub-solver branches at the same time).
+#define NCG_OUTLINE __device__ __noinline__
 
 #include "ncg_dw.cuh"
 
@@ -319,7 +323,7 @@ struct EdgeTest {
     bool hit;
     real u;
 };
-NCG_DEV EdgeTest tet_edge(vec3<real> nabc, vec3<real> nabd, vec3<real> ap, vec3<real> ab, real ap_ab, real bp_ab) {
+NCG_OUTLINE EdgeTest tet_edge(vec3<real> nabc, vec3<real> nabd, vec3<real> ap, vec3<real> ab, real ap_ab, real bp_ab) {
     EdgeTest r;
     real ab_ab = ap_ab - bp_ab;
     vec3<real> x = cross(ap, ab);
@@ -329,7 +333,7 @@ NCG_DEV EdgeTest tet_edge(vec3<real> nabc, vec3<real> nabd, vec3<real> ap, vec3<
     r.u = r.hit ? ap_ab / ab_ab : real(0.0f);
     return r;
 }
-NCG_DEV bool tet_face(vec3<real> a, vec3<real> b, vec3<real> c, vec3<real> ap, vec3<real> bp, vec3<real> cp,
+NCG_OUTLINE bool tet_face(vec3<real> a, vec3<real> b, vec3<real> c, vec3<real> ap, vec3<real> bp, vec3<real> cp,
                       vec3<real> ab, vec3<real> ac, vec3<real> ad, real dabc, real dbca, real dacb, real eps,
                       vec3<real>& proj, real bc[3], uint32_t& status) {
     if (dabc < real(0.0f) && dbca < real(0.0f) && dacb < real(0.0f)) {

@@ -77,6 +77,17 @@ struct __align__(16) EpaItem {
     float v[4][9];
 };
 
+// Pairs are counting-sorted into cost buckets before GJK so that the threads
+// of a warp run pairs of one shape-kind combination (analytic pairs) or of
+// similar hull sizes (ConvexHull pairs): the hull arg-max scans of a warp then
+// take about the same time.  Buckets 0-24: analytic kind pairs (k1 * 5 + k2,
+// k1 <= k2); 25-36: ConvexHull pairs by floor(log2(points scanned)), largest
+// first.
+constexpr int NB_ANALYTIC = 25;
+constexpr int NB_HULL = 12;
+constexpr int NB = NB_ANALYTIC + NB_HULL;
+constexpr uint8_t NO_BUCKET = 0xff;
+
 struct DevCounters {
     unsigned long long n_analytic, n_hull;
     unsigned long long hull_next;
@@ -84,11 +95,14 @@ struct DevCounters {
     unsigned long long epa_count[4];  // items queued for: thread stage, tier A, B, C
     unsigned long long epa_next[4];
     unsigned long long gjk_iters, epa_iters;
+    uint32_t bucket_n[NB], bucket_fill[NB];
 };
+constexpr size_t CTR_SLOT = 512;
+static_assert(sizeof(DevCounters) <= CTR_SLOT, "counters must fit their slot");
 
 struct Scratch {
-    uint32_t* analytic;
-    uint32_t* hull;
+    uint8_t* bucket;  // per pair: its cost bucket, NO_BUCKET for bad input
+    uint32_t* sorted;  // pair indices by bucket: analytic pairs, then hull pairs
     uint32_t* queue[4];  // item indices per EPA stage
     EpaItem* items;
     DevCounters* ctr;
@@ -222,6 +236,33 @@ NCG_DEV vec3<float> initial_dir(const QueryParams& qp, const ncg_batch& b, uint3
 // Runs one pair through GJK; writes its outputs or its EPA work item.
 // All lanes of a warp call this with the same pair when Scan is WarpScan.
 // epa_queue: the EPA stage the pair starts in (0 = thread stage, 1 = warp tier A).
+// Writes an EPA work item (GJK's final simplex) and queues it for `queue`.
+NCG_DEV void enqueue_epa(const Scratch& s, uint32_t i, int queue, const Simplex& sx, uint32_t iters, uint32_t status,
+                         int mode, bool flip) {
+    unsigned long long slot = atomicAdd(&s.ctr->n_items, 1ull);
+    unsigned long long pos = atomicAdd(&s.ctr->epa_count[queue], 1ull);
+    s.queue[queue][pos] = (uint32_t)slot;
+    EpaItem& it = s.items[slot];
+    it.pair = i;
+    it.gjk_iters = iters;
+    it.status = status;
+    it.dim = (uint8_t)sx.dim;
+    it.mode = (uint8_t)mode;
+    it.flip = flip ? 1 : 0;
+    for (int k = 0; k <= sx.dim; ++k) {
+        const CSO& c = sx.v[k];
+        float* w = it.v[k];
+        w[0] = c.p.x; w[1] = c.p.y; w[2] = c.p.z;
+        w[3] = c.o1.x; w[4] = c.o1.y; w[5] = c.o1.z;
+        w[6] = c.o2.x; w[7] = c.o2.y; w[8] = c.o2.z;
+    }
+}
+
+// Runs one pair through GJK; writes its outputs or its EPA work item.
+// All lanes of a warp call this with the same pair when Scan is WarpScan.
+// epa_queue: the EPA stage the pair starts in (0 = thread stage, 1 = warp tier A).
+// Both GJK routes (the pair itself, or the point projection of a ball's centre
+// on a ConvexHull) share one inlined GJK loop to keep the kernel's code small.
 template <class Scan>
 NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, uint32_t i,
                       const Scan& scan, bool writer, unsigned long long& iter_acc, int epa_queue) {
@@ -230,18 +271,23 @@ NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& 
     load_shape(b, b.g2[i], g.g2);
     g.m1 = load_pose(b.m1 + i);
     g.m2 = load_pose(b.m2 + i);
+    int mode = 0;  // 0: GJK on the pair; 1: point projection of a ball's centre on a hull
+    bool flip = false;
+    const real pred = from_host(qp.param);
+    vec3<float> d;
+    real max_dist;
+    bool exact;
     if (qp.query == Q_CONTACT && qp.dispatch == NCG_DISPATCH_QUERY) {
         const bool b1 = g.g1.kind == NCG_BALL, b2 = g.g2.kind == NCG_BALL;
         const bool p1 = g.g1.kind == NCG_CUBOID || g.g1.kind == NCG_CONVEX_HULL;
         const bool p2 = g.g2.kind == NCG_CUBOID || g.g2.kind == NCG_CONVEX_HULL;
-        const real pred = from_host(qp.param);
         if (b1 && b2) {
             QContact q = contact_ball_ball(g.m1.t, g.g1.p0, g.m2.t, g.g2.p0, pred);
             if (writer) write_qcontact(o, i, q, 0, 0);
             return;
         }
         if ((b1 && p2) || (p1 && b2)) {
-            const bool flip = !b1;
+            flip = !b1;
             const Pose& pb = flip ? g.m2 : g.m1;
             const Shape& sb = flip ? g.g2 : g.g1;
             const Pose& pp = flip ? g.m1 : g.m2;
@@ -256,100 +302,102 @@ NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& 
                 return;
             }
             // point_projection_on_support_map: GJK on the translated hull
-            PairGeom pg = projection_geom(pp, sp, pb.t);
-            vec3<float> dir;
-            float dn;
-            if (!try_normalize(-pg.m1.t, FLT_EPSILON, dir, dn)) dir = mk(1.0f, 0.0f, 0.0f);
-            Simplex ps;
-            ps.reset(cso_support(pg, dir, scan));
-            uint32_t it = 0, st = 0;
-            GjkOut r = gjk(pg, dw_max(), true, ps, qp.tol, scan, it, st, qp.gjk_max_iter);
-            iter_acc += it;
-            if (r.kind == GJK_INTERSECTION) {
-                if (writer) {
-                    unsigned long long slot = atomicAdd(&s.ctr->n_items, 1ull);
-                    unsigned long long pos = atomicAdd(&s.ctr->epa_count[epa_queue], 1ull);
-                    s.queue[epa_queue][pos] = (uint32_t)slot;
-                    EpaItem& e = s.items[slot];
-                    e.pair = i;
-                    e.gjk_iters = it;
-                    e.status = st;
-                    e.dim = (uint8_t)ps.dim;
-                    e.mode = 1;
-                    e.flip = flip ? 1 : 0;
-                    for (int k = 0; k <= ps.dim; ++k) {
-                        const CSO& c = ps.v[k];
-                        float* w = e.v[k];
-                        w[0] = c.p.x; w[1] = c.p.y; w[2] = c.p.z;
-                        w[3] = c.o1.x; w[4] = c.o1.y; w[5] = c.o1.z;
-                        w[6] = c.o2.x; w[7] = c.o2.y; w[8] = c.o2.z;
-                    }
-                }
-                return;
-            }
-            bool inside = r.kind != GJK_CLOSEST_POINTS;  // the iteration cap: unreachable!() in gjk.rs:57
-            vec3<real> w2 = inside ? to_r(pb.t) : r.p1 + to_r(pb.t);
-            QContact q = ball_polyhedron_assemble(pb.t, sb.p0, inside, w2, F_UNKNOWN, 0, false, pred, flip);
-            if (writer) write_qcontact(o, i, q, st, pack_iters(it, 0));
-            return;
+            mode = 1;
         }
     }
-    vec3<float> d = initial_dir(qp, b, i, g);
+    PairGeom gg = g;
+    if (mode == 1) {
+        gg = projection_geom(flip ? g.m1 : g.m2, flip ? g.g1 : g.g2, flip ? g.m2.t : g.m1.t);
+        float dn;
+        if (!try_normalize(-gg.m1.t, FLT_EPSILON, d, dn)) d = mk(1.0f, 0.0f, 0.0f);
+        max_dist = dw_max();
+        exact = true;
+    } else {
+        d = initial_dir(qp, b, i, g);
+        max_dist = qp.query == Q_DISTANCE ? dw_max() : pred;
+        exact = qp.query != Q_PROXIMITY;
+    }
     Simplex sx;
-    sx.reset(cso_support(g, d, scan));
+    sx.reset(cso_support(gg, d, scan));
     uint32_t iters = 0, status = 0;
-    real max_dist = qp.query == Q_DISTANCE ? dw_max() : from_host(qp.param);
-    bool exact = qp.query != Q_PROXIMITY;
-    GjkOut r = gjk(g, max_dist, exact, sx, qp.tol, scan, iters, status, qp.gjk_max_iter);
+    GjkOut r = gjk(gg, max_dist, exact, sx, qp.tol, scan, iters, status, qp.gjk_max_iter);
     iter_acc += iters;
     if (qp.query == Q_CONTACT && r.kind == GJK_INTERSECTION) {
-        if (writer) {
-            unsigned long long slot = atomicAdd(&s.ctr->n_items, 1ull);
-            unsigned long long pos = atomicAdd(&s.ctr->epa_count[epa_queue], 1ull);
-            s.queue[epa_queue][pos] = (uint32_t)slot;
-            EpaItem& it = s.items[slot];
-            it.pair = i;
-            it.gjk_iters = iters;
-            it.status = status;
-            it.dim = (uint8_t)sx.dim;
-            it.mode = 0;
-            it.flip = 0;
-            for (int k = 0; k <= sx.dim; ++k) {
-                const CSO& c = sx.v[k];
-                float* w = it.v[k];
-                w[0] = c.p.x; w[1] = c.p.y; w[2] = c.p.z;
-                w[3] = c.o1.x; w[4] = c.o1.y; w[5] = c.o1.z;
-                w[6] = c.o2.x; w[7] = c.o2.y; w[8] = c.o2.z;
-            }
-        }
+        if (writer) enqueue_epa(s, i, epa_queue, sx, iters, status, mode, flip);
+        return;
+    }
+    if (mode == 1) {
+        const Pose& pb = flip ? g.m2 : g.m1;
+        const Shape& sb = flip ? g.g2 : g.g1;
+        bool inside = r.kind != GJK_CLOSEST_POINTS;  // the iteration cap: unreachable!() in gjk.rs:57
+        vec3<real> w2 = inside ? to_r(pb.t) : r.p1 + to_r(pb.t);
+        QContact q = ball_polyhedron_assemble(pb.t, sb.p0, inside, w2, F_UNKNOWN, 0, false, pred, flip);
+        if (writer) write_qcontact(o, i, q, status, pack_iters(iters, 0));
         return;
     }
     if (writer) write_outputs(qp, o, i, r, d, status, pack_iters(iters, 0));
 }
 
+NCG_DEV int pair_bucket(const Shape& a, const Shape& c) {
+    if (a.kind == NCG_CONVEX_HULL || c.kind == NCG_CONVEX_HULL) {
+        uint32_t n = (a.kind == NCG_CONVEX_HULL ? a.n : 0u) + (c.kind == NCG_CONVEX_HULL ? c.n : 0u);
+        int lg = 31 - __clz(n);  // n >= 1: load_shape rejects empty hulls
+        lg = lg < 3 ? 3 : (lg > 3 + NB_HULL - 1 ? 3 + NB_HULL - 1 : lg);
+        return NB_ANALYTIC + (3 + NB_HULL - 1 - lg);
+    }
+    uint32_t k1 = a.kind < c.kind ? a.kind : c.kind, k2 = a.kind < c.kind ? c.kind : a.kind;
+    return (int)(k1 * 5u + k2);
+}
+
+// Warp-aggregated add to a per-bucket counter; returns this thread's slot.
+NCG_DEV uint32_t bucket_slot(uint32_t* ctr, int key, bool active) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    uint32_t slot = 0;
+    if (active) {
+        const unsigned peers = __match_any_sync(act, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&ctr[key], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        slot = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    }
+    return slot;
+}
+
+// Validates every pair, writes the outputs of bad ones and counts the buckets.
 __global__ void k_classify(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool hull = false, analytic = false;
+    int key = -1;
     if (i < b.n_pairs) {
         Shape a, c;
         bool ok = load_shape(b, b.g1[i], a) && load_shape(b, b.g2[i], c);
         if (!ok) write_bad(qp, o, (uint32_t)i);
-        else if (a.kind == NCG_CONVEX_HULL || c.kind == NCG_CONVEX_HULL) hull = true;
-        else analytic = true;
+        else key = pair_bucket(a, c);
+        s.bucket[i] = key < 0 ? NO_BUCKET : (uint8_t)key;
     }
-    // warp-aggregated appends
-    const unsigned lane = threadIdx.x & 31u;
-    unsigned mh = __ballot_sync(0xffffffffu, hull), ma = __ballot_sync(0xffffffffu, analytic);
-    unsigned long long bh = 0, ba = 0;
-    if (lane == 0) {
-        if (mh) bh = atomicAdd(&s.ctr->n_hull, (unsigned long long)__popc(mh));
-        if (ma) ba = atomicAdd(&s.ctr->n_analytic, (unsigned long long)__popc(ma));
+    (void)bucket_slot(s.ctr->bucket_n, key < 0 ? 0 : key, key >= 0);
+}
+
+// Scatters the pairs into `sorted`, bucket by bucket (order inside a bucket is
+// arbitrary: every pair's result depends on the pair alone).
+__global__ void k_bucket(ncg_batch b, Scratch s) {
+    __shared__ uint32_t base[NB];
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int k = 0; k < NB; ++k) {
+            base[k] = acc;
+            acc += s.ctr->bucket_n[k];
+            if (k == NB_ANALYTIC - 1 && blockIdx.x == 0) s.ctr->n_analytic = acc;
+        }
+        if (blockIdx.x == 0) s.ctr->n_hull = acc - base[NB_ANALYTIC];
     }
-    bh = __shfl_sync(0xffffffffu, bh, 0);
-    ba = __shfl_sync(0xffffffffu, ba, 0);
-    unsigned below = (1u << lane) - 1u;
-    if (hull) s.hull[bh + __popc(mh & below)] = (uint32_t)i;
-    if (analytic) s.analytic[ba + __popc(ma & below)] = (uint32_t)i;
+    __syncthreads();
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int key = i < b.n_pairs ? (int)s.bucket[i] : (int)NO_BUCKET;
+    const bool active = key != NO_BUCKET;
+    const uint32_t slot = bucket_slot(s.ctr->bucket_fill, active ? key : 0, active);
+    if (active) s.sorted[base[key] + slot] = (uint32_t)i;
 }
 
 NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
@@ -362,7 +410,7 @@ NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
 // thread stage.
 __global__ void __launch_bounds__(128) k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list) {
     const unsigned long long n = *(volatile unsigned long long*)(list == 0 ? &s.ctr->n_analytic : &s.ctr->n_hull);
-    const uint32_t* ids = list == 0 ? s.analytic : s.hull;
+    const uint32_t* ids = list == 0 ? s.sorted : s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
     ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     unsigned long long acc = 0;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
@@ -377,6 +425,7 @@ __global__ void __launch_bounds__(128) k_gjk_thread(ncg_batch b, QueryParams qp,
 
 __global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
     const unsigned long long n = *(volatile unsigned long long*)&s.ctr->n_hull;
+    const uint32_t* ids = s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
     WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     const unsigned lane = threadIdx.x & 31u;
     unsigned long long acc = 0;
@@ -386,7 +435,7 @@ __global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, O
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= n) break;
         unsigned long long a = 0;
-        gjk_pair(b, qp, o, s, s.hull[k], scan, lane == 0, a, 1);
+        gjk_pair(b, qp, o, s, ids[k], scan, lane == 0, a, 1);
         if (lane == 0) acc += a;
     }
     warp_add(&s.ctr->gjk_iters, acc);
@@ -617,7 +666,7 @@ bool ensure_scratch(ncg_ctx* c, uint64_t n) {
     if (c->scratch) cudaFree(c->scratch);
     c->scratch = nullptr;
     uint64_t cap = n < 1024 ? 1024 : n;
-    size_t bytes = 6 * 4 * cap + sizeof(EpaItem) * cap + sizeof(DevCounters) + 1024;
+    size_t bytes = 6 * 4 * cap + sizeof(EpaItem) * cap + CTR_SLOT + 1024;
     if (!cuda_ok(cudaMalloc(&c->scratch, bytes), "cudaMalloc(scratch)")) return false;
     c->scratch_cap_pairs = cap;
     return true;
@@ -627,10 +676,10 @@ Scratch carve_scratch(ncg_ctx* c) {
     Scratch s;
     uint64_t cap = c->scratch_cap_pairs;
     char* p = c->scratch;
-    s.ctr = (DevCounters*)p; p += 256;
+    s.ctr = (DevCounters*)p; p += CTR_SLOT;
     s.items = (EpaItem*)p; p += sizeof(EpaItem) * cap;
-    s.analytic = (uint32_t*)p; p += 4 * cap;
-    s.hull = (uint32_t*)p; p += 4 * cap;
+    s.bucket = (uint8_t*)p; p += 4 * cap;
+    s.sorted = (uint32_t*)p; p += 4 * cap;
     for (int q = 0; q < 4; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * cap; }
     s.slabs[0] = c->slabs;
     s.slabs[1] = c->slabs + c->slab_bytes[0] * c->n_slabs[0];
@@ -672,13 +721,14 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     unsigned n = (unsigned)b->n_pairs;
     mark(-1);
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
+    k_bucket<<<(n + 255) / 256, 256, 0, st>>>(bb, s);
     mark(0);
     k_gjk_thread<<<c->num_sms * c->occ_thread, 128, 0, st>>>(bb, qp, o, s, 0);
     mark(1);
     if (c->hull_gjk_warp) k_gjk_warp<<<c->num_sms * c->occ_warp, 128, 0, st>>>(bb, qp, o, s);
     else k_gjk_thread<<<c->num_sms * c->occ_thread, 128, 0, st>>>(bb, qp, o, s, 1);
     mark(2);
-    launches += 3;
+    launches += 4;
     if (query == Q_CONTACT) {
         k_epa_thread<<<c->num_sms * c->occ_ethread, 128, 0, st>>>(bb, qp, o, s);
         mark(3);
@@ -976,7 +1026,7 @@ int ncg_proximity_batch_host(ncg_ctx* c, const ncg_batch* b, float margin, uint8
 // ------------------------------------------------------------------ no-allocation entry point
 // ncg_contact_batch_noalloc runs the contact pipeline on a fixed scratch array
 // in the library's device image instead of context-owned allocations.  Layout
-// of the array: counters (256 B), EPA work items, routing lists and stage
+// of the array: counters (512 B), EPA work items, routing lists and stage
 // queues (6 x 4 B per pair), NA_TIER_B_SLABS tier-B EPA slabs, one tier-C slab.
 namespace {
 constexpr uint64_t NA_MAX_PAIRS = NCG_NOALLOC_MAX_PAIRS;
@@ -987,8 +1037,7 @@ constexpr size_t NA_SLAB_BYTES =
     (EpaStore::bytes(EpaTier<3>::VC, EpaTier<3>::FC, EpaTier<3>::SC, EpaTier<3>::TC) + 255) & ~size_t(255);
 constexpr size_t NA_ITEMS_BYTES = sizeof(EpaItem) * NA_MAX_PAIRS;
 constexpr size_t NA_LISTS_BYTES = 6 * 4 * NA_MAX_PAIRS;
-constexpr size_t NA_BYTES = 256 + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_TIER_B_SLABS * NA_SLAB_B_BYTES + NA_SLAB_BYTES;
-static_assert(sizeof(DevCounters) <= 256, "counters must fit their slot");
+constexpr size_t NA_BYTES = CTR_SLOT + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_TIER_B_SLABS * NA_SLAB_B_BYTES + NA_SLAB_BYTES;
 }  // namespace
 
 // Host code must not use this name as an address: it is only a host-side stand-in.
@@ -1060,10 +1109,10 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     cudaStream_t st = (cudaStream_t)stream;
     Scratch s;
     char* p = d.base;
-    s.ctr = (DevCounters*)p; p += 256;
+    s.ctr = (DevCounters*)p; p += CTR_SLOT;
     s.items = (EpaItem*)p; p += NA_ITEMS_BYTES;
-    s.analytic = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
-    s.hull = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
+    s.bucket = (uint8_t*)p; p += 4 * NA_MAX_PAIRS;
+    s.sorted = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
     for (int q = 0; q < 4; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS; }
     s.slabs[0] = p;
     s.slab_bytes[0] = NA_SLAB_B_BYTES;
@@ -1088,6 +1137,7 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset noalloc counters")) return NCG_ECUDA;
     unsigned n = (unsigned)b->n_pairs;
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
+    k_bucket<<<(n + 255) / 256, 256, 0, st>>>(bb, s);
     k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s, 0);
     k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s, 1);
     k_epa_thread<<<d.num_sms * d.occ_ethread, 128, 0, st>>>(bb, qp, o, s);
