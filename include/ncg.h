@@ -154,6 +154,25 @@ int ncg_ctx_destroy(ncg_ctx* ctx);
 int ncg_ctx_set_tolerance(ncg_ctx* ctx, int tolerance);
 int ncg_ctx_set_warm_start(ncg_ctx* ctx, int warm_start);
 int ncg_ctx_set_dispatch(ncg_ctx* ctx, int dispatch);
+/* Launch tuning (no reference counterpart).  Keys:
+ *   NCG_TUNE_HULL_GJK_WARP   0: GJK of ConvexHull pairs one thread per pair
+ *                            (default), 1: one warp per pair
+ *   NCG_TUNE_GJK_BLOCKS      blocks of 128 threads per SM for the thread-per-pair
+ *                            GJK kernel; 0 = as many as fit (default)
+ *   NCG_TUNE_EPA_BLOCKS      the same for the thread-per-pair EPA kernel
+ *   NCG_TUNE_L1_CARVEOUT     shared-memory carveout (percent) preferred by the
+ *                            kernels that use no shared memory; -1 = driver
+ *                            default, 0 = largest L1 (default)
+ *   NCG_TUNE_TIER_B_WARPS    warps per SM of EPA tier B, 1..8 (default 8)
+ * Results do not depend on any of these. */
+enum ncg_tune {
+    NCG_TUNE_HULL_GJK_WARP = 0,
+    NCG_TUNE_GJK_BLOCKS = 1,
+    NCG_TUNE_EPA_BLOCKS = 2,
+    NCG_TUNE_L1_CARVEOUT = 3,
+    NCG_TUNE_TIER_B_WARPS = 4
+};
+int ncg_ctx_set_tuning(ncg_ctx* ctx, int key, int value);
 int ncg_sync(ncg_ctx* ctx, void* stream);
 int ncg_get_stats(ncg_ctx* ctx, ncg_stats* out);
 

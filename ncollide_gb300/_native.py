@@ -31,8 +31,9 @@ EXPORTED = [
     "ncg_get_stats", "ncg_last_error", "ncg_abi_version", "ncg_contact_batch", "ncg_distance_batch",
     "ncg_proximity_batch", "ncg_closest_points_batch", "ncg_contact_batch_host", "ncg_distance_batch_host",
     "ncg_proximity_batch_host", "ncg_ctx_set_profiling", "ncg_get_stage_ms", "ncg_contact_batch_noalloc",
-    "ncg_ctx_set_dispatch",
+    "ncg_ctx_set_dispatch", "ncg_ctx_set_tuning",
 ]
+TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT, TUNE_TIER_B_WARPS = range(5)
 DISPATCH_SUPPORT_MAP, DISPATCH_QUERY = 0, 1
 STATUS_UNSUPPORTED_FEATURE = 1 << 7
 NOALLOC_MAX_PAIRS = 32768

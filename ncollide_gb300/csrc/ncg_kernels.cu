@@ -641,6 +641,7 @@ struct ncg_ctx {
     int dispatch = NCG_DISPATCH_SUPPORT_MAP;
     int hull_gjk_warp = 0;  // GJK of ConvexHull pairs: 0 one thread per pair, 1 one warp per pair
     int occ_thread = 1, occ_warp = 1, occ_epa0 = 1, occ_ethread = 1;
+    int gjk_blocks = 0, epa_blocks = 0, l1_carveout = 0, tier_b_warps = 0, tier_b_max = 0;
     char* scratch = nullptr;
     size_t scratch_cap_pairs = 0;
     char* slabs = nullptr;  // tier B slabs, then tier C slabs
@@ -690,6 +691,17 @@ Scratch carve_scratch(ncg_ctx* c) {
     return s;
 }
 
+// Shared-memory carveout preference of the kernels without shared memory
+// (their local-memory and hull traffic wants the largest L1).
+bool set_carveout(int pct) {
+    bool ok = true;
+    ok &= cuda_ok(cudaFuncSetAttribute(k_gjk_thread, cudaFuncAttributePreferredSharedMemoryCarveout, pct),
+                  "carveout(k_gjk_thread)");
+    ok &= cuda_ok(cudaFuncSetAttribute(k_epa_thread, cudaFuncAttributePreferredSharedMemoryCarveout, pct),
+                  "carveout(k_epa_thread)");
+    return ok;
+}
+
 int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outputs& o, cudaStream_t st) {
     if (!c || !b) { g_last_error = "null context or batch"; return NCG_EINVAL; }
     if (b->n_pairs == 0) return NCG_OK;
@@ -723,18 +735,20 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
     k_bucket<<<(n + 255) / 256, 256, 0, st>>>(bb, s);
     mark(0);
-    k_gjk_thread<<<c->num_sms * c->occ_thread, 128, 0, st>>>(bb, qp, o, s, 0);
+    const int gjk_grid = c->num_sms * (c->gjk_blocks > 0 ? c->gjk_blocks : c->occ_thread);
+    k_gjk_thread<<<gjk_grid, 128, 0, st>>>(bb, qp, o, s, 0);
     mark(1);
     if (c->hull_gjk_warp) k_gjk_warp<<<c->num_sms * c->occ_warp, 128, 0, st>>>(bb, qp, o, s);
-    else k_gjk_thread<<<c->num_sms * c->occ_thread, 128, 0, st>>>(bb, qp, o, s, 1);
+    else k_gjk_thread<<<gjk_grid, 128, 0, st>>>(bb, qp, o, s, 1);
     mark(2);
     launches += 4;
     if (query == Q_CONTACT) {
-        k_epa_thread<<<c->num_sms * c->occ_ethread, 128, 0, st>>>(bb, qp, o, s);
+        k_epa_thread<<<c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread), 128, 0, st>>>(bb, qp, o,
+                                                                                                     s);
         mark(3);
         k_epa<<<c->num_sms * c->occ_epa0, 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>());
         mark(4);
-        k_epa<<<c->n_slabs[0], 32, 0, st>>>(bb, qp, o, s, caps<2>());
+        k_epa<<<c->num_sms * c->tier_b_warps, 32, 0, st>>>(bb, qp, o, s, caps<2>());
         mark(5);
         k_epa<<<c->n_slabs[1], 32, 0, st>>>(bb, qp, o, s, caps<3>());
         mark(6);
@@ -782,6 +796,8 @@ int ncg_ctx_create(ncg_ctx** out, int device) {
     c->slab_bytes[0] = (tier_bytes<2>() + 255) & ~size_t(255);
     c->slab_bytes[1] = (tier_bytes<3>() + 255) & ~size_t(255);
     c->n_slabs[0] = c->num_sms * occ_global;
+    c->tier_b_warps = c->tier_b_max = occ_global;
+    set_carveout(c->l1_carveout);
     c->n_slabs[1] = c->num_sms;
     if (!cuda_ok(cudaMalloc(&c->slabs, c->slab_bytes[0] * c->n_slabs[0] + c->slab_bytes[1] * c->n_slabs[1]),
                  "cudaMalloc(slabs)") ||
@@ -812,6 +828,36 @@ int ncg_ctx_set_tolerance(ncg_ctx* c, int tol) {
     if (!c || (tol != NCG_TOL_REFERENCE && tol != NCG_TOL_PRECISE)) return NCG_EINVAL;
     c->tol_mode = tol;
     return NCG_OK;
+}
+
+int ncg_ctx_set_tuning(ncg_ctx* c, int key, int value) {
+    if (!c) return NCG_EINVAL;
+    switch (key) {
+    case NCG_TUNE_HULL_GJK_WARP:
+        if (value != 0 && value != 1) return NCG_EINVAL;
+        c->hull_gjk_warp = value;
+        return NCG_OK;
+    case NCG_TUNE_GJK_BLOCKS:
+        if (value < 0 || value > c->occ_thread) return NCG_EINVAL;
+        c->gjk_blocks = value;
+        return NCG_OK;
+    case NCG_TUNE_EPA_BLOCKS:
+        if (value < 0 || value > c->occ_ethread) return NCG_EINVAL;
+        c->epa_blocks = value;
+        return NCG_OK;
+    case NCG_TUNE_L1_CARVEOUT:
+        if (value < -1 || value > 100) return NCG_EINVAL;
+        if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+        c->l1_carveout = value;
+        return set_carveout(value) ? NCG_OK : NCG_ECUDA;
+    case NCG_TUNE_TIER_B_WARPS:
+        if (value < 1 || value > c->tier_b_max) return NCG_EINVAL;
+        c->tier_b_warps = value;
+        return NCG_OK;
+    default:
+        g_last_error = "unknown tuning key";
+        return NCG_EINVAL;
+    }
 }
 
 int ncg_ctx_set_dispatch(ncg_ctx* c, int dispatch) {
