@@ -154,6 +154,119 @@ def accuracy_report(batch, gpu_out, sample, query):
     }
 
 
+def _quat_mul_t(a, b):
+    import torch
+    ai, aj, ak, aw = a.unbind(1)
+    bi, bj, bk, bw = b.unbind(1)
+    return torch.stack([aw * bi + ai * bw + aj * bk - ak * bj, aw * bj - ai * bk + aj * bw + ak * bi,
+                        aw * bk + ai * bj - aj * bi + ak * bw, aw * bw - ai * bi - aj * bj - ak * bk], 1)
+
+
+def _advance_poses_t(m, gen, sigma_t=0.01, sigma_r=0.02):
+    """One frame of coherent motion on the device (the workload generator's
+    advance_frame): translation += N(0, sigma_t^2) per axis, rotation about a
+    random axis by N(0, sigma_r^2) rad."""
+    import torch
+    n = m.shape[0]
+    ax = torch.randn((n, 3), generator=gen, device=m.device, dtype=torch.float64)
+    ax = ax / ax.norm(dim=1, keepdim=True)
+    ang = torch.randn(n, generator=gen, device=m.device, dtype=torch.float64) * sigma_r
+    dq = torch.cat([ax * torch.sin(ang / 2)[:, None], torch.cos(ang / 2)[:, None]], 1)
+    q = _quat_mul_t(dq, m[:, :4].double())
+    q = q / q.norm(dim=1, keepdim=True)
+    out = m.clone()
+    out[:, :4] = q.float()
+    out[:, 4:7] += (torch.randn((n, 3), generator=gen, device=m.device, dtype=torch.float64) * sigma_t).float()
+    return out
+
+
+def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32):
+    """Large coherent batch: ConvexHull-ConvexHull pairs over a pool of shared
+    hulls, stepped over 8 frames; plain GJK vs previous-frame direction reuse,
+    each frame one replay of a captured CUDA graph."""
+    import torch
+    from ncollide_gb300 import _native as Nn
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import workloads as W
+    from oracle import oracle as O
+    n, frames = args.coherent_pairs, 8
+    b0 = W.coherent_hull_pairs(n, seed=5, pool=1 << 16)
+    db = Q.DeviceBatch.from_host(b0, device=f"cuda:{local}")
+    gen = torch.Generator(device=f"cuda:{local}")
+    gen.manual_seed(5)
+    poses = [(db.m1.clone(), db.m2.clone())]
+    for _ in range(frames - 1):
+        poses.append((_advance_poses_t(poses[-1][0], gen), _advance_poses_t(poses[-1][1], gen)))
+    ctx = Q.Context(local, tolerance=tolerance, dispatch="support_map")
+    dirs = torch.empty((n, 3), dtype=torch.float32, device=db.m1.device)
+    g_plain = Q.ContactGraph(ctx, db, 0.0)
+    res = {}
+    for strategy in ("plain", "previous_frame_dir"):
+        if strategy == "previous_frame_dir":
+            ctx.set_warm_start(Nn.WARM_NONE)
+        times, iters = [], []
+        g_warm = None
+        for f in range(frames):
+            db.m1.copy_(poses[f][0])
+            db.m2.copy_(poses[f][1])
+            if strategy == "previous_frame_dir" and f == 1:
+                ctx.set_warm_start(Nn.WARM_INIT_DIR)
+                g_warm = Q.ContactGraph(ctx, db.with_init_dir(dirs), 0.0, reuse_dir=True)
+            g = g_warm if (strategy == "previous_frame_dir" and f >= 1) else g_plain
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            out = g.launch()
+            e1.record()
+            torch.cuda.synchronize()
+            if strategy == "previous_frame_dir" and f == 0:
+                dirs.copy_(out["dir"])
+            st = ctx.stats()
+            if f >= 1:
+                times.append(e0.elapsed_time(e1))
+                iters.append(st["gjk_iters"] / n)
+        last = {k: (None if v is None else v[:4096].cpu().numpy()) for k, v in out.items()}
+        ms = sum(times) / len(times)
+        res[strategy] = {"pairs_per_s": n / (ms / 1e3), "ms_per_frame": ms,
+                         "gjk_iters_per_pair": sum(iters) / len(iters), "frames_timed": len(times),
+                         "_last": last}
+        if g_warm is not None:
+            g_warm.close()
+    ctx.set_warm_start(Nn.WARM_NONE)
+    # algorithmic bytes / flops (plain-path counts from the oracle on a sample of frame 0)
+    sample = b0.subset(np.arange(16384))
+    rs = O.query(sample, O.CONTACT, O.MIXED, param=0.0, eps=-1.0 if tolerance == "precise" else 0.0,
+                 epa_tol=1e-6 if tolerance == "precise" else 0.0)
+    bytes_pp, _, _, flops_pp = algorithmic(sample, rs.counters)
+    # accuracy of the last frame (first 4096 pairs) against the f64 oracle
+    lastb = b0.subset(np.arange(4096))
+    lastb = type(lastb)(lastb.shapes, lastb.hull_points, poses[-1][0][:4096].cpu().numpy(), lastb.g1,
+                        poses[-1][1][:4096].cpu().numpy(), lastb.g2, None, lastb.scale, dict(lastb.meta))
+    r64 = O.query(lastb, O.CONTACT, O.F64, param=0.0)
+    both_ok = True
+    for strategy, r in res.items():
+        last = r.pop("_last")
+        m = (last["has_contact"] == 1) & (r64.tag == 1)
+        rel = np.abs(last["contact"][:, 9].astype(np.float64) - r64.value) / np.maximum(np.abs(r64.value),
+                                                                                      lastb.scale)
+        r["depth_rel_err_vs_f64"] = {"p99": float(np.percentile(rel[m], 99)) if m.any() else None,
+                                     "max": float(rel[m].max()) if m.any() else None}
+        r["classification_mismatch_vs_f64"] = int((last["has_contact"] != r64.tag).sum())
+        r["hbm_gbs"] = r["pairs_per_s"] * bytes_pp / 1e9
+        r["hbm_frac"] = r["hbm_gbs"] / peak_hbm
+        r["fp32_frac"] = r["pairs_per_s"] * flops_pp / 1e12 / peak_fp32
+        both_ok &= r["classification_mismatch_vs_f64"] >= 0
+    g_plain.close()
+    ctx.close()
+    out = {"workload": f"coherent_hull_pairs: {n} ConvexHull-ConvexHull pairs, 32-1024 points, pool of 65536 "
+                       f"shared hulls, 8 frames (sigma_t 0.01, sigma_r 0.02), seed 5; frames 1-7 timed",
+           "strategies": res,
+           "speedup_previous_frame_vs_plain": res["previous_frame_dir"]["pairs_per_s"] / res["plain"]["pairs_per_s"],
+           "bytes_per_pair": bytes_pp, "flops_per_pair": flops_pp,
+           "accuracy_sample": "first 4096 pairs of the last frame"}
+    return out
+
+
 def cpu_baseline(batch, threads, query):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -208,6 +321,9 @@ def main():
     ap.add_argument("--accuracy-sample", type=int, default=32768)
     ap.add_argument("--pairs", type=int, default=N_PAIRS,
                     help="workload size (profiling runs only: the reported config is 1048576 pairs)")
+    ap.add_argument("--coherent-pairs", type=int, default=1 << 21,
+                    help="pairs of the coherent warm-start workload (16777216 for the full configuration)")
+    ap.add_argument("--no-coherent", action="store_true")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profiling: stop after the timed device steps (no second dispatch, no e2e, no report)")
     args = ap.parse_args()
@@ -365,6 +481,10 @@ def main():
         out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
         acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs), qo)
 
+    coherent = None
+    if not args.no_coherent:
+        coherent = coherent_warm_start(args, local, args.tolerance, hbm_peak, fp32_peak)
+
     line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -374,7 +494,7 @@ def main():
                        "seed": SEED, "parallelism": f"weak x{world}" if world > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (%.2f GB resident)" % (batch.nbytes_inputs() / 1e9)},
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
-            "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc,
+            "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc, "warm_start_coherent": coherent,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
             "epa": {"pairs": stats["n_epa"], "tier_b_pairs": stats["n_epa_overflow"],

@@ -143,7 +143,8 @@ typedef struct ncg_stats {
     uint64_t gjk_iters;      /* sum over pairs                                */
     uint64_t epa_iters;      /* sum over pairs                                */
     uint32_t kernels_launched;
-    uint32_t pad;
+    uint32_t flags;          /* bit 0: a learned warm-start tensor-core wait
+                                timed out (directions fell back to default) */
 } ncg_stats;
 
 /* ---- context --------------------------------------------------------------- */
@@ -197,6 +198,59 @@ int ncg_abi_version(void);
 int ncg_contact_batch(ncg_ctx* ctx, const ncg_batch* batch, float prediction,
                       ncg_contact* out, uint8_t* has_contact, float* out_dir,
                       uint32_t* status, uint32_t* iters, void* stream);
+
+/* ---- learned warm start (no reference counterpart) --------------------------
+ * A 39 -> 128 -> 128 -> 4 MLP (GELU) predicts GJK's first search direction
+ * and the sign of the separation from the relative pose and two 16-float
+ * shape descriptors.  Parameters: NCG_MLP_N_PARAMS f32 values laid out
+ * W1[128][48], b1[128], W2[128][128], b2[128], W3[4][128], b3[4] (inputs
+ * 39..47 are zero padding).  With NCG_WARM_MLP the context runs the network
+ * (tcgen05 tensor cores, bf16 operands, f32 accumulation) before GJK and uses
+ * its unit direction as init_dir; GJK and EPA still run to their own
+ * termination.  Training entry points work on device buffers:
+ *   ncg_mlp_features   shape descriptors (desc: 16 floats per shape) and the
+ *                      48 input features of every pair (X: 48 floats per pair)
+ *   ncg_mlp_infer      the network's world-space unit direction per pair
+ *   ncg_mlp_grad       mean-loss gradient of a batch of n samples: X [n][48],
+ *                      labels [n][4] = unit direction in the first shape's
+ *                      frame, then 1 (intersecting) or 0; loss = (1 - cos) +
+ *                      logit_weight * BCE.  partial needs ceil(n/128) *
+ *                      (NCG_MLP_N_PARAMS + 4) floats; grad receives
+ *                      NCG_MLP_N_PARAMS gradients then the loss, the
+ *                      direction loss and the logit loss
+ *   ncg_mlp_adam       one Adam step (step counts from 1)
+ * err (device uint32) gets bit 0 when a tensor-core wait times out. */
+#define NCG_MLP_N_INPUTS 48
+#define NCG_MLP_N_PARAMS 23300
+int ncg_mlp_n_params(void);
+int ncg_ctx_set_mlp_params(ncg_ctx* ctx, const float* params, int n);
+int ncg_mlp_features(const ncg_batch* batch, float* desc, float* X, void* stream);
+int ncg_mlp_infer(const ncg_batch* batch, const float* params, float* desc, float* init_dir, uint32_t* err,
+                  void* stream);
+int ncg_mlp_grad(const float* params, const float* X, const float* labels, uint64_t n, float logit_weight,
+                 float* partial, float* grad, uint32_t* err, void* stream);
+int ncg_mlp_adam(float* params, float* m, float* v, const float* grad, float lr, float beta1, float beta2,
+                 float eps, int step, void* stream);
+
+/* ---- CUDA graphs of one query (no reference counterpart) ------------------
+ * ncg_contact_graph_create captures one ncg_contact_batch call with these
+ * arguments into a CUDA graph owned by the context.  Each ncg_graph_launch
+ * re-runs the query on whatever the batch's device buffers hold when the
+ * replay executes (poses updated in place between frames, an init_dir buffer
+ * refreshed from out_dir), with the context's tolerance, dispatch and warm
+ * start as they were at capture time.  out_dir may alias batch->init_dir: each
+ * pair reads its init_dir before its out_dir is written, which gives the
+ * previous-frame direction reuse of the reference's manifold generator
+ * (convex_polyhedron_convex_polyhedron_manifold_generator.rs:96-145).
+ * Replays and other calls on the same context share its scratch: serialise
+ * them on one stream.  The graph is destroyed with ncg_graph_destroy or with
+ * the context. */
+typedef struct ncg_graph ncg_graph;
+int ncg_contact_graph_create(ncg_ctx* ctx, const ncg_batch* batch, float prediction,
+                             ncg_contact* out, uint8_t* has_contact, float* out_dir,
+                             uint32_t* status, uint32_t* iters, ncg_graph** graph);
+int ncg_graph_launch(ncg_graph* graph, void* stream);
+int ncg_graph_destroy(ncg_graph* graph);
 
 /* distance_support_map_support_map_with_params for every pair. */
 int ncg_distance_batch(ncg_ctx* ctx, const ncg_batch* batch, float* out_dist,

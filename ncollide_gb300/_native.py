@@ -31,8 +31,11 @@ EXPORTED = [
     "ncg_get_stats", "ncg_last_error", "ncg_abi_version", "ncg_contact_batch", "ncg_distance_batch",
     "ncg_proximity_batch", "ncg_closest_points_batch", "ncg_contact_batch_host", "ncg_distance_batch_host",
     "ncg_proximity_batch_host", "ncg_ctx_set_profiling", "ncg_get_stage_ms", "ncg_contact_batch_noalloc",
-    "ncg_ctx_set_dispatch", "ncg_ctx_set_tuning",
+    "ncg_ctx_set_dispatch", "ncg_ctx_set_tuning", "ncg_contact_graph_create", "ncg_graph_launch",
+    "ncg_graph_destroy", "ncg_mlp_n_params", "ncg_ctx_set_mlp_params", "ncg_mlp_features", "ncg_mlp_infer",
+    "ncg_mlp_grad", "ncg_mlp_adam",
 ]
+MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
 TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT, TUNE_TIER_B_WARPS = range(5)
 DISPATCH_SUPPORT_MAP, DISPATCH_QUERY = 0, 1
 STATUS_UNSUPPORTED_FEATURE = 1 << 7
@@ -50,7 +53,7 @@ class NcgBatch(ctypes.Structure):
 class NcgStats(ctypes.Structure):
     _fields_ = [("n_pairs", ctypes.c_uint64), ("n_epa", ctypes.c_uint64), ("n_epa_overflow", ctypes.c_uint64),
                 ("gjk_iters", ctypes.c_uint64), ("epa_iters", ctypes.c_uint64),
-                ("kernels_launched", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+                ("kernels_launched", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
 
 
 class NcgError(RuntimeError):
@@ -90,6 +93,16 @@ def load(build_if_missing=True):
     L.ncg_ctx_set_dispatch.argtypes = [vp, i32]
     L.ncg_get_stage_ms.argtypes = [vp, vp, i32]
     L.ncg_contact_batch_noalloc.argtypes = [P(NcgBatch), f32, i32, vp, vp, vp, vp, vp]
+    L.ncg_ctx_set_tuning.argtypes = [vp, i32, i32]
+    L.ncg_contact_graph_create.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp, vp, P(vp)]
+    L.ncg_graph_launch.argtypes = [vp, vp]
+    L.ncg_graph_destroy.argtypes = [vp]
+    L.ncg_mlp_n_params.argtypes = []
+    L.ncg_ctx_set_mlp_params.argtypes = [vp, vp, i32]
+    L.ncg_mlp_features.argtypes = [P(NcgBatch), vp, vp, vp]
+    L.ncg_mlp_infer.argtypes = [P(NcgBatch), vp, vp, vp, vp, vp]
+    L.ncg_mlp_grad.argtypes = [vp, vp, vp, ctypes.c_uint64, f32, vp, vp, vp, vp]
+    L.ncg_mlp_adam.argtypes = [vp, vp, vp, vp, f32, f32, f32, f32, i32, vp]
     for name in EXPORTED:
         if name != "ncg_last_error":
             getattr(L, name).restype = ctypes.c_int

@@ -15,8 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libncg.so")
-SOURCES = ["ncg_kernels.cu"]
-HEADERS = ["ncg_core.cuh", "ncg_epa.cuh"]
+SOURCES = ["ncg_kernels.cu", "ncg_mlp.cu"]
+HEADERS = ["ncg_core.cuh", "ncg_epa.cuh", "ncg_dw.cuh", "ncg_query.cuh", "ncg_tc.cuh", "ncg_mlp.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-shared"]
@@ -40,14 +40,23 @@ def _stale():
 
 
 def build(force=False, verbose=False, extra=()):
+    """Compiles each translation unit in parallel, then links libncg.so."""
     if not force and not _stale():
         return LIB_PATH
     os.makedirs(LIB_DIR, exist_ok=True)
-    tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-o", tmp] + [os.path.join(CSRC, s) for s in SOURCES]
+    objs = [os.path.join(LIB_DIR, os.path.splitext(s)[0] + ".o") for s in SOURCES]
+    flags = [f for f in NVCC_FLAGS if f != "-shared"]
+    cmds = [[nvcc(), *ARCH, *flags, *extra, "-c", "-o", o, os.path.join(CSRC, s)] for s, o in zip(SOURCES, objs)]
     if verbose:
-        print(" ".join(cmd), file=sys.stderr)
-    subprocess.run(cmd, check=True)
+        for c in cmds:
+            print(" ".join(c), file=sys.stderr)
+    procs = [subprocess.Popen(c) for c in cmds]
+    rcs = [p.wait() for p in procs]
+    if any(rcs):
+        raise RuntimeError(f"nvcc failed: {rcs}")
+    tmp = LIB_PATH + ".tmp"
+    link = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", tmp, *objs]
+    subprocess.run(link, check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 

@@ -26,7 +26,7 @@
 // Large double-word sub-solvers are kept out of line: inlined at every call
 // site they overflow the instruction cache (warps of a thread-per-pair kernel
 // sit in different sub-solver branches at the same time).
-#define NCG_OUTLINE __device__ __noinline__
+#define NCG_OUTLINE static __device__ __noinline__
 
 #include "ncg_dw.cuh"
 

@@ -34,6 +34,7 @@
 
 #include "../../include/ncg.h"
 #include "ncg_core.cuh"
+#include "ncg_mlp.h"
 #include "ncg_epa.cuh"
 #include "ncg_query.cuh"
 
@@ -96,6 +97,7 @@ struct DevCounters {
     unsigned long long epa_next[4];
     unsigned long long gjk_iters, epa_iters;
     uint32_t bucket_n[NB], bucket_fill[NB];
+    uint32_t mlp_err;  // bit 0: a learned warm-start tensor-core wait timed out
 };
 constexpr size_t CTR_SLOT = 512;
 static_assert(sizeof(DevCounters) <= CTR_SLOT, "counters must fit their slot");
@@ -596,6 +598,12 @@ __global__ void __launch_bounds__(128) k_epa_thread(ncg_batch b, QueryParams qp,
 }
 
 // ------------------------------------------------------------------ host side
+}  // namespace
+namespace ncg {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace ncg
+namespace {
+
 bool cuda_ok(cudaError_t e, const char* what) {
     if (e == cudaSuccess) return true;
     g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
@@ -655,6 +663,13 @@ struct ncg_ctx {
     size_t stage_cap = 0;
     cudaStream_t own_stream = nullptr;
     int profiling = 0;
+    std::vector<ncg_graph*> graphs;  // destroyed with the context
+    float* mlp_params = nullptr;     // NCG_MLP_N_PARAMS floats (device)
+    float* desc_buf = nullptr;       // shape descriptors for the network
+    size_t desc_cap = 0;
+    float* idir_buf = nullptr;       // the network's init_dir per pair
+    size_t idir_cap = 0;
+    uint32_t graph_launches = 0;     // kernels in a captured query
     int n_marks = 0;
     int mark_stage[NCG_N_STAGES + 1];
     cudaEvent_t marks[NCG_N_STAGES + 1] = {};
@@ -731,6 +746,32 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     };
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset counters")) return NCG_ECUDA;
     unsigned n = (unsigned)b->n_pairs;
+    if (c->warm == NCG_WARM_MLP && (query == Q_CONTACT || query == Q_PROXIMITY)) {
+        // the network's start direction replaces the default one (contact and
+        // proximity start from normalize(t2 - t1) in the reference)
+        if (!c->mlp_params) { g_last_error = "NCG_WARM_MLP without parameters (ncg_ctx_set_mlp_params)"; return NCG_EINVAL; }
+        if (c->desc_cap < b->n_shapes) {
+            if (c->desc_buf) cudaFree(c->desc_buf);
+            c->desc_buf = nullptr;
+            c->desc_cap = 0;
+            if (!cuda_ok(cudaMalloc(&c->desc_buf, 64 * (size_t)(b->n_shapes < 1024 ? 1024 : b->n_shapes)), "cudaMalloc(desc)"))
+                return NCG_ENOMEM;
+            c->desc_cap = b->n_shapes < 1024 ? 1024 : b->n_shapes;
+        }
+        if (c->idir_cap < b->n_pairs) {
+            if (c->idir_buf) cudaFree(c->idir_buf);
+            c->idir_buf = nullptr;
+            c->idir_cap = 0;
+            if (!cuda_ok(cudaMalloc(&c->idir_buf, 12 * (size_t)b->n_pairs), "cudaMalloc(init_dir)")) return NCG_ENOMEM;
+            c->idir_cap = b->n_pairs;
+        }
+        int rc = mlp_shape_desc(bb, c->desc_buf, st);
+        if (rc == NCG_OK) rc = mlp_infer(bb, c->mlp_params, c->desc_buf, c->idir_buf, &s.ctr->mlp_err, c->num_sms, st);
+        if (rc != NCG_OK) return rc;
+        bb.init_dir = c->idir_buf;
+        qp.use_init_dir = 1;
+        launches += 2;
+    }
     mark(-1);
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
     k_bucket<<<(n + 255) / 256, 256, 0, st>>>(bb, s);
@@ -759,6 +800,7 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
                  "copy counters"))
         return NCG_ECUDA;
     c->launches = launches;
+    c->graph_launches = launches;
     c->last.n_pairs = b->n_pairs;
     return NCG_OK;
 }
@@ -812,9 +854,13 @@ int ncg_ctx_create(ncg_ctx** out, int device) {
 
 int ncg_ctx_destroy(ncg_ctx* c) {
     if (!c) return NCG_OK;
+    while (!c->graphs.empty()) ncg_graph_destroy(c->graphs.back());
     cudaSetDevice(c->device);
     if (c->scratch) cudaFree(c->scratch);
     if (c->slabs) cudaFree(c->slabs);
+    if (c->mlp_params) cudaFree(c->mlp_params);
+    if (c->desc_buf) cudaFree(c->desc_buf);
+    if (c->idir_buf) cudaFree(c->idir_buf);
     if (c->stage) cudaFree(c->stage);
     if (c->host_ctr) cudaFreeHost(c->host_ctr);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -828,6 +874,16 @@ int ncg_ctx_set_tolerance(ncg_ctx* c, int tol) {
     if (!c || (tol != NCG_TOL_REFERENCE && tol != NCG_TOL_PRECISE)) return NCG_EINVAL;
     c->tol_mode = tol;
     return NCG_OK;
+}
+
+int ncg_ctx_set_mlp_params(ncg_ctx* c, const float* params, int n) {
+    if (!c || !params || n != NCG_MLP_N_PARAMS) { g_last_error = "expected NCG_MLP_N_PARAMS parameters"; return NCG_EINVAL; }
+    if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    if (!c->mlp_params && !cuda_ok(cudaMalloc(&c->mlp_params, 4 * (size_t)n), "cudaMalloc(mlp params)"))
+        return NCG_ENOMEM;
+    // host or device source (unified addressing)
+    return cuda_ok(cudaMemcpy(c->mlp_params, params, 4 * (size_t)n, cudaMemcpyDefault), "copy mlp params") ? NCG_OK
+                                                                                                          : NCG_ECUDA;
 }
 
 int ncg_ctx_set_tuning(ncg_ctx* c, int key, int value) {
@@ -895,7 +951,7 @@ int ncg_get_stage_ms(ncg_ctx* c, float* ms, int n_max) {
 }
 
 int ncg_ctx_set_warm_start(ncg_ctx* c, int w) {
-    if (!c || w < NCG_WARM_NONE || w > NCG_WARM_INIT_DIR) return NCG_EINVAL;
+    if (!c || w < NCG_WARM_NONE || w > NCG_WARM_MLP) return NCG_EINVAL;
     c->warm = w;
     return NCG_OK;
 }
@@ -916,7 +972,7 @@ int ncg_get_stats(ncg_ctx* c, ncg_stats* out) {
     out->gjk_iters = c->host_ctr->gjk_iters;
     out->epa_iters = c->host_ctr->epa_iters;
     out->kernels_launched = c->launches;
-    out->pad = 0;
+    out->flags = c->host_ctr->mlp_err & 1u;
     return NCG_OK;
 }
 
@@ -926,6 +982,68 @@ int ncg_contact_batch(ncg_ctx* c, const ncg_batch* b, float prediction, ncg_cont
     if (!out || !has_contact) { g_last_error = "null output"; return NCG_EINVAL; }
     Outputs o{out, has_contact, out_dir, nullptr, nullptr, status, iters};
     return run_query(c, b, Q_CONTACT, prediction, o, (cudaStream_t)stream);
+}
+
+struct ncg_graph {
+    ncg_ctx* ctx;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+};
+
+int ncg_contact_graph_create(ncg_ctx* c, const ncg_batch* b, float prediction, ncg_contact* out, uint8_t* has_contact,
+                             float* out_dir, uint32_t* status, uint32_t* iters, ncg_graph** g) {
+    if (!g) return NCG_EINVAL;
+    *g = nullptr;
+    if (!c || !b || !out || !has_contact) { g_last_error = "null argument"; return NCG_EINVAL; }
+    if (b->n_pairs == 0) { g_last_error = "empty batch"; return NCG_EINVAL; }
+    if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    // everything that allocates happens before the capture
+    if (!ensure_scratch(c, b->n_pairs)) return NCG_ENOMEM;
+    cudaStream_t cs;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate")) return NCG_ECUDA;
+    const int prof = c->profiling;
+    c->profiling = 0;
+    Outputs o{out, has_contact, out_dir, nullptr, nullptr, status, iters};
+    int rc = NCG_OK;
+    cudaGraph_t graph = nullptr;
+    if (!cuda_ok(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture")) rc = NCG_ECUDA;
+    if (rc == NCG_OK) {
+        rc = run_query(c, b, Q_CONTACT, prediction, o, cs);
+        cudaError_t e = cudaStreamEndCapture(cs, &graph);
+        if (rc == NCG_OK && !cuda_ok(e, "cudaStreamEndCapture")) rc = NCG_ECUDA;
+    }
+    c->profiling = prof;
+    cudaGraphExec_t exec = nullptr;
+    if (rc == NCG_OK && !cuda_ok(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate")) rc = NCG_ECUDA;
+    cudaStreamDestroy(cs);
+    if (rc != NCG_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    ncg_graph* h = new ncg_graph{c, graph, exec};
+    c->graphs.push_back(h);
+    *g = h;
+    return NCG_OK;
+}
+
+int ncg_graph_launch(ncg_graph* g, void* stream) {
+    if (!g) return NCG_EINVAL;
+    if (!cuda_ok(cudaSetDevice(g->ctx->device), "cudaSetDevice")) return NCG_ECUDA;
+    if (!cuda_ok(cudaGraphLaunch(g->exec, (cudaStream_t)stream), "cudaGraphLaunch")) return NCG_ECUDA;
+    g->ctx->launches = g->ctx->graph_launches;
+    return NCG_OK;
+}
+
+int ncg_graph_destroy(ncg_graph* g) {
+    if (!g) return NCG_OK;
+    auto& v = g->ctx->graphs;
+    for (size_t i = 0; i < v.size(); ++i)
+        if (v[i] == g) { v.erase(v.begin() + (long)i); break; }
+    cudaSetDevice(g->ctx->device);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return NCG_OK;
 }
 
 int ncg_distance_batch(ncg_ctx* c, const ncg_batch* b, float* out_dist, uint32_t* status, uint32_t* iters,

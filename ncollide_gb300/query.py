@@ -71,6 +71,17 @@ class Context:
         N.check(self._L.ncg_ctx_set_warm_start(self._p, int(mode)), "ncg_ctx_set_warm_start")
         self.warm_start = int(mode)
 
+    def set_mlp_params(self, params):
+        """Parameters of the learned warm start (NCG_MLP_N_PARAMS f32 values, host or device)."""
+        if isinstance(params, torch.Tensor):
+            t = params.detach().contiguous().float()
+            N.check(self._L.ncg_ctx_set_mlp_params(self._p, ctypes.c_void_p(t.data_ptr()), int(t.numel())),
+                    "ncg_ctx_set_mlp_params")
+        else:
+            a = np.ascontiguousarray(params, np.float32)
+            N.check(self._L.ncg_ctx_set_mlp_params(self._p, ctypes.c_void_p(a.ctypes.data), int(a.size)),
+                    "ncg_ctx_set_mlp_params")
+
     def set_profiling(self, on=True):
         """Records CUDA events between the library's kernel launches."""
         N.check(self._L.ncg_ctx_set_profiling(self._p, 1 if on else 0), "ncg_ctx_set_profiling")
@@ -87,7 +98,7 @@ class Context:
     def stats(self):
         s = N.NcgStats()
         N.check(self._L.ncg_get_stats(self._p, ctypes.byref(s)), "ncg_get_stats")
-        return {k: int(getattr(s, k)) for k, _ in N.NcgStats._fields_ if k != "pad"}
+        return {k: int(getattr(s, k)) for k, _ in N.NcgStats._fields_ }
 
     def close(self):
         if self._p:
@@ -167,6 +178,47 @@ def contact_batch(ctx: Context, db: DeviceBatch, prediction=0.0, with_dir=True, 
                                      _ptr(out["has_contact"]), _ptr(out["dir"]), _ptr(out["status"]),
                                      _ptr(out["iters"]), _stream(stream)), "ncg_contact_batch")
     return out
+
+
+class ContactGraph:
+    """One ncg_contact_batch call captured as a CUDA graph (ncg_contact_graph_create).
+
+    `launch()` replays it on the batch's buffers as they are at replay time;
+    the outputs live in `self.out`.  With `reuse_dir=True` the batch's init_dir
+    buffer is also the out_dir buffer, so each replay starts GJK from the
+    direction the previous replay returned (the reference's `last_gjk_dir`);
+    the context must then have NCG_WARM_INIT_DIR set."""
+
+    def __init__(self, ctx: Context, db: DeviceBatch, prediction=0.0, reuse_dir=False, with_iters=False):
+        n, dev = db.n_pairs, db.m1.device
+        self.ctx, self.db = ctx, db
+        self.out = {"contact": _empty(n, (10,), torch.float32, dev), "has_contact": _empty(n, (), torch.uint8, dev),
+                    "status": _empty(n, (), torch.int32, dev),
+                    "iters": _empty(n, (), torch.int32, dev) if with_iters else None}
+        if reuse_dir:
+            if db.init_dir is None:
+                raise ValueError("reuse_dir needs a batch with an init_dir buffer")
+            self.out["dir"] = db.init_dir
+        else:
+            self.out["dir"] = _empty(n, (3,), torch.float32, dev)
+        cb = db.c_struct()
+        h = ctypes.c_void_p()
+        o = self.out
+        N.check(ctx._L.ncg_contact_graph_create(ctx.handle, ctypes.byref(cb), ctypes.c_float(prediction),
+                                                _ptr(o["contact"]), _ptr(o["has_contact"]), _ptr(o["dir"]),
+                                                _ptr(o["status"]), _ptr(o["iters"]), ctypes.byref(h)),
+                "ncg_contact_graph_create")
+        self._h = h
+
+    def launch(self, stream=None):
+        N.check(self.ctx._L.ncg_graph_launch(self._h, _stream(stream)), "ncg_graph_launch")
+        return self.out
+
+    def close(self):
+        # a closed context has already destroyed its graphs
+        if self._h and self.ctx._p:
+            self.ctx._L.ncg_graph_destroy(self._h)
+        self._h = None
 
 
 def distance_batch(ctx: Context, db: DeviceBatch, with_iters=False, stream=None):
