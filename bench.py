@@ -180,7 +180,7 @@ def _advance_poses_t(m, gen, sigma_t=0.01, sigma_r=0.02):
     return out
 
 
-def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32):
+def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32, mlp_params=None):
     """Large coherent batch: ConvexHull-ConvexHull pairs over a pool of shared
     hulls, stepped over 8 frames; plain GJK vs previous-frame direction reuse,
     each frame one replay of a captured CUDA graph."""
@@ -200,8 +200,16 @@ def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32):
     ctx = Q.Context(local, tolerance=tolerance, dispatch="support_map")
     dirs = torch.empty((n, 3), dtype=torch.float32, device=db.m1.device)
     g_plain = Q.ContactGraph(ctx, db, 0.0)
+    g_mlp = None
+    strategies = ["plain", "previous_frame_dir"]
+    if mlp_params is not None:
+        ctx.set_mlp_params(mlp_params)
+        ctx.set_warm_start(Nn.WARM_MLP)
+        g_mlp = Q.ContactGraph(ctx, db, 0.0)
+        ctx.set_warm_start(Nn.WARM_NONE)
+        strategies.append("mlp")
     res = {}
-    for strategy in ("plain", "previous_frame_dir"):
+    for strategy in strategies:
         if strategy == "previous_frame_dir":
             ctx.set_warm_start(Nn.WARM_NONE)
         times, iters = [], []
@@ -213,6 +221,16 @@ def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32):
                 ctx.set_warm_start(Nn.WARM_INIT_DIR)
                 g_warm = Q.ContactGraph(ctx, db.with_init_dir(dirs), 0.0, reuse_dir=True)
             g = g_warm if (strategy == "previous_frame_dir" and f >= 1) else g_plain
+            if strategy == "mlp":
+                g = g_mlp
+            if f == frames - 1:  # the start directions of the last frame, for the accuracy check
+                if strategy == "previous_frame_dir":
+                    init_last = dirs[:4096].cpu().numpy()
+                elif strategy == "mlp":
+                    from ncollide_gb300 import warm_mlp as M
+                    init_last = M.infer(db, mlp_params)[:4096].cpu().numpy()
+                else:
+                    init_last = None
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             e0.record()
@@ -229,7 +247,7 @@ def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32):
         ms = sum(times) / len(times)
         res[strategy] = {"pairs_per_s": n / (ms / 1e3), "ms_per_frame": ms,
                          "gjk_iters_per_pair": sum(iters) / len(iters), "frames_timed": len(times),
-                         "_last": last}
+                         "_last": last, "_init": init_last}
         if g_warm is not None:
             g_warm.close()
     ctx.set_warm_start(Nn.WARM_NONE)
@@ -243,28 +261,124 @@ def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32):
     lastb = type(lastb)(lastb.shapes, lastb.hull_points, poses[-1][0][:4096].cpu().numpy(), lastb.g1,
                         poses[-1][1][:4096].cpu().numpy(), lastb.g2, None, lastb.scale, dict(lastb.meta))
     r64 = O.query(lastb, O.CONTACT, O.F64, param=0.0)
+
+    def rel_err(last, ref):
+        m = (last["has_contact"] == 1) & (ref.tag == 1)
+        rel = np.abs(last["contact"][:, 9].astype(np.float64) - ref.value) / np.maximum(np.abs(ref.value),
+                                                                                      lastb.scale)
+        return {"p99": float(np.percentile(rel[m], 99)) if m.any() else None,
+                "max": float(rel[m].max()) if m.any() else None,
+                "frac_gt_1e-5": float((rel[m] > 1e-5).mean()) if m.any() else None}
     both_ok = True
     for strategy, r in res.items():
         last = r.pop("_last")
-        m = (last["has_contact"] == 1) & (r64.tag == 1)
-        rel = np.abs(last["contact"][:, 9].astype(np.float64) - r64.value) / np.maximum(np.abs(r64.value),
-                                                                                      lastb.scale)
-        r["depth_rel_err_vs_f64"] = {"p99": float(np.percentile(rel[m], 99)) if m.any() else None,
-                                     "max": float(rel[m].max()) if m.any() else None}
-        r["classification_mismatch_vs_f64"] = int((last["has_contact"] != r64.tag).sum())
+        init = r.pop("_init")
+        # against the f64 reference started like the plain method, and started
+        # from the same directions (the same algorithm and inputs in f64)
+        r["depth_rel_err_vs_f64_plain_start"] = rel_err(last, r64)
+        r64s = r64 if init is None else O.query(lastb.with_init_dir(init), O.CONTACT, O.F64, param=0.0)
+        r["depth_rel_err_vs_f64_same_start"] = rel_err(last, r64s)
+        r["classification_mismatch_vs_f64"] = int((last["has_contact"] != r64s.tag).sum())
         r["hbm_gbs"] = r["pairs_per_s"] * bytes_pp / 1e9
         r["hbm_frac"] = r["hbm_gbs"] / peak_hbm
         r["fp32_frac"] = r["pairs_per_s"] * flops_pp / 1e12 / peak_fp32
         both_ok &= r["classification_mismatch_vs_f64"] >= 0
     g_plain.close()
+    if g_mlp is not None:
+        g_mlp.close()
     ctx.close()
     out = {"workload": f"coherent_hull_pairs: {n} ConvexHull-ConvexHull pairs, 32-1024 points, pool of 65536 "
                        f"shared hulls, 8 frames (sigma_t 0.01, sigma_r 0.02), seed 5; frames 1-7 timed",
            "strategies": res,
            "speedup_previous_frame_vs_plain": res["previous_frame_dir"]["pairs_per_s"] / res["plain"]["pairs_per_s"],
+           "speedup_mlp_vs_plain": (res["mlp"]["pairs_per_s"] / res["plain"]["pairs_per_s"]) if "mlp" in res else None,
            "bytes_per_pair": bytes_pp, "flops_per_pair": flops_pp,
            "accuracy_sample": "first 4096 pairs of the last frame"}
     return out
+
+
+def learned_warm_start(args, local, tolerance, dispatch, headline_db, headline_batch):
+    """Trains the warm-start network on plain-GJK labels (20 epochs, batch 8192,
+    4,194,304 pairs of the mixed distribution over a pool of shared shapes),
+    evaluates it on 4,194,304 held-out pairs (other seed, other pool) and times
+    the warm-started contact against plain on the headline batch."""
+    import torch
+    from ncollide_gb300 import _native as Nn
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import warm_mlp as M
+    from ncollide_gb300 import workloads as W
+    from oracle import oracle as O
+    dev = f"cuda:{local}"
+    ctx = Q.Context(local, tolerance=tolerance, dispatch="support_map")
+    t0 = time.perf_counter()
+    train_b = W.mixed_convex_pooled(args.mlp_pairs, seed=3, pool=1 << 17)
+    held_b = W.mixed_convex_pooled(args.mlp_pairs, seed=4, pool=1 << 17)
+    gen_s = time.perf_counter() - t0
+    dtr = Q.DeviceBatch.from_host(train_b, device=dev)
+    dhe = Q.DeviceBatch.from_host(held_b, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, Xtr = M.features(dtr)
+    Ytr = M.labels(ctx, dtr)
+    torch.cuda.synchronize()
+    label_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    params, hist = M.train(Xtr, Ytr, epochs=args.mlp_epochs, batch_size=8192, lr=2e-3, seed=0)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    _, Xhe = M.features(dhe)
+    Yhe = M.labels(ctx, dhe)
+    held_loss = M.evaluate(Xhe, Yhe, params)
+    ctx.set_mlp_params(params)
+    ctx.set_dispatch(dispatch)
+
+    def run(db, warm, steps):
+        ctx.set_warm_start(warm)
+        for _ in range(2):
+            Q.contact_batch(ctx, db, 0.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            o = Q.contact_batch(ctx, db, 0.0, with_iters=True)
+        e1.record()
+        torch.cuda.synchronize()
+        it = o["iters"].cpu().numpy().view(np.uint32)
+        g = (it & 0xffff).astype(np.float64)
+        e = (it >> 16).astype(np.float64)
+        return {"pairs_per_s": db.n_pairs * steps / (e0.elapsed_time(e1) / 1e3),
+                "ms_per_step": e0.elapsed_time(e1) / steps,
+                "gjk_iters_mean": float(g.mean()), "gjk_iters_p99": float(np.percentile(g, 99)),
+                "epa_iters_mean": float(e.mean()), "flags": ctx.stats()["flags"]}, o
+
+    held = {"plain": run(dhe, Nn.WARM_NONE, 3)[0], "mlp": run(dhe, Nn.WARM_MLP, 3)[0]}
+    head_plain, op = run(headline_db, Nn.WARM_NONE, args.steps)
+    head_mlp, om = run(headline_db, Nn.WARM_MLP, args.steps)
+    ctx.set_warm_start(Nn.WARM_NONE)
+    # accuracy of both against the f64 oracle on the first 4096 headline pairs
+    k = 4096
+    sub = headline_batch.subset(np.arange(k))
+    q = O.CONTACT_QUERY if dispatch == "query" else O.CONTACT
+    r64 = O.query(sub, q, O.F64, param=0.0)
+    acc = {}
+    for name, o in (("plain", op), ("mlp", om)):
+        has = o["has_contact"][:k].cpu().numpy()
+        c = o["contact"][:k].cpu().numpy().astype(np.float64)
+        m = (has == 1) & (r64.tag == 1)
+        rel = np.abs(c[:, 9] - r64.value) / np.maximum(np.abs(r64.value), sub.scale)
+        acc[name] = {"depth_rel_err_p99": float(np.percentile(rel[m], 99)) if m.any() else None,
+                     "depth_rel_err_max": float(rel[m].max()) if m.any() else None,
+                     "frac_gt_1e-5": float((rel[m] > 1e-5).mean()) if m.any() else None,
+                     "has_contact_mismatch_vs_f64": int((has != r64.tag).sum())}
+    ctx.close()
+    return params, {"train": {"pairs": train_b.n_pairs, "epochs": args.mlp_epochs, "batch": 8192,
+                      "optimizer": "Adam lr 2e-3", "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1],
+                      "seconds_generate_host": gen_s, "seconds_label_gpu": label_s, "seconds_train_gpu": train_s,
+                      "data": "mixed_convex over a pool of 131072 shapes, seed 3 (train) / 4 (held out)"},
+            "held_out": {"pairs": held_b.n_pairs, "loss": held_loss, **held},
+            "headline_batch": {"plain": head_plain, "mlp": head_mlp,
+                               "speedup_mlp_vs_plain": head_mlp["pairs_per_s"] / head_plain["pairs_per_s"],
+                               "accuracy_vs_f64_first_4096": acc}}
 
 
 def cpu_baseline(batch, threads, query):
@@ -324,6 +438,9 @@ def main():
     ap.add_argument("--coherent-pairs", type=int, default=1 << 21,
                     help="pairs of the coherent warm-start workload (16777216 for the full configuration)")
     ap.add_argument("--no-coherent", action="store_true")
+    ap.add_argument("--mlp-pairs", type=int, default=1 << 22)
+    ap.add_argument("--mlp-epochs", type=int, default=20)
+    ap.add_argument("--no-mlp", action="store_true")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profiling: stop after the timed device steps (no second dispatch, no e2e, no report)")
     args = ap.parse_args()
@@ -481,9 +598,12 @@ def main():
         out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
         acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs), qo)
 
+    learned = mlp_params = None
+    if not args.no_mlp:
+        mlp_params, learned = learned_warm_start(args, local, args.tolerance, args.dispatch, db, batch)
     coherent = None
     if not args.no_coherent:
-        coherent = coherent_warm_start(args, local, args.tolerance, hbm_peak, fp32_peak)
+        coherent = coherent_warm_start(args, local, args.tolerance, hbm_peak, fp32_peak, mlp_params)
 
     line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -495,6 +615,7 @@ def main():
                        "l2": "inputs larger than L2 (%.2f GB resident)" % (batch.nbytes_inputs() / 1e9)},
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc, "warm_start_coherent": coherent,
+            "warm_start_learned": learned,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
             "epa": {"pairs": stats["n_epa"], "tier_b_pairs": stats["n_epa_overflow"],

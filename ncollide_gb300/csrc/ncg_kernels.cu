@@ -665,6 +665,7 @@ struct ncg_ctx {
     int profiling = 0;
     std::vector<ncg_graph*> graphs;  // destroyed with the context
     float* mlp_params = nullptr;     // NCG_MLP_N_PARAMS floats (device)
+    bool mlp_ready = false;          // kernel attributes set on this device
     float* desc_buf = nullptr;       // shape descriptors for the network
     size_t desc_cap = 0;
     float* idir_buf = nullptr;       // the network's init_dir per pair
@@ -686,6 +687,31 @@ bool ensure_scratch(ncg_ctx* c, uint64_t n) {
     if (!cuda_ok(cudaMalloc(&c->scratch, bytes), "cudaMalloc(scratch)")) return false;
     c->scratch_cap_pairs = cap;
     return true;
+}
+
+// Buffers of the learned warm start (shape descriptors, one init_dir per pair).
+int ensure_mlp_buffers(ncg_ctx* c, const ncg_batch* b) {
+    if (!c->mlp_params) { g_last_error = "NCG_WARM_MLP without parameters (ncg_ctx_set_mlp_params)"; return NCG_EINVAL; }
+    if (!c->mlp_ready) {
+        if (mlp_prepare() != NCG_OK) return NCG_ECUDA;
+        c->mlp_ready = true;
+    }
+    if (c->desc_cap < b->n_shapes) {
+        if (c->desc_buf) cudaFree(c->desc_buf);
+        c->desc_buf = nullptr;
+        c->desc_cap = 0;
+        const size_t cap = b->n_shapes < 1024 ? 1024 : b->n_shapes;
+        if (!cuda_ok(cudaMalloc(&c->desc_buf, 64 * cap), "cudaMalloc(desc)")) return NCG_ENOMEM;
+        c->desc_cap = cap;
+    }
+    if (c->idir_cap < b->n_pairs) {
+        if (c->idir_buf) cudaFree(c->idir_buf);
+        c->idir_buf = nullptr;
+        c->idir_cap = 0;
+        if (!cuda_ok(cudaMalloc(&c->idir_buf, 12 * (size_t)b->n_pairs), "cudaMalloc(init_dir)")) return NCG_ENOMEM;
+        c->idir_cap = b->n_pairs;
+    }
+    return NCG_OK;
 }
 
 Scratch carve_scratch(ncg_ctx* c) {
@@ -749,23 +775,9 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     if (c->warm == NCG_WARM_MLP && (query == Q_CONTACT || query == Q_PROXIMITY)) {
         // the network's start direction replaces the default one (contact and
         // proximity start from normalize(t2 - t1) in the reference)
-        if (!c->mlp_params) { g_last_error = "NCG_WARM_MLP without parameters (ncg_ctx_set_mlp_params)"; return NCG_EINVAL; }
-        if (c->desc_cap < b->n_shapes) {
-            if (c->desc_buf) cudaFree(c->desc_buf);
-            c->desc_buf = nullptr;
-            c->desc_cap = 0;
-            if (!cuda_ok(cudaMalloc(&c->desc_buf, 64 * (size_t)(b->n_shapes < 1024 ? 1024 : b->n_shapes)), "cudaMalloc(desc)"))
-                return NCG_ENOMEM;
-            c->desc_cap = b->n_shapes < 1024 ? 1024 : b->n_shapes;
-        }
-        if (c->idir_cap < b->n_pairs) {
-            if (c->idir_buf) cudaFree(c->idir_buf);
-            c->idir_buf = nullptr;
-            c->idir_cap = 0;
-            if (!cuda_ok(cudaMalloc(&c->idir_buf, 12 * (size_t)b->n_pairs), "cudaMalloc(init_dir)")) return NCG_ENOMEM;
-            c->idir_cap = b->n_pairs;
-        }
-        int rc = mlp_shape_desc(bb, c->desc_buf, st);
+        int rc = ensure_mlp_buffers(c, b);
+        if (rc != NCG_OK) return rc;
+        rc = mlp_shape_desc(bb, c->desc_buf, st);
         if (rc == NCG_OK) rc = mlp_infer(bb, c->mlp_params, c->desc_buf, c->idir_buf, &s.ctr->mlp_err, c->num_sms, st);
         if (rc != NCG_OK) return rc;
         bb.init_dir = c->idir_buf;
@@ -999,6 +1011,10 @@ int ncg_contact_graph_create(ncg_ctx* c, const ncg_batch* b, float prediction, n
     if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
     // everything that allocates happens before the capture
     if (!ensure_scratch(c, b->n_pairs)) return NCG_ENOMEM;
+    if (c->warm == NCG_WARM_MLP) {
+        int rc0 = ensure_mlp_buffers(c, b);
+        if (rc0 != NCG_OK) return rc0;
+    }
     cudaStream_t cs;
     if (!cuda_ok(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate")) return NCG_ECUDA;
     const int prof = c->profiling;

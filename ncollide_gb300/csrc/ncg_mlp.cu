@@ -607,16 +607,18 @@ int mlp_shape_desc(const ncg_batch& b, float* desc, cudaStream_t st) {
     return mlp::ok(cudaGetLastError(), "k_shape_desc") ? NCG_OK : NCG_ECUDA;
 }
 
+int mlp_prepare() {
+    bool a = mlp::ok(cudaFuncSetAttribute(mlp::k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)mlp::InferSmem::BYTES),
+                     "k_mlp_infer attribute");
+    bool b = mlp::ok(cudaFuncSetAttribute(mlp::k_mlp_train_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)mlp::TrainSmem::BYTES),
+                     "k_mlp_train_tile attribute");
+    return a && b ? NCG_OK : NCG_ECUDA;
+}
+
 int mlp_infer(const ncg_batch& b, const float* params, const float* desc, float* init_dir, uint32_t* err, int num_sms,
               cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        if (!mlp::ok(cudaFuncSetAttribute(mlp::k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)mlp::InferSmem::BYTES),
-                     "k_mlp_infer attribute"))
-            return NCG_ECUDA;
-        attr = true;
-    }
     const uint64_t tiles = (b.n_pairs + mlp::TILE - 1) / mlp::TILE;
     const unsigned grid = (unsigned)(tiles < (uint64_t)num_sms ? tiles : (uint64_t)num_sms);
     if (grid == 0) return NCG_OK;
@@ -648,7 +650,9 @@ int ncg_mlp_infer(const ncg_batch* b, const float* params, float* desc, float* i
     if (!ncg::mlp::ok(cudaGetDevice(&dev), "cudaGetDevice")) return NCG_ECUDA;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaStream_t st = (cudaStream_t)stream;
-    int rc = ncg::mlp_shape_desc(*b, desc, st);
+    int rc = ncg::mlp_prepare();
+    if (rc) return rc;
+    rc = ncg::mlp_shape_desc(*b, desc, st);
     if (rc) return rc;
     return ncg::mlp_infer(*b, params, desc, init_dir, err, sms, st);
 }
@@ -656,14 +660,8 @@ int ncg_mlp_infer(const ncg_batch* b, const float* params, float* desc, float* i
 int ncg_mlp_grad(const float* params, const float* X, const float* labels, uint64_t n, float logit_weight,
                  float* partial, float* grad, uint32_t* err, void* stream) {
     if (!params || !X || !labels || !partial || !grad || !err || n == 0) return NCG_EINVAL;
-    static bool attr = false;
-    if (!attr) {
-        if (!ncg::mlp::ok(cudaFuncSetAttribute(ncg::mlp::k_mlp_train_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)ncg::mlp::TrainSmem::BYTES),
-                          "k_mlp_train_tile attribute"))
-            return NCG_ECUDA;
-        attr = true;
-    }
+    int rc = ncg::mlp_prepare();
+    if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const uint64_t tiles = (n + ncg::mlp::TILE - 1) / ncg::mlp::TILE;
     ncg::mlp::k_mlp_train_tile<<<(unsigned)tiles, 128, ncg::mlp::TrainSmem::BYTES, st>>>(

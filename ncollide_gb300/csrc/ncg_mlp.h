@@ -13,6 +13,10 @@ namespace ncg {
 // Records the message ncg_last_error() returns on this thread.
 void set_last_error(const std::string& msg);
 
+// Sets the network kernels' shared-memory limits on the current device (call
+// outside stream capture).
+int mlp_prepare();
+
 // Per-shape descriptors (16 floats per shape) of the batch's shape table.
 int mlp_shape_desc(const ncg_batch& b, float* desc, cudaStream_t st);
 

@@ -163,6 +163,21 @@ def mixed_convex(n=1 << 20, seed=1, kinds=MIXED_KINDS, hull_n=(8, 1024), thin=Fa
                        {"workload": "mixed_convex", "n": n, "seed": seed, "thin": thin})
 
 
+def mixed_convex_pooled(n=1 << 22, seed=3, pool=1 << 17, kinds=MIXED_KINDS, hull_n=(8, 1024)):
+    """The mixed convex distribution over a pool of `pool` shared shapes: both
+    shapes of a pair are drawn uniformly from the pool (so pair kinds stay
+    uniform), poses as in mixed_convex.  Keeps multi-million-pair training and
+    evaluation sets to a few hundred MB of hull points."""
+    rng = np.random.default_rng(seed)
+    shapes, pts = random_shapes(rng, pool, kinds=kinds, hull_n=hull_n)
+    radii = _circumradius(shapes, pts)
+    g1 = rng.integers(0, pool, n).astype(np.uint32)
+    g2 = rng.integers(0, pool, n).astype(np.uint32)
+    m1, m2 = _poses(rng, n, radii[g1], radii[g2])
+    return PairBatch(shapes, pts, m1, g1, m2, g2, scale=radii[g1] + radii[g2],
+                     meta={"workload": "mixed_convex_pooled", "n": n, "seed": seed, "pool": pool})
+
+
 def coherent_hull_pairs(n=1 << 24, seed=5, pool=1 << 16, hull_n=(32, 1024)):
     """ConvexHull-ConvexHull pairs over a pool of `pool` shared hulls."""
     rng = np.random.default_rng(seed)
