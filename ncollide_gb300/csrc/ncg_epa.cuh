@@ -1,19 +1,19 @@
 // ncg_epa.cuh — warp-cooperative 3-D EPA (src/query/algorithms/epa3.rs:171-454).
 //
 // The algorithm is written once for two execution policies:
-//   ThreadExec  one thread expands one polytope held in its local memory (the
-//               hardware interleaves local memory per lane, so a warp runs 32
-//               independent pairs and thousands of threads hide the latency);
-//               used for pairs of analytic shapes.
+//   ThreadExec  one thread expands one polytope held in its local memory (a
+//               warp runs 32 independent pairs and thousands of threads hide
+//               the latency); used for small polytopes.
 //   WarpExec    one warp expands one polytope held in shared memory (tiers A
 //               and B) or a global-memory slab (tier C); used for ConvexHull
 //               pairs (warp-parallel support scans) and for polytopes that
 //               outgrow a thread's store.
 //
-// Layout (all 16-byte records):
+// Layout (one store is contiguous, so a thread's records share cache sectors):
 //   vertex  float4 (x, y, z, 0); the two support points behind each vertex
-//           (witness data, read only at the end) in a separate 6 x f32 array
-//   face    float4 (normal xyz, p0 | p1 << 16) + uint4 (p2 | gen << 16, adj0, adj1, adj2)
+//           (witness data, read only at the end) in a separate 6 x f32 record
+//   face    float4 (normal xyz, p0 | p1 << 16) then uint4 (p2 | gen << 16,
+//           adj0, adj1, adj2): one 32-byte record
 //   heap    float4 (key hi, key lo, push sequence, face reference)
 // A face reference is slot | gen << 16.  Deleting a face bumps its slot's
 // generation and frees the slot, so every reference taken before the deletion
@@ -60,10 +60,10 @@ NCG_DEV int rslot(uint32_t r) { return (int)(r & 0xffffu); }
 
 struct EpaStore {
     float4* vpt;      // [VC]
-    float* vo;        // [6][VC] orig1 xyz, orig2 xyz
-    float4* fa;       // [FC] normal xyz, pts p0 | p1 << 16
-    uint4* fb;        // [FC] p2 | gen << 16, adj0, adj1, adj2
-    float4* heap;     // [FC] key hi, key lo, seq, ref
+    float* vo;        // [VC][6] orig1 xyz, orig2 xyz
+    float4* face;     // [FC][2] float4 (normal xyz, pts p0 | p1 << 16), uint4 (p2 | gen << 16, adj0..2)
+    float4* heap;     // [FC] key hi, key lo, seq, ref (binary heap, or flat list of live faces)
+    uint16_t* hpos;   // [FC] flat list only: position of a face slot's entry, 0xffff if none
     uint32_t* freel;  // [FC] free slots (stack)
     uint32_t* sref;   // [SC] silhouette face references
     uint32_t* snew;   // [SC] reference of the face built on edge k
@@ -75,22 +75,28 @@ struct EpaStore {
     uint32_t* tref;   // [TC] flood-fill stack: references
     uint8_t* topp;    // [TC] flood-fill stack: opposite vertex
     int VC, FC, SC, TC;
+    bool flat;  // queue of live faces: flat list (small stores) or binary heap with lazy deletion
 
+    // Stores with at most this many face slots keep a flat list of the live
+    // queued faces (deleted faces leave it at once; a pop is an arg-max scan
+    // of independent loads, warp-parallel under WarpExec) instead of the heap.
+    static constexpr int FLAT_MAX = 512;
     static constexpr __host__ __device__ size_t r16(size_t b) { return (b + 15) & ~size_t(15); }
     // Bytes of one store.
     static constexpr __host__ __device__ size_t bytes(int VC, int FC, int SC, int TC) {
-        return r16(16 * (size_t)VC) + r16(16 * (size_t)FC) + r16(16 * (size_t)FC) + r16(16 * (size_t)FC) +
+        return r16(16 * (size_t)VC) + r16(32 * (size_t)FC) + r16(16 * (size_t)FC) + r16(2 * (size_t)FC) +
                r16(4 * (size_t)FC) + 4 * r16(4 * (size_t)SC) + r16(8 * (size_t)SC) + 2 * r16((size_t)SC) +
                r16(4 * (size_t)TC) + r16((size_t)TC) + r16(24 * (size_t)VC);
     }
 
     NCG_DEV void carve(char* base, int vc, int fc, int sc, int tc) {
         VC = vc; FC = fc; SC = sc; TC = tc;
+        flat = fc <= FLAT_MAX;
         char* p = base;
         vpt = (float4*)p; p += r16(16 * (size_t)VC);
-        fa = (float4*)p; p += r16(16 * (size_t)FC);
-        fb = (uint4*)p; p += r16(16 * (size_t)FC);
+        face = (float4*)p; p += r16(32 * (size_t)FC);
         heap = (float4*)p; p += r16(16 * (size_t)FC);
+        hpos = (uint16_t*)p; p += r16(2 * (size_t)FC);
         freel = (uint32_t*)p; p += r16(4 * (size_t)FC);
         sref = (uint32_t*)p; p += r16(4 * (size_t)SC);
         snew = (uint32_t*)p; p += r16(4 * (size_t)SC);
@@ -108,23 +114,28 @@ struct EpaStore {
         float4 v = vpt[i];
         return {v.x, v.y, v.z};
     }
-    NCG_DEV vec3<real> vo1(int i) const { return {real(vo[i]), real(vo[VC + i]), real(vo[2 * VC + i])}; }
-    NCG_DEV vec3<real> vo2(int i) const { return {real(vo[3 * VC + i]), real(vo[4 * VC + i]), real(vo[5 * VC + i])}; }
+    // A face's two 16-byte halves are adjacent (one 32-byte sector).
+    NCG_DEV float4& FA(int f) const { return face[2 * f]; }
+    NCG_DEV uint4& FB(int f) const { return reinterpret_cast<uint4*>(face)[2 * f + 1]; }
+    NCG_DEV vec3<real> vo1(int i) const { return {real(vo[6 * i]), real(vo[6 * i + 1]), real(vo[6 * i + 2])}; }
+    NCG_DEV vec3<real> vo2(int i) const { return {real(vo[6 * i + 3]), real(vo[6 * i + 4]), real(vo[6 * i + 5])}; }
     NCG_DEV void put_vertex(int i, const CSO& c) {
         vpt[i] = make_float4(c.p.x, c.p.y, c.p.z, 0.0f);
-        vo[i] = c.o1.x; vo[VC + i] = c.o1.y; vo[2 * VC + i] = c.o1.z;
-        vo[3 * VC + i] = c.o2.x; vo[4 * VC + i] = c.o2.y; vo[5 * VC + i] = c.o2.z;
+        float* w = vo + 6 * i;
+        w[0] = c.o1.x; w[1] = c.o1.y; w[2] = c.o1.z;
+        w[3] = c.o2.x; w[4] = c.o2.y; w[5] = c.o2.z;
     }
     NCG_DEV CSO get_vertex(int i) const {
-        return CSO{vf(i), {vo[i], vo[VC + i], vo[2 * VC + i]}, {vo[3 * VC + i], vo[4 * VC + i], vo[5 * VC + i]}};
+        const float* w = vo + 6 * i;
+        return CSO{vf(i), {w[0], w[1], w[2]}, {w[3], w[4], w[5]}};
     }
-    NCG_DEV uint32_t gen(int f) const { return fb[f].x >> 16; }
+    NCG_DEV uint32_t gen(int f) const { return FB(f).x >> 16; }
     NCG_DEV bool live(uint32_t ref) const { return gen(rslot(ref)) == (ref >> 16); }
     NCG_DEV void pts(int f, int& a, int& b, int& c) const {
-        uint32_t ab = __float_as_uint(fa[f].w);
+        uint32_t ab = __float_as_uint(FA(f).w);
         a = (int)(ab & 0xffffu);
         b = (int)(ab >> 16);
-        c = (int)(fb[f].x & 0xffffu);
+        c = (int)(FB(f).x & 0xffffu);
     }
     NCG_DEV int pt(int f, int k) const {
         int a, b, c;
@@ -132,23 +143,37 @@ struct EpaStore {
         return k == 0 ? a : (k == 1 ? b : c);
     }
     NCG_DEV uint32_t adj(int f, int k) const {
-        uint4 b = fb[f];
+        uint4 b = FB(f);
         return k == 0 ? b.y : (k == 1 ? b.z : b.w);
     }
     NCG_DEV void set_adj(int f, int k, uint32_t r) {
-        if (k == 0) fb[f].y = r;
-        else if (k == 1) fb[f].z = r;
-        else fb[f].w = r;
+        if (k == 0) FB(f).y = r;
+        else if (k == 1) FB(f).z = r;
+        else FB(f).w = r;
     }
     NCG_DEV vec3<float> normalf(int f) const {
-        float4 a = fa[f];
+        float4 a = FA(f);
         return {a.x, a.y, a.z};
     }
     NCG_DEV vec3<real> normal(int f) const { return to_r(normalf(f)); }
-    // Deletes a face: bumps its slot's generation (all references go stale) and frees the slot.
-    NCG_DEV void kill(int f, int& nfree) {
-        fb[f].x += 1u << 16;
+    // Deletes a face: bumps its slot's generation (all references go stale),
+    // frees the slot and, with a flat list, drops its queue entry.
+    NCG_DEV void kill(int f, int& nfree, int& hsize) {
+        FB(f).x += 1u << 16;
         freel[nfree++] = (uint32_t)f;
+        if (flat) unlist(f, hsize);
+    }
+    // Flat list: removes face slot f's entry (moves the last entry into its place).
+    NCG_DEV void unlist(int f, int& hsize) {
+        const int at = hpos[f];
+        if (at == 0xffff) return;
+        hpos[f] = 0xffff;
+        const int last = --hsize;
+        if (at != last) {
+            const float4 e = heap[last];
+            heap[at] = e;
+            hpos[rslot(__float_as_uint(e.w))] = (uint16_t)at;
+        }
     }
 
     // Face::new (epa3.rs:96-115) + ccw_face_normal (utils/ccw_face_normal.rs:21-27).
@@ -163,8 +188,9 @@ struct EpaStore {
         vec3<float> n;
         float len;
         if (!try_normalize(to_f(cross(to_r(Bf) - A, to_r(Cf) - A)), eps, n, len)) n = zero3<float>();
-        fa[f] = make_float4(n.x, n.y, n.z, __uint_as_float((uint32_t)p0 | ((uint32_t)p1 << 16)));
-        fb[f] = make_uint4((uint32_t)p2 | (g << 16), a0, a1, a2);
+        FA(f) = make_float4(n.x, n.y, n.z, __uint_as_float((uint32_t)p0 | ((uint32_t)p1 << 16)));
+        FB(f) = make_uint4((uint32_t)p2 | (g << 16), a0, a1, a2);
+        hpos[f] = 0xffff;
         dist = dot(to_r(n), A);
         return loc.kind == LOC_FACE;
     }
@@ -241,15 +267,45 @@ struct EpaStore {
         size = j;
         for (int i = size / 2 - 1; i >= 0; --i) sift_down(i, size, heap[i]);
     }
-    // Returns false when the heap is full even after purging.
+    // Returns false when the queue is full of live faces (a heap is purged first).
     NCG_DEV bool push(int& size, uint32_t& seq, uint32_t ref, real key) {
+        float4 e = make_float4(key.h, key.l, __uint_as_float(seq++), __uint_as_float(ref));
+        if (flat) {
+            if (size >= FC) return false;
+            hpos[rslot(ref)] = (uint16_t)size;
+            heap[size++] = e;
+            return true;
+        }
         if (size >= FC) {
             purge(size);
             if (size >= FC) return false;
         }
-        float4 e = make_float4(key.h, key.l, __uint_as_float(seq++), __uint_as_float(ref));
         sift_up(size++, e);
         return true;
+    }
+    // Flat list: position of the first entry in queue order (-1 if empty).
+    // Every lane of a warp (W = 32) or the one thread (W = 1) calls it.
+    template <int W>
+    NCG_DEV int flat_best(int size) const {
+        int bi = -1;
+        float4 be = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int i = (W > 1 ? (int)(threadIdx.x & 31) : 0); i < size; i += W) {
+            const float4 e = heap[i];
+            if (bi < 0 || before(e, be)) { bi = i; be = e; }
+        }
+        if (W > 1) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                float4 oe;
+                oe.x = __shfl_xor_sync(0xffffffffu, be.x, o);
+                oe.y = __shfl_xor_sync(0xffffffffu, be.y, o);
+                oe.z = __shfl_xor_sync(0xffffffffu, be.z, o);
+                oe.w = __shfl_xor_sync(0xffffffffu, be.w, o);
+                if (oi >= 0 && (bi < 0 || before(oe, be))) { bi = oi; be = oe; }
+            }
+        }
+        return bi;
     }
     // Pops the first live entry; false when none is left.
     NCG_DEV bool pop_live(int& size, int& fid, real& key) {
@@ -388,7 +444,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         return res;
     }
     // best face (its points and normal are kept: its slot may be recycled)
-    int bslot = rslot(__float_as_uint(st.heap[0].w));
+    int bslot = rslot(__float_as_uint(st.heap[st.flat ? st.template flat_best<E::W>(hsize) : 0].w));
     int b0, b1, b2;
     st.pts(bslot, b0, b1, b2);
     vec3<float> bn = st.normalf(bslot);
@@ -396,10 +452,19 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
     int niter = 0;
 
     for (;;) {
-        // ---- pop the closest live face (lane 0)
+        // ---- pop the closest live face (heap: lane 0; flat list: arg-max over the lanes)
         int fid = -1;
         real key(0.0f);
-        if (lane == 0) {
+        if (st.flat) {
+            const int at = st.template flat_best<E::W>(hsize);
+            if (at >= 0) {
+                const float4 e = st.heap[at];
+                fid = rslot(__float_as_uint(e.w));
+                key = real(e.x, e.y);
+            }
+            E::sync();
+            if (lane == 0 && fid >= 0) st.unlist(fid, hsize);
+        } else if (lane == 0) {
             if (!st.pop_live(hsize, fid, key)) fid = -1;
         }
         fid = E::bcast(fid);
@@ -443,7 +508,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
             int o0 = st.next_ccw(rslot(a0), f0);
             int o1 = st.next_ccw(rslot(a1), f1);
             int o2 = st.next_ccw(rslot(a2), f2);
-            st.kill(fid, nfree);
+            st.kill(fid, nfree, hsize);
             int top = 0;
             if (st.TC < 3) ovf = 1;
             else {
@@ -467,7 +532,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
                     uint32_t r1 = st.adj(id, k1), r2 = st.adj(id, k2);
                     int q1 = st.next_ccw(rslot(r1), st.pt(id, k1));
                     int q2 = st.next_ccw(rslot(r2), st.pt(id, k2));
-                    st.kill(id, nfree);
+                    st.kill(id, nfree, hsize);
                     if (top + 2 > st.TC) { ovf = 1; break; }
                     st.tref[top] = r2; st.topp[top++] = (uint8_t)q2;
                     st.tref[top] = r1; st.topp[top++] = (uint8_t)q1;
@@ -477,6 +542,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         nsil = E::bcast(nsil);
         ovf = E::bcast(ovf);
         nfree = E::bcast(nfree);
+        hsize = E::bcast(hsize);
         E::sync();
         if (ovf) { res.exit = EPA_OVERFLOW; return res; }
         if (nsil == 0) {

