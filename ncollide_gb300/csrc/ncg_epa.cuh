@@ -62,8 +62,7 @@ struct EpaStore {
     float4* vpt;      // [VC]
     float* vo;        // [VC][6] orig1 xyz, orig2 xyz
     float4* face;     // [FC][2] float4 (normal xyz, pts p0 | p1 << 16), uint4 (p2 | gen << 16, adj0..2)
-    float4* heap;     // [FC] key hi, key lo, seq, ref (binary heap, or flat list of live faces)
-    uint16_t* hpos;   // [FC] flat list only: position of a face slot's entry, 0xffff if none
+    float4* heap;     // [FC] key hi, key lo, seq, ref
     uint32_t* freel;  // [FC] free slots (stack)
     uint32_t* sref;   // [SC] silhouette face references
     uint32_t* snew;   // [SC] reference of the face built on edge k
@@ -75,28 +74,21 @@ struct EpaStore {
     uint32_t* tref;   // [TC] flood-fill stack: references
     uint8_t* topp;    // [TC] flood-fill stack: opposite vertex
     int VC, FC, SC, TC;
-    bool flat;  // queue of live faces: flat list (small stores) or binary heap with lazy deletion
 
-    // Stores with at most this many face slots keep a flat list of the live
-    // queued faces (deleted faces leave it at once; a pop is an arg-max scan
-    // of independent loads, warp-parallel under WarpExec) instead of the heap.
-    static constexpr int FLAT_MAX = 512;
     static constexpr __host__ __device__ size_t r16(size_t b) { return (b + 15) & ~size_t(15); }
     // Bytes of one store.
     static constexpr __host__ __device__ size_t bytes(int VC, int FC, int SC, int TC) {
-        return r16(16 * (size_t)VC) + r16(32 * (size_t)FC) + r16(16 * (size_t)FC) + r16(2 * (size_t)FC) +
+        return r16(16 * (size_t)VC) + r16(32 * (size_t)FC) + r16(16 * (size_t)FC) +
                r16(4 * (size_t)FC) + 4 * r16(4 * (size_t)SC) + r16(8 * (size_t)SC) + 2 * r16((size_t)SC) +
                r16(4 * (size_t)TC) + r16((size_t)TC) + r16(24 * (size_t)VC);
     }
 
     NCG_DEV void carve(char* base, int vc, int fc, int sc, int tc) {
         VC = vc; FC = fc; SC = sc; TC = tc;
-        flat = fc <= FLAT_MAX;
         char* p = base;
         vpt = (float4*)p; p += r16(16 * (size_t)VC);
         face = (float4*)p; p += r16(32 * (size_t)FC);
         heap = (float4*)p; p += r16(16 * (size_t)FC);
-        hpos = (uint16_t*)p; p += r16(2 * (size_t)FC);
         freel = (uint32_t*)p; p += r16(4 * (size_t)FC);
         sref = (uint32_t*)p; p += r16(4 * (size_t)SC);
         snew = (uint32_t*)p; p += r16(4 * (size_t)SC);
@@ -156,24 +148,10 @@ struct EpaStore {
         return {a.x, a.y, a.z};
     }
     NCG_DEV vec3<real> normal(int f) const { return to_r(normalf(f)); }
-    // Deletes a face: bumps its slot's generation (all references go stale),
-    // frees the slot and, with a flat list, drops its queue entry.
-    NCG_DEV void kill(int f, int& nfree, int& hsize) {
+    // Deletes a face: bumps its slot's generation (all references go stale) and frees the slot.
+    NCG_DEV void kill(int f, int& nfree) {
         FB(f).x += 1u << 16;
         freel[nfree++] = (uint32_t)f;
-        if (flat) unlist(f, hsize);
-    }
-    // Flat list: removes face slot f's entry (moves the last entry into its place).
-    NCG_DEV void unlist(int f, int& hsize) {
-        const int at = hpos[f];
-        if (at == 0xffff) return;
-        hpos[f] = 0xffff;
-        const int last = --hsize;
-        if (at != last) {
-            const float4 e = heap[last];
-            heap[at] = e;
-            hpos[rslot(__float_as_uint(e.w))] = (uint16_t)at;
-        }
     }
 
     // Face::new (epa3.rs:96-115) + ccw_face_normal (utils/ccw_face_normal.rs:21-27).
@@ -190,7 +168,6 @@ struct EpaStore {
         if (!try_normalize(to_f(cross(to_r(Bf) - A, to_r(Cf) - A)), eps, n, len)) n = zero3<float>();
         FA(f) = make_float4(n.x, n.y, n.z, __uint_as_float((uint32_t)p0 | ((uint32_t)p1 << 16)));
         FB(f) = make_uint4((uint32_t)p2 | (g << 16), a0, a1, a2);
-        hpos[f] = 0xffff;
         dist = dot(to_r(n), A);
         return loc.kind == LOC_FACE;
     }
@@ -267,45 +244,15 @@ struct EpaStore {
         size = j;
         for (int i = size / 2 - 1; i >= 0; --i) sift_down(i, size, heap[i]);
     }
-    // Returns false when the queue is full of live faces (a heap is purged first).
+    // Returns false when the heap is full even after purging.
     NCG_DEV bool push(int& size, uint32_t& seq, uint32_t ref, real key) {
-        float4 e = make_float4(key.h, key.l, __uint_as_float(seq++), __uint_as_float(ref));
-        if (flat) {
-            if (size >= FC) return false;
-            hpos[rslot(ref)] = (uint16_t)size;
-            heap[size++] = e;
-            return true;
-        }
         if (size >= FC) {
             purge(size);
             if (size >= FC) return false;
         }
+        float4 e = make_float4(key.h, key.l, __uint_as_float(seq++), __uint_as_float(ref));
         sift_up(size++, e);
         return true;
-    }
-    // Flat list: position of the first entry in queue order (-1 if empty).
-    // Every lane of a warp (W = 32) or the one thread (W = 1) calls it.
-    template <int W>
-    NCG_DEV int flat_best(int size) const {
-        int bi = -1;
-        float4 be = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        for (int i = (W > 1 ? (int)(threadIdx.x & 31) : 0); i < size; i += W) {
-            const float4 e = heap[i];
-            if (bi < 0 || before(e, be)) { bi = i; be = e; }
-        }
-        if (W > 1) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                float4 oe;
-                oe.x = __shfl_xor_sync(0xffffffffu, be.x, o);
-                oe.y = __shfl_xor_sync(0xffffffffu, be.y, o);
-                oe.z = __shfl_xor_sync(0xffffffffu, be.z, o);
-                oe.w = __shfl_xor_sync(0xffffffffu, be.w, o);
-                if (oi >= 0 && (bi < 0 || before(oe, be))) { bi = oi; be = oe; }
-            }
-        }
-        return bi;
     }
     // Pops the first live entry; false when none is left.
     NCG_DEV bool pop_live(int& size, int& fid, real& key) {
@@ -444,7 +391,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         return res;
     }
     // best face (its points and normal are kept: its slot may be recycled)
-    int bslot = rslot(__float_as_uint(st.heap[st.flat ? st.template flat_best<E::W>(hsize) : 0].w));
+    int bslot = rslot(__float_as_uint(st.heap[0].w));
     int b0, b1, b2;
     st.pts(bslot, b0, b1, b2);
     vec3<float> bn = st.normalf(bslot);
@@ -452,19 +399,10 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
     int niter = 0;
 
     for (;;) {
-        // ---- pop the closest live face (heap: lane 0; flat list: arg-max over the lanes)
+        // ---- pop the closest live face (lane 0)
         int fid = -1;
         real key(0.0f);
-        if (st.flat) {
-            const int at = st.template flat_best<E::W>(hsize);
-            if (at >= 0) {
-                const float4 e = st.heap[at];
-                fid = rslot(__float_as_uint(e.w));
-                key = real(e.x, e.y);
-            }
-            E::sync();
-            if (lane == 0 && fid >= 0) st.unlist(fid, hsize);
-        } else if (lane == 0) {
+        if (lane == 0) {
             if (!st.pop_live(hsize, fid, key)) fid = -1;
         }
         fid = E::bcast(fid);
@@ -508,7 +446,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
             int o0 = st.next_ccw(rslot(a0), f0);
             int o1 = st.next_ccw(rslot(a1), f1);
             int o2 = st.next_ccw(rslot(a2), f2);
-            st.kill(fid, nfree, hsize);
+            st.kill(fid, nfree);
             int top = 0;
             if (st.TC < 3) ovf = 1;
             else {
@@ -532,7 +470,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
                     uint32_t r1 = st.adj(id, k1), r2 = st.adj(id, k2);
                     int q1 = st.next_ccw(rslot(r1), st.pt(id, k1));
                     int q2 = st.next_ccw(rslot(r2), st.pt(id, k2));
-                    st.kill(id, nfree, hsize);
+                    st.kill(id, nfree);
                     if (top + 2 > st.TC) { ovf = 1; break; }
                     st.tref[top] = r2; st.topp[top++] = (uint8_t)q2;
                     st.tref[top] = r1; st.topp[top++] = (uint8_t)q1;
@@ -542,7 +480,6 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         nsil = E::bcast(nsil);
         ovf = E::bcast(ovf);
         nfree = E::bcast(nfree);
-        hsize = E::bcast(hsize);
         E::sync();
         if (ovf) { res.exit = EPA_OVERFLOW; return res; }
         if (nsil == 0) {
