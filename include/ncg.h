@@ -284,9 +284,9 @@ int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
  * start-up, and host runtimes (game engines, FFI hosts) that own every device
  * allocation themselves.  This entry point needs no ncg_ctx and never calls
  * cudaMalloc, cudaFree or any allocating routine: its scratch (pair lists, EPA
- * work items and one global-memory EPA slab) is a fixed array of 7.1 MiB
- * (7,433,728 bytes) compiled into the library, which every GPU that loads the
- * library holds until the process exits.
+ * work items, 32 tier-B and one tier-C global-memory EPA slab) is a fixed
+ * array of NCG_NOALLOC_SCRATCH_BYTES (13.8 MiB) compiled into the library,
+ * which every GPU that loads the library holds until the process exits.
  * Limit: at most NCG_NOALLOC_MAX_PAIRS pairs per call; a larger batch returns
  * NCG_EINVAL with a message in ncg_last_error().
  * The first call on a device performs a one-time set-up with that device
@@ -300,6 +300,7 @@ int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
  * first GJK direction of every pair.  Results equal ncg_contact_batch's.
  * This entry point has no counterpart in the reference. */
 #define NCG_NOALLOC_MAX_PAIRS 32768
+#define NCG_NOALLOC_SCRATCH_BYTES 14454528
 int ncg_contact_batch_noalloc(const ncg_batch* batch, float prediction, int tolerance,
                               ncg_contact* out, uint8_t* has_contact, float* out_dir,
                               uint32_t* status, void* stream);

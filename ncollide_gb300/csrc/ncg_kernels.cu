@@ -1228,6 +1228,7 @@ constexpr size_t NA_BYTES = CTR_SLOT + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_TIER
 }  // namespace
 
 // Host code must not use this name as an address: it is only a host-side stand-in.
+static_assert(NA_BYTES == NCG_NOALLOC_SCRATCH_BYTES, "ncg.h states the no-allocation scratch size");
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
 namespace {
