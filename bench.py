@@ -381,6 +381,129 @@ def learned_warm_start(args, local, tolerance, dispatch, headline_db, headline_b
                                "accuracy_vs_f64_first_4096": acc}}
 
 
+def near_touching(batch, seed=2, newton=3):
+    """Places every pair at a signed gap +-g, g log-uniform in [1e-7, 1e-1] (sign
+    50/50), by Newton steps on the f64 oracle's signed distance along the
+    centre line (the contact query with prediction 1: -depth, normal A->B).
+    Returns the batch with the moved second poses and the target gaps."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed + 1000)
+    n = batch.n_pairs
+    target = np.exp(rng.uniform(np.log(1e-7), np.log(1e-1), n)) * np.where(rng.random(n) < 0.5, -1.0, 1.0)
+    c1 = batch.m1[:, 4:7].astype(np.float64)
+    d = batch.m2[:, 4:7].astype(np.float64) - c1
+    t = np.linalg.norm(d, axis=1)
+    u = d / np.maximum(t, 1e-30)[:, None]
+    b = batch
+    for _ in range(newton):
+        r = O.query(b, O.CONTACT, O.F64, param=1.0)
+        ok = r.tag == 1
+        s_now = np.where(ok, -r.value, 1.0)
+        slope = np.maximum((r.dir * u).sum(1), 0.05)
+        t = np.maximum(t + np.where(ok, (target - s_now) / slope, -0.5 * t), 0.0)
+        m2 = b.m2.copy()
+        m2[:, 4:7] = (c1 + t[:, None] * u).astype(np.float32)
+        b = type(b)(b.shapes, b.hull_points, b.m1, b.g1, m2, b.g2, None, b.scale, dict(b.meta))
+    return b, target
+
+
+def precision_stress(args, local, tolerance):
+    """Thin shapes (one axis scaled by logU[1e-3, 1]) placed near touching; the
+    GPU's contact and distance against the f64 oracle on the same f32 inputs,
+    and the intersect classification against the f32 reference path outside
+    a +-1e-6 band around touching."""
+    import torch
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import workloads as W
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    base = W.mixed_convex(args.stress_pairs, seed=2, thin=True)
+    b, target = near_touching(base)
+    prep_s = time.perf_counter() - t0
+    db = Q.DeviceBatch.from_host(b, device=f"cuda:{local}")
+    ctx = Q.Context(local, tolerance=tolerance, dispatch="support_map")
+    oc = Q.contact_batch(ctx, db, 0.0)
+    od = Q.distance_batch(ctx, db)
+    torch.cuda.synchronize()
+    has = oc["has_contact"].cpu().numpy()
+    c = oc["contact"].cpu().numpy().astype(np.float64)
+    dist = od["distance"].cpu().numpy().astype(np.float64)
+    ctx.close()
+    r64c = O.query(b, O.CONTACT, O.F64, param=0.0)
+    r64d = O.query(b, O.DISTANCE, O.F64)
+    r32c = O.query(b, O.CONTACT, O.F32, param=0.0)
+    scale = b.scale
+    k1, k2 = b.kinds()
+    ballball = (k1 == 0) & (k2 == 0)
+    gap = np.where(r64c.tag == 1, -r64c.value, r64d.value)  # true signed gap of the f32 inputs
+    band = np.abs(gap) <= 1e-6
+
+    def dist_stats(x, m):
+        if not m.any():
+            return None
+        return {"n": int(m.sum()), "p50": float(np.percentile(x[m], 50)), "p99": float(np.percentile(x[m], 99)),
+                "max": float(x[m].max()), "frac_gt_1e-5": float((x[m] > 1e-5).mean())}
+    sep = (r64d.value > 0) & ~ballball
+    d_err = np.abs(dist - r64d.value) / scale
+    pen = (has == 1) & (r64c.tag == 1) & (r64c.value > 0) & ~ballball
+    dep_err = np.abs(c[:, 9] - r64c.value) / scale
+    cosang = np.clip((c[:, 6:9] * r64c.dir).sum(1), -1.0, 1.0)
+    ang = np.arccos(cosang)
+    wit = np.maximum(np.linalg.norm(c[:, 0:3] - r64c.p1, axis=1), np.linalg.norm(c[:, 3:6] - r64c.p2, axis=1)) / scale
+    gpu_int = has == 1
+    ref_int = r32c.tag == 1
+    curved = np.isin(k1, [0, 2, 3]) | np.isin(k2, [0, 2, 3])
+    return {"workload": f"{b.n_pairs} mixed pairs (seed 2), thin shapes (one axis x logU[1e-3,1]), signed gap "
+                        "+-logU[1e-7,1e-1] set by 3 Newton steps of the f64 oracle; errors relative to rA+rB",
+            "seconds_prepare_host": prep_s,
+            "achieved_gap_minus_target_p50": float(np.percentile(np.abs(gap - target), 50)),
+            "distance_error": {"all": dist_stats(d_err, sep), "polytope": dist_stats(d_err, sep & ~curved),
+                               "curved": dist_stats(d_err, sep & curved)},
+            "depth_error": {"all": dist_stats(dep_err, pen), "polytope": dist_stats(dep_err, pen & ~curved),
+                            "curved": dist_stats(dep_err, pen & curved)},
+            "normal_angle_rad": {"polytope": dist_stats(ang, pen & ~curved), "curved": dist_stats(ang, pen & curved)},
+            "witness_error": {"polytope": dist_stats(wit, pen & ~curved), "curved": dist_stats(wit, pen & curved)},
+            "classification_mismatch_vs_f32_reference_outside_band": {
+                "pairs_outside_band": int((~band).sum()),
+                "mismatches": int(((gpu_int != ref_int) & ~band).sum()),
+                "rate": float(((gpu_int != ref_int) & ~band).sum() / max(1, (~band).sum()))},
+            "classification_mismatch_vs_f64_outside_band": int(((gpu_int != (r64c.tag == 1)) & ~band).sum()),
+            "ball_ball_pairs_excluded": int(ballball.sum())}
+
+
+def cuboid_small(args, local, tolerance):
+    """65,536 Cuboid-Cuboid pairs, query::contact with prediction 0: GPU
+    throughput, the CPU reference path on the same pairs, and agreement."""
+    import torch
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import workloads as W
+    from oracle import oracle as O
+    b = W.cuboid_pairs(65536, seed=0)
+    db = Q.DeviceBatch.from_host(b, device=f"cuda:{local}")
+    ctx = Q.Context(local, tolerance=tolerance, dispatch="query")
+    for _ in range(3):
+        Q.contact_batch(ctx, db, 0.0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(20):
+        o = Q.contact_batch(ctx, db, 0.0)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 20
+    has = o["has_contact"].cpu().numpy()
+    ctx.close()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    r32 = O.query(b, O.CONTACT, O.F32, param=0.0, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    r64 = O.query(b, O.CONTACT, O.F64, param=0.0)
+    return {"workload": "65536 Cuboid-Cuboid pairs, seed 0, contact prediction 0", "pairs_per_s": 65536 / (ms / 1e3),
+            "ms_per_step": ms, "cpu_reference_path_pairs_per_s": 65536 / cpu_s, "cpu_cores": threads,
+            "has_contact_mismatch_vs_f32_reference": int((has != r32.tag).sum()),
+            "has_contact_mismatch_vs_f64": int((has != r64.tag).sum())}
+
+
 def cpu_baseline(batch, threads, query):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -441,6 +564,8 @@ def main():
     ap.add_argument("--mlp-pairs", type=int, default=1 << 22)
     ap.add_argument("--mlp-epochs", type=int, default=20)
     ap.add_argument("--no-mlp", action="store_true")
+    ap.add_argument("--stress-pairs", type=int, default=1 << 20)
+    ap.add_argument("--no-extras", action="store_true", help="skip the precision-stress and cuboid reports")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profiling: stop after the timed device steps (no second dispatch, no e2e, no report)")
     args = ap.parse_args()
@@ -598,6 +723,10 @@ def main():
         out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
         acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs), qo)
 
+    stress = cuboids = None
+    if not args.no_extras:
+        stress = precision_stress(args, local, args.tolerance)
+        cuboids = cuboid_small(args, local, args.tolerance)
     learned = mlp_params = None
     if not args.no_mlp:
         mlp_params, learned = learned_warm_start(args, local, args.tolerance, args.dispatch, db, batch)
@@ -616,6 +745,7 @@ def main():
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc, "warm_start_coherent": coherent,
             "warm_start_learned": learned,
+            "precision_stress": stress, "cuboid_pairs_65536": cuboids,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
             "epa": {"pairs": stats["n_epa"], "tier_b_pairs": stats["n_epa_overflow"],

@@ -102,6 +102,9 @@ enum ncg_closest_points { NCG_CP_INTERSECTING = 0, NCG_CP_WITHIN_MARGIN = 1, NCG
 #define NCG_STATUS_BAD_INPUT     (1u << 6) /* shape index out of range, bad hull slice */
 #define NCG_STATUS_UNSUPPORTED_FEATURE (1u << 7) /* query dispatch: ball centre on a ConvexHull's
                                                     surface needs the hull's face topology */
+#define NCG_STATUS_EPA_PRECISION_LIMIT (1u << 8) /* NCG_TOL_PRECISE: EPA's expansion would have
+                                                    returned None (f32 noise on sliver faces); the
+                                                    contact is the best face found so far */
 
 /* Return codes. */
 #define NCG_OK          0

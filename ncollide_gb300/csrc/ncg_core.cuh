@@ -242,6 +242,7 @@ struct Tol {
     dw_host add_tol;                // VoronoiSimplex::add_point's degeneracy threshold
     float eps_tol_f, affine_eps_f;  // the same thresholds for the f32 EPA visibility test
     float init_eps;                 // f32::EPSILON: Unit::try_new on the initial direction
+    int best_on_failure;            // PRECISE: a failed EPA expansion answers with the best face so far
 };
 
 // ------------------------------------------------------------------ projections

@@ -53,7 +53,9 @@ enum EpaExit : int {
     EPA_OK_HEAP_EMPTY = 4,
     EPA_NONE = 5,        // EPA returned None
     EPA_OVERFLOW = 6,    // store capacity exceeded (result not valid)
+    EPA_OK_PRECISION = 7,  // PRECISE set: a failed expansion step answered with the best face
 };
+NCG_DEV bool epa_ok(int e) { return (e >= EPA_OK_DIM0 && e <= EPA_OK_HEAP_EMPTY) || e == EPA_OK_PRECISION; }
 
 NCG_DEV uint32_t mkref(int slot, uint32_t gen) { return (uint32_t)slot | (gen << 16); }
 NCG_DEV int rslot(uint32_t r) { return (int)(r & 0xffffu); }
@@ -483,6 +485,13 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         E::sync();
         if (ovf) { res.exit = EPA_OVERFLOW; return res; }
         if (nsil == 0) {
+            if (tol.best_on_failure) {
+                st.face_points(b0, b1, b2, res.p1, res.p2);
+                res.n = to_r(bn);
+                res.exit = EPA_OK_PRECISION;
+                res.status |= NCG_STATUS_EPA_PRECISION_LIMIT;
+                return res;
+            }
             res.status |= NCG_STATUS_EPA_FAILED;
             return res;
         }
@@ -520,6 +529,13 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         E::sync();
         if (ovf) { res.exit = EPA_OVERFLOW; return res; }
         if (built == 0) {  // epa3.rs:409-413
+            if (tol.best_on_failure) {
+                st.face_points(b0, b1, b2, res.p1, res.p2);
+                res.n = to_r(bn);
+                res.exit = EPA_OK_PRECISION;
+                res.status |= NCG_STATUS_EPA_PRECISION_LIMIT;
+                return res;
+            }
             res.status |= NCG_STATUS_EPA_FAILED;
             return res;
         }
@@ -564,6 +580,13 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
             return res;
         }
         if (outcome == 2) {
+            if (tol.best_on_failure) {
+                st.face_points(b0, b1, b2, res.p1, res.p2);
+                res.n = to_r(bn);
+                res.exit = EPA_OK_PRECISION;
+                res.status |= NCG_STATUS_EPA_PRECISION_LIMIT;
+                return res;
+            }
             res.status |= NCG_STATUS_EPA_FAILED;
             return res;
         }

@@ -450,7 +450,7 @@ NCG_DEV void write_epa(const Outputs& o, const EpaItem& it, const EpaResult& r, 
     memset(&c, 0, sizeof(c));
     uint8_t tag = 0;
     vec3<real> dir = mk(real(1.0f), real(0.0f), real(0.0f));
-    if (r.exit >= EPA_OK_DIM0 && r.exit <= EPA_OK_HEAP_EMPTY) {
+    if (epa_ok(r.exit)) {
         tag = 1;
         wr3(c.world1, r.p1);
         wr3(c.world2, r.p2);
@@ -496,7 +496,7 @@ NCG_DEV void finish_epa(const ncg_batch& b, const QueryParams& qp, const Outputs
     PairGeom g = load_geom(b, it.pair);
     const Pose& pb = it.flip ? g.m2 : g.m1;
     const Shape& sb = it.flip ? g.g2 : g.g1;
-    const bool ok = r.exit >= EPA_OK_DIM0 && r.exit <= EPA_OK_HEAP_EMPTY;
+    const bool ok = epa_ok(r.exit);
     vec3<real> w2 = ok ? r.p1 + to_r(pb.t) : to_r(pb.t);
     QContact q = ball_polyhedron_assemble(pb.t, sb.p0, true, w2, F_UNKNOWN, 0, false, from_host(qp.param), it.flip != 0);
     write_qcontact(o, it.pair, q, it.status | r.status | extra_status, pack_iters(it.gjk_iters, r.iters));
@@ -640,6 +640,7 @@ Tol make_tol(int mode) {
         t.add_tol = dw_split(10.0 * (double)DBL_EPSILON);
         t.epa_eps_tol = dw_split(1e-6);
     }
+    t.best_on_failure = mode == NCG_TOL_PRECISE ? 1 : 0;
     t.eps_tol_f = t.eps_tol.h;
     t.affine_eps_f = t.affine_eps.h;
     t.init_eps = FLT_EPSILON;

@@ -124,6 +124,7 @@ enum EpaExit : uint32_t {
     EXIT_NUMERIC = 3,       // :397-402 (new face closer than the popped one)
     EXIT_HEAP_EMPTY = 4,    // :427-429
     EXIT_FAILED = 5,        // None: :278-293, :369-372, :404, :409-413, :421-424
+    EXIT_PRECISION = 7,     // PRECISE set: a None of the expansion loop, answered with the best face
 };
 
 enum StatusBits : uint32_t {
@@ -135,6 +136,7 @@ enum StatusBits : uint32_t {
     ST_DEGENERATE = 1u << 5,
     ST_BAD_INPUT = 1u << 6,
     ST_UNSUPPORTED_FEATURE = 1u << 7,
+    ST_EPA_PRECISION_LIMIT = 1u << 8,
 };
 
 // src/utils/point_cloud_support_point.rs:6-33 — first maximum wins.
@@ -225,6 +227,10 @@ inline CSOPoint<N> cso_from_shapes(const Iso<N>& m1, const Shape<N>& g1, const I
 template <class S> struct Tol {
     S eps, eps_tol, eps_rel, epa_eps_tol, affine_eps;
     S add_tol;  // VoronoiSimplex::add_point's degeneracy threshold (gjk::eps_tol in the reference)
+    // PRECISE set only: when the expansion loop would return None (a new face
+    // with the origin more than eps_tol outside it, or no new face), EPA
+    // answers with the best face found so far instead.
+    bool best_on_failure = false;
     Tol() {}
     // In S arithmetic, as the reference computes them for N = S.
     // epa_tol > 0 replaces EPA's termination threshold (100 eps) only.
@@ -262,12 +268,14 @@ template <class S> inline Tol<S> make_tol_precise(double epa_tol) {
     Tol<S> t = make_tol<S>((double)FLT_EPSILON, epa_tol);
     t.eps_rel = S(std::sqrt(10.0 * (double)DBL_EPSILON));
     t.add_tol = S(10.0 * (double)DBL_EPSILON);
+    t.best_on_failure = true;
     return t;
 }
 template <> inline Tol<dw> make_tol_precise<dw>(double epa_tol) {
     Tol<dw> t = make_tol<dw>((double)FLT_EPSILON, epa_tol);
     t.eps_rel = dw::from_double(std::sqrt(10.0 * (double)DBL_EPSILON));
     t.add_tol = dw::from_double(10.0 * (double)DBL_EPSILON);
+    t.best_on_failure = true;
     return t;
 }
 
@@ -1016,6 +1024,7 @@ template <class N, class S> struct EPA {
 
             size_t first_new_face_id = faces.size();
             if (silhouette.empty()) {
+                if (t.best_on_failure) return best_face(best_face_id, out_p1, out_p2, out_n, cnt);
                 if (cnt) cnt->status |= ST_EPA_FAILED;
                 track(cnt);
                 return false;
@@ -1041,6 +1050,7 @@ template <class N, class S> struct EPA {
                             return true;
                         }
                         if (-dist > t.eps_tol) {
+                            if (t.best_on_failure) return best_face(best_face_id, out_p1, out_p2, out_n, cnt);
                             if (cnt) cnt->status |= ST_EPA_FAILED;
                             track(cnt);
                             return false;
@@ -1050,6 +1060,7 @@ template <class N, class S> struct EPA {
                 }
             }
             if (first_new_face_id == faces.size()) {
+                if (t.best_on_failure) return best_face(best_face_id, out_p1, out_p2, out_n, cnt);
                 if (cnt) cnt->status |= ST_EPA_FAILED;
                 track(cnt);
                 return false;
@@ -1068,6 +1079,18 @@ template <class N, class S> struct EPA {
         face_closest_points(bf, out_p1, out_p2);
         *out_n = cvt<S>(bf.normal);
         if (cnt) cnt->epa_exit = EXIT_HEAP_EMPTY;
+        track(cnt);
+        return true;
+    }
+    // The PRECISE set's answer to a failed expansion step.
+    bool best_face(const FaceId<S>& best, V3<S>* out_p1, V3<S>* out_p2, V3<S>* out_n, Counters* cnt) {
+        const Face<N>& bf = faces[best.id];
+        face_closest_points(bf, out_p1, out_p2);
+        *out_n = cvt<S>(bf.normal);
+        if (cnt) {
+            cnt->status |= ST_EPA_PRECISION_LIMIT;
+            cnt->epa_exit = EXIT_PRECISION;
+        }
         track(cnt);
         return true;
     }

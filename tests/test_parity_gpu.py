@@ -146,6 +146,16 @@ def test_thin_shapes_bit_exact(ctx_factory):
     check_query(ctx, W.mixed_convex(4096, seed=13, thin=True), O.CONTACT, 0.0, N.TOL_REFERENCE)
 
 
+@pytest.mark.parametrize("tol", TOLS)
+def test_near_touching_thin_pairs_bit_exact(ctx_factory, tol):
+    """The precision-stress inputs: thin shapes at signed gaps down to 1e-7."""
+    import bench
+    b, _ = bench.near_touching(W.mixed_convex(4096, seed=60, thin=True))
+    ctx = ctx_factory(tolerance=tol)
+    for q, p in ((O.CONTACT, 0.0), (O.DISTANCE, 0.0), (O.PROXIMITY, 1e-6), (O.CONTACT_QUERY, 0.0)):
+        check_query(ctx, b, q, p, tol)
+
+
 def test_cylinders_bit_exact(ctx_factory):
     ctx = ctx_factory(tolerance=N.TOL_REFERENCE)
     b = W.mixed_convex(4096, seed=14, kinds=(S.CYLINDER, S.CUBOID, S.CONVEX_HULL, S.BALL))
