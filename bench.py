@@ -702,8 +702,8 @@ def main():
                  epa_tol=1e-6 if args.tolerance == "precise" else 0.0)
     bytes_pp, in_pp, out_pp, flops_pp = algorithmic(batch, rs.counters)
     units = {"classify": batch.n_pairs, "gjk_thread": stats.get("n_pairs", 0), "gjk_warp": stats.get("n_pairs", 0),
-             "epa_thread": stats["n_epa"], "epa_tier_a": stats["n_epa"], "epa_tier_b": stats["n_epa_overflow"],
-             "epa_tier_c": stats["n_epa_overflow"]}.get(dom, batch.n_pairs)
+             "epa_thread": stats["n_epa"], "epa_warp": stats["n_epa_overflow"],
+             "epa_wide": stats["n_epa_overflow"]}.get(dom, batch.n_pairs)
     dom_s = mean_stage[dom] / 1e3
     achieved = units * bytes_pp / dom_s / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -748,7 +748,7 @@ def main():
             "precision_stress": stress, "cuboid_pairs_65536": cuboids,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
-            "epa": {"pairs": stats["n_epa"], "tier_b_pairs": stats["n_epa_overflow"],
+            "epa": {"pairs": stats["n_epa"], "warp_stage_pairs": stats["n_epa_overflow"],
                     "gjk_iters_per_pair": stats["gjk_iters"] / batch.n_pairs,
                     "epa_iters_per_epa_pair": stats["epa_iters"] / max(1, stats["n_epa"])}}
     print(json.dumps(line), flush=True)

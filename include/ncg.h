@@ -142,7 +142,7 @@ typedef struct ncg_ctx ncg_ctx;
 typedef struct ncg_stats {
     uint64_t n_pairs;
     uint64_t n_epa;          /* pairs that went through EPA                   */
-    uint64_t n_epa_overflow; /* pairs re-run with the global-memory polytope  */
+    uint64_t n_epa_overflow; /* pairs that outgrew the thread stage (warp EPA) */
     uint64_t gjk_iters;      /* sum over pairs                                */
     uint64_t epa_iters;      /* sum over pairs                                */
     uint32_t kernels_launched;
@@ -167,14 +167,12 @@ int ncg_ctx_set_dispatch(ncg_ctx* ctx, int dispatch);
  *   NCG_TUNE_L1_CARVEOUT     shared-memory carveout (percent) preferred by the
  *                            kernels that use no shared memory; -1 = driver
  *                            default, 0 = largest L1 (default)
- *   NCG_TUNE_TIER_B_WARPS    warps per SM of EPA tier B, 1..8 (default 8)
  * Results do not depend on any of these. */
 enum ncg_tune {
     NCG_TUNE_HULL_GJK_WARP = 0,
     NCG_TUNE_GJK_BLOCKS = 1,
     NCG_TUNE_EPA_BLOCKS = 2,
-    NCG_TUNE_L1_CARVEOUT = 3,
-    NCG_TUNE_TIER_B_WARPS = 4
+    NCG_TUNE_L1_CARVEOUT = 3
 };
 int ncg_ctx_set_tuning(ncg_ctx* ctx, int key, int value);
 int ncg_sync(ncg_ctx* ctx, void* stream);
@@ -183,10 +181,10 @@ int ncg_get_stats(ncg_ctx* ctx, ncg_stats* out);
 /* Stage timing: when enabled, each batch call records CUDA events between its
  * kernel launches on the caller's stream.  ncg_get_stage_ms fills up to
  * n_max durations in milliseconds (order: classify, gjk_thread, gjk_warp,
- * epa_thread, epa_tier_a, epa_tier_b, epa_tier_c) of the last call and returns
+ * epa_thread, epa_warp, epa_wide) of the last call and returns
  * how many it wrote; it synchronises on the last call's events.  No reference
  * counterpart (the reference has no instrumentation). */
-#define NCG_N_STAGES 7
+#define NCG_N_STAGES 6
 int ncg_ctx_set_profiling(ncg_ctx* ctx, int enabled);
 int ncg_get_stage_ms(ncg_ctx* ctx, float* ms, int n_max);
 const char* ncg_last_error(void);
@@ -287,8 +285,8 @@ int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
  * start-up, and host runtimes (game engines, FFI hosts) that own every device
  * allocation themselves.  This entry point needs no ncg_ctx and never calls
  * cudaMalloc, cudaFree or any allocating routine: its scratch (pair lists, EPA
- * work items, 32 tier-B and one tier-C global-memory EPA slab) is a fixed
- * array of NCG_NOALLOC_SCRATCH_BYTES (13.8 MiB) compiled into the library,
+ * work items and one global-memory EPA slab) is a fixed array of
+ * NCG_NOALLOC_SCRATCH_BYTES (7.5 MiB) compiled into the library,
  * which every GPU that loads the library holds until the process exits.
  * Limit: at most NCG_NOALLOC_MAX_PAIRS pairs per call; a larger batch returns
  * NCG_EINVAL with a message in ncg_last_error().
@@ -303,7 +301,7 @@ int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
  * first GJK direction of every pair.  Results equal ncg_contact_batch's.
  * This entry point has no counterpart in the reference. */
 #define NCG_NOALLOC_MAX_PAIRS 32768
-#define NCG_NOALLOC_SCRATCH_BYTES 14454528
+#define NCG_NOALLOC_SCRATCH_BYTES 7827200
 int ncg_contact_batch_noalloc(const ncg_batch* batch, float prediction, int tolerance,
                               ncg_contact* out, uint8_t* has_contact, float* out_dir,
                               uint32_t* status, void* stream);

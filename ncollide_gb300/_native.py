@@ -36,12 +36,13 @@ EXPORTED = [
     "ncg_mlp_grad", "ncg_mlp_adam",
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
-TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT, TUNE_TIER_B_WARPS = range(5)
+TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT = range(4)
 DISPATCH_SUPPORT_MAP, DISPATCH_QUERY = 0, 1
 STATUS_UNSUPPORTED_FEATURE = 1 << 7
 STATUS_EPA_PRECISION_LIMIT = 1 << 8
 NOALLOC_MAX_PAIRS = 32768
-STAGES = ["classify", "gjk_thread", "gjk_warp", "epa_thread", "epa_tier_a", "epa_tier_b", "epa_tier_c"]
+NOALLOC_SCRATCH_BYTES = 7827200
+STAGES = ["classify", "gjk_thread", "gjk_warp", "epa_thread", "epa_warp", "epa_wide"]
 
 
 class NcgBatch(ctypes.Structure):

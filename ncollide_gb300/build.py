@@ -14,7 +14,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "_lib")
-LIB_PATH = os.path.join(LIB_DIR, "libncg.so")
+# NCG_LIB selects another build of the library (launch-tuning variants built
+# with NCG_DEFINES, e.g. "-DNCG_EPA_THREAD_VC=64"); the default is the in-tree build.
+LIB_PATH = os.environ.get("NCG_LIB") or os.path.join(LIB_DIR, "libncg.so")
 SOURCES = ["ncg_kernels.cu", "ncg_mlp.cu"]
 HEADERS = ["ncg_core.cuh", "ncg_epa.cuh", "ncg_dw.cuh", "ncg_query.cuh", "ncg_tc.cuh", "ncg_mlp.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -44,8 +46,9 @@ def build(force=False, verbose=False, extra=()):
     if not force and not _stale():
         return LIB_PATH
     os.makedirs(LIB_DIR, exist_ok=True)
-    objs = [os.path.join(LIB_DIR, os.path.splitext(s)[0] + ".o") for s in SOURCES]
-    flags = [f for f in NVCC_FLAGS if f != "-shared"]
+    tag = os.path.splitext(os.path.basename(LIB_PATH))[0]
+    objs = [os.path.join(LIB_DIR, f"{tag}_{os.path.splitext(s)[0]}.o") for s in SOURCES]
+    flags = [f for f in NVCC_FLAGS if f != "-shared"] + os.environ.get("NCG_DEFINES", "").split()
     cmds = [[nvcc(), *ARCH, *flags, *extra, "-c", "-o", o, os.path.join(CSRC, s)] for s, o in zip(SOURCES, objs)]
     if verbose:
         for c in cmds:
@@ -54,6 +57,7 @@ def build(force=False, verbose=False, extra=()):
     rcs = [p.wait() for p in procs]
     if any(rcs):
         raise RuntimeError(f"nvcc failed: {rcs}")
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
     tmp = LIB_PATH + ".tmp"
     link = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", tmp, *objs]
     subprocess.run(link, check=True)

@@ -89,12 +89,18 @@ constexpr int NB_HULL = 12;
 constexpr int NB = NB_ANALYTIC + NB_HULL;
 constexpr uint8_t NO_BUCKET = 0xff;
 
+// EPA queues: 0 the thread stage; 1 and 2 the first warp stage (1: pairs of two
+// curved shapes, whose polytopes grow longest, drained first; 2: the rest);
+// 3 and 4 the later warp stages.
+constexpr int N_EPA_QUEUES = 5;
+constexpr int Q_WARP_LONG = 1, Q_WARP = 2;
+
 struct DevCounters {
     unsigned long long n_analytic, n_hull;
     unsigned long long hull_next;
     unsigned long long n_items;       // EPA work items written
-    unsigned long long epa_count[4];  // items queued for: thread stage, tier A, B, C
-    unsigned long long epa_next[4];
+    unsigned long long epa_count[N_EPA_QUEUES];  // items per queue
+    unsigned long long epa_next[N_EPA_QUEUES];
     unsigned long long gjk_iters, epa_iters;
     uint32_t bucket_n[NB], bucket_fill[NB];
     uint32_t mlp_err;  // bit 0: a learned warm-start tensor-core wait timed out
@@ -103,25 +109,48 @@ constexpr size_t CTR_SLOT = 512;
 static_assert(sizeof(DevCounters) <= CTR_SLOT, "counters must fit their slot");
 
 struct Scratch {
+    // Shape kinds of a pair's two shapes (validated by k_classify).
+    NCG_DEV uint32_t bucket_kind1(const ncg_batch& b, uint32_t i) const { return __ldg(&b.shapes[b.g1[i]].kind); }
+    NCG_DEV uint32_t bucket_kind2(const ncg_batch& b, uint32_t i) const { return __ldg(&b.shapes[b.g2[i]].kind); }
     uint8_t* bucket;  // per pair: its cost bucket, NO_BUCKET for bad input
     uint32_t* sorted;  // pair indices by bucket: analytic pairs, then hull pairs
-    uint32_t* queue[4];  // item indices per EPA stage
+    uint32_t* queue[N_EPA_QUEUES];  // item indices per EPA stage
     EpaItem* items;
     DevCounters* ctr;
-    char* slabs[2];  // global EPA stores of tiers B and C
+    char* slabs[2];  // global EPA stores of the warp stages that use them, one per block
     size_t slab_bytes[2];
     int n_slabs[2];
 };
 
-// EPA store capacities per stage: vertices, live face slots (about twice the
-// vertices), silhouette edges, flood-fill stack.  Stage 0 is the per-thread
-// store, 1-3 the warp tiers A, B, C.
+// EPA store capacities: vertices, live face slots (about twice the vertices),
+// silhouette edges, flood-fill stack.  Store 0 is the per-thread store, 1-4
+// the warp stores (shared memory or one global slab per block).
 template <int T> struct EpaTier;
-template <> struct EpaTier<0> { static constexpr int VC = 48, FC = 2 * 48 + 16, SC = 32, TC = 96; };
+// Compile-time tuning: the thread stage's capacity and its minimum resident
+// blocks per SM (which caps its registers).
+#ifndef NCG_EPA_THREAD_VC
+#define NCG_EPA_THREAD_VC 64
+#endif
+#ifndef NCG_EPA_THREAD_MIN_BLOCKS
+#define NCG_EPA_THREAD_MIN_BLOCKS 4
+#endif
+#ifndef NCG_GJK_THREAD_MIN_BLOCKS
+#define NCG_GJK_THREAD_MIN_BLOCKS 4
+#endif
+template <> struct EpaTier<0> {
+    static constexpr int VC = NCG_EPA_THREAD_VC, FC = 2 * VC + 16, SC = VC < 64 ? 32 : VC / 2, TC = 2 * VC;
+};
+// 1: shared-memory warp store (the no-allocation path); 2: the warp stage's
+// global slabs; 3: the wide stage (one global slab per SM).
 template <> struct EpaTier<1> { static constexpr int VC = 128, FC = 2 * 128 + 64, SC = 64, TC = 256; };
 template <> struct EpaTier<2> { static constexpr int VC = 1280, FC = 2 * 1280 + 64, SC = 512, TC = 2048; };
 template <> struct EpaTier<3> { static constexpr int VC = 10240, FC = 2 * 10240 + 64, SC = 4096, TC = 16384; };
 static_assert(EpaTier<3>::FC < 65536 && EpaTier<3>::VC < 65536, "16-bit face and vertex indices");
+// Warps per SM of the warp stage (registers allow 12 at 168 per thread).
+#ifndef NCG_WARP_STAGE_PER_SM
+#define NCG_WARP_STAGE_PER_SM 12
+#endif
+constexpr int WARP_STAGE_MAX_PER_SM = NCG_WARP_STAGE_PER_SM;
 template <int T> size_t tier_bytes() {
     return EpaStore::bytes(EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC);
 }
@@ -410,7 +439,7 @@ NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
 // One thread per pair over a pair list (list 0: analytic pairs, list 1:
 // ConvexHull pairs, whose points the thread scans itself); EPA starts in the
 // thread stage.
-__global__ void __launch_bounds__(128) k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list) {
+__global__ void __launch_bounds__(128, NCG_GJK_THREAD_MIN_BLOCKS) k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list) {
     const unsigned long long n = *(volatile unsigned long long*)(list == 0 ? &s.ctr->n_analytic : &s.ctr->n_hull);
     const uint32_t* ids = list == 0 ? s.sorted : s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
     ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
@@ -437,7 +466,7 @@ __global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, O
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= n) break;
         unsigned long long a = 0;
-        gjk_pair(b, qp, o, s, ids[k], scan, lane == 0, a, 1);
+        gjk_pair(b, qp, o, s, ids[k], scan, lane == 0, a, Q_WARP);
         if (lane == 0) acc += a;
     }
     warp_add(&s.ctr->gjk_iters, acc);
@@ -509,43 +538,56 @@ NCG_DEV void load_simplex(const EpaItem& it, CSO* sv) {
     }
 }
 
-// EPA warp tier T: tier A (T = 1) keeps the polytope in dynamic shared memory
-// (one warp per block), tiers B and C in a global-memory slab per block.  A
-// pair whose polytope outgrows its tier is queued for the next tier and re-run
-// there from GJK's simplex; at tier C it ends with NCG_STATUS_EPA_CAPACITY.  One kernel
-// serves the three tiers (runtime capacities) to keep the code footprint small.
+// A warp EPA stage: one warp per pair (one warp per block), the polytope in
+// dynamic shared memory or in a global-memory slab per block.  It drains queue
+// q_in, then q_in2 (when >= 0); a pair whose polytope outgrows the store is
+// queued on q_out and re-run there from GJK's simplex, or, when q_out < 0,
+// ends with NCG_STATUS_EPA_CAPACITY.  One kernel serves every stage (runtime
+// capacities) to keep the code footprint small.
 struct TierCaps {
-    int tier, VC, FC, SC, TC;
+    int q_in, q_in2, q_out;
+    int slab;  // -1: shared memory; else index into Scratch::slabs
+    int VC, FC, SC, TC;
 };
-__global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs o, Scratch s, TierCaps tc) {
+#ifndef NCG_EPA_WARP_MIN_BLOCKS
+#define NCG_EPA_WARP_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(32, NCG_EPA_WARP_MIN_BLOCKS) k_epa(ncg_batch b, QueryParams qp, Outputs o, Scratch s, TierCaps tc) {
     extern __shared__ __align__(16) char smem[];
     const unsigned lane = threadIdx.x & 31u;
-    const int T = tc.tier;  // 1, 2 or 3
     EpaStore st;
-    if (T == 1) {
+    if (tc.slab < 0) {
         st.carve(smem, tc.VC, tc.FC, tc.SC, tc.TC);
     } else {
-        if (blockIdx.x >= (unsigned)s.n_slabs[T - 2]) return;
-        st.carve(s.slabs[T - 2] + (size_t)blockIdx.x * s.slab_bytes[T - 2], tc.VC, tc.FC, tc.SC, tc.TC);
+        if (blockIdx.x >= (unsigned)s.n_slabs[tc.slab]) return;
+        st.carve(s.slabs[tc.slab] + (size_t)blockIdx.x * s.slab_bytes[tc.slab], tc.VC, tc.FC, tc.SC, tc.TC);
     }
-    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[T];
     WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     unsigned long long acc = 0;
+    int q = tc.q_in;
+    unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[q];
     for (;;) {
         unsigned long long k = 0;
-        if (lane == 0) k = atomicAdd(&s.ctr->epa_next[T], 1ull);
+        if (lane == 0) k = atomicAdd(&s.ctr->epa_next[q], 1ull);
         k = __shfl_sync(0xffffffffu, k, 0);
-        if (k >= n) break;
-        const uint32_t item = s.queue[T][k];
+        if (k >= n) {
+            if (q == tc.q_in && tc.q_in2 >= 0) {
+                q = tc.q_in2;
+                n = *(volatile unsigned long long*)&s.ctr->epa_count[q];
+                continue;
+            }
+            break;
+        }
+        const uint32_t item = s.queue[q][k];
         const EpaItem& it = s.items[item];
         PairGeom g = item_geom(b, it);
         CSO sv[4];
         load_simplex(it, sv);
         EpaResult r = epa_run<WarpExec>(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
-        if (r.exit == EPA_OVERFLOW && T < 3) {
+        if (r.exit == EPA_OVERFLOW && tc.q_out >= 0) {
             if (lane == 0) {
-                unsigned long long q = atomicAdd(&s.ctr->epa_count[T + 1], 1ull);
-                s.queue[T + 1][q] = item;
+                unsigned long long pos = atomicAdd(&s.ctr->epa_count[tc.q_out], 1ull);
+                s.queue[tc.q_out][pos] = item;
             }
         } else {
             acc += r.iters;
@@ -563,8 +605,6 @@ __global__ void __launch_bounds__(32) k_epa(ncg_batch b, QueryParams qp, Outputs
     }
     if (lane == 0 && acc) atomicAdd(&s.ctr->epa_iters, acc);
 }
-// Tier B runs at most this many warps per SM: 8 x 152 slabs of 206 KiB.
-constexpr int TIER_B_WARPS_PER_SM = 8;
 NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
                              EpaStore& st) {
     const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[0];
@@ -579,8 +619,13 @@ NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Ou
         load_simplex(it, sv);
         EpaResult r = epa_run<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
         if (r.exit == EPA_OVERFLOW) {
-            unsigned long long q = atomicAdd(&s.ctr->epa_count[1], 1ull);
-            s.queue[1][q] = item;
+            // pairs of two curved shapes (their polytopes grow longest) go first;
+            // the shape kinds are re-read here (rare path) rather than kept live
+            const uint32_t k1 = s.bucket_kind1(b, it.pair), k2 = s.bucket_kind2(b, it.pair);
+            const bool curved = k1 != NCG_CUBOID && k1 != NCG_CONVEX_HULL && k2 != NCG_CUBOID && k2 != NCG_CONVEX_HULL;
+            const int qo = curved ? Q_WARP_LONG : Q_WARP;
+            unsigned long long pos = atomicAdd(&s.ctr->epa_count[qo], 1ull);
+            s.queue[qo][pos] = item;
         } else {
             acc += r.iters;
             finish_epa(b, qp, o, it, r, 0);
@@ -589,14 +634,16 @@ NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Ou
     warp_add(&s.ctr->epa_iters, acc);
 }
 
-template <int T> TierCaps caps() { return TierCaps{T, EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC}; }
+template <int T> TierCaps caps(int q_in, int q_in2, int q_out, int slab) {
+    return TierCaps{q_in, q_in2, q_out, slab, EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC};
+}
 
 // Thread stage: one thread per pair, the polytope in the thread's local
 // memory (L1 write-back; a per-thread global slab measured 17% slower, its
 // stores write through to L2).  A pair that outgrows it goes to warp tier A.
 constexpr size_t THREAD_STORE_BYTES =
     EpaStore::bytes(EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
-__global__ void __launch_bounds__(128) k_epa_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+__global__ void __launch_bounds__(128, NCG_EPA_THREAD_MIN_BLOCKS) k_epa_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
     __align__(16) char buf[THREAD_STORE_BYTES];
     EpaStore st;
     st.carve(buf, EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
@@ -656,11 +703,13 @@ struct ncg_ctx {
     int warm = NCG_WARM_NONE;
     int dispatch = NCG_DISPATCH_SUPPORT_MAP;
     int hull_gjk_warp = 0;  // GJK of ConvexHull pairs: 0 one thread per pair, 1 one warp per pair
-    int occ_thread = 1, occ_warp = 1, occ_epa0 = 1, occ_ethread = 1;
-    int gjk_blocks = 0, epa_blocks = 0, l1_carveout = 0, tier_b_warps = 0, tier_b_max = 0;
+    int occ_thread = 1, occ_warp = 1, occ_ethread = 1;
+    int occ_smem[2] = {1, 1};  // warps per SM of k_epa with a store of EpaTier<1> / <2> in shared memory
+    int occ_global = 1;        // warps per SM of k_epa on global slabs
+    int gjk_blocks = 0, epa_blocks = 0, l1_carveout = 0;
     char* scratch = nullptr;
     size_t scratch_cap_pairs = 0;
-    char* slabs = nullptr;  // tier B slabs, then tier C slabs
+    char* slabs = nullptr;  // warp-stage slabs, then wide-stage slabs
     int n_slabs[2] = {0, 0};
     size_t slab_bytes[2] = {0, 0};
     DevCounters* host_ctr = nullptr;  // pinned
@@ -691,7 +740,7 @@ bool ensure_scratch(ncg_ctx* c, uint64_t n) {
     if (c->scratch) cudaFree(c->scratch);
     c->scratch = nullptr;
     uint64_t cap = n < 1024 ? 1024 : n;
-    size_t bytes = 6 * 4 * cap + sizeof(EpaItem) * cap + CTR_SLOT + 1024;
+    size_t bytes = (2 + N_EPA_QUEUES) * 4 * cap + sizeof(EpaItem) * cap + CTR_SLOT + 1024;
     if (!cuda_ok(cudaMalloc(&c->scratch, bytes), "cudaMalloc(scratch)")) return false;
     c->scratch_cap_pairs = cap;
     return true;
@@ -730,7 +779,7 @@ Scratch carve_scratch(ncg_ctx* c) {
     s.items = (EpaItem*)p; p += sizeof(EpaItem) * cap;
     s.bucket = (uint8_t*)p; p += 4 * cap;
     s.sorted = (uint32_t*)p; p += 4 * cap;
-    for (int q = 0; q < 4; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * cap; }
+    for (int q = 0; q < N_EPA_QUEUES; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * cap; }
     s.slabs[0] = c->slabs;
     s.slabs[1] = c->slabs + c->slab_bytes[0] * c->n_slabs[0];
     for (int t = 0; t < 2; ++t) {
@@ -738,6 +787,27 @@ Scratch carve_scratch(ncg_ctx* c) {
         s.n_slabs[t] = c->n_slabs[t];
     }
     return s;
+}
+
+// Resident blocks per SM of every kernel (and the shared-memory limit of k_epa).
+struct Limits {
+    int occ_thread = 1, occ_warp = 1, occ_ethread = 1, occ_global = 1;
+    int occ_smem[2] = {1, 1};
+};
+Limits launch_limits() {
+    Limits l;
+    cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<2>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_thread, k_gjk_thread, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_warp, k_gjk_warp, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_ethread, k_epa_thread, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_global, k_epa, 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_smem[0], k_epa, 32, tier_bytes<1>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_smem[1], k_epa, 32, tier_bytes<2>());
+    int* all[] = {&l.occ_thread, &l.occ_warp, &l.occ_ethread, &l.occ_global, &l.occ_smem[0], &l.occ_smem[1]};
+    for (int* v : all)
+        if (*v < 1) *v = 1;
+    if (l.occ_global > WARP_STAGE_MAX_PER_SM) l.occ_global = WARP_STAGE_MAX_PER_SM;
+    return l;
 }
 
 // Shared-memory carveout preference of the kernels without shared memory
@@ -807,13 +877,12 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
         k_epa_thread<<<c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread), 128, 0, st>>>(
             bb, qp, o, s);
         mark(3);
-        k_epa<<<c->num_sms * c->occ_epa0, 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>());
+        // warp stage: the thread stage's overflow, pairs of curved shapes first
+        k_epa<<<c->n_slabs[0], 32, 0, st>>>(bb, qp, o, s, caps<2>(Q_WARP_LONG, Q_WARP, 3, 0));
         mark(4);
-        k_epa<<<c->num_sms * c->tier_b_warps, 32, 0, st>>>(bb, qp, o, s, caps<2>());
+        k_epa<<<c->n_slabs[1], 32, 0, st>>>(bb, qp, o, s, caps<3>(3, -1, -1, 1));
         mark(5);
-        k_epa<<<c->n_slabs[1], 32, 0, st>>>(bb, qp, o, s, caps<3>());
-        mark(6);
-        launches += 4;
+        launches += 3;
     }
     if (!cuda_ok(cudaGetLastError(), "kernel launch")) return NCG_ECUDA;
     if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st),
@@ -842,24 +911,17 @@ int ncg_ctx_create(ncg_ctx** out, int device) {
     ncg_ctx* c = new ncg_ctx();
     c->device = device;
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-    cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<1>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_thread, k_gjk_thread, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_warp, k_gjk_warp, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_epa0, k_epa, 32, tier_bytes<1>());
-    int occ_global = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_global, k_epa, 32, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_ethread, k_epa_thread, 128, 0);
-    if (c->occ_ethread < 1) c->occ_ethread = 1;
-    if (c->occ_thread < 1) c->occ_thread = 1;
-    if (c->occ_warp < 1) c->occ_warp = 1;
-    if (c->occ_epa0 < 1) c->occ_epa0 = 1;
-    if (occ_global < 1) occ_global = 1;
-    if (occ_global > TIER_B_WARPS_PER_SM) occ_global = TIER_B_WARPS_PER_SM;
+    Limits lim = launch_limits();
+    c->occ_thread = lim.occ_thread;
+    c->occ_warp = lim.occ_warp;
+    c->occ_ethread = lim.occ_ethread;
+    c->occ_global = lim.occ_global;
+    c->occ_smem[0] = lim.occ_smem[0];
+    c->occ_smem[1] = lim.occ_smem[1];
+    set_carveout(c->l1_carveout);
     c->slab_bytes[0] = (tier_bytes<2>() + 255) & ~size_t(255);
     c->slab_bytes[1] = (tier_bytes<3>() + 255) & ~size_t(255);
-    c->n_slabs[0] = c->num_sms * occ_global;
-    c->tier_b_warps = c->tier_b_max = occ_global;
-    set_carveout(c->l1_carveout);
+    c->n_slabs[0] = c->num_sms * c->occ_global;
     c->n_slabs[1] = c->num_sms;
     if (!cuda_ok(cudaMalloc(&c->slabs, c->slab_bytes[0] * c->n_slabs[0] + c->slab_bytes[1] * c->n_slabs[1]),
                  "cudaMalloc(slabs)") ||
@@ -926,10 +988,6 @@ int ncg_ctx_set_tuning(ncg_ctx* c, int key, int value) {
         if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
         c->l1_carveout = value;
         return set_carveout(value) ? NCG_OK : NCG_ECUDA;
-    case NCG_TUNE_TIER_B_WARPS:
-        if (value < 1 || value > c->tier_b_max) return NCG_EINVAL;
-        c->tier_b_warps = value;
-        return NCG_OK;
     default:
         g_last_error = "unknown tuning key";
         return NCG_EINVAL;
@@ -988,7 +1046,7 @@ int ncg_get_stats(ncg_ctx* c, ncg_stats* out) {
     // the caller synchronises the stream before reading the statistics.
     out->n_pairs = c->last.n_pairs;
     out->n_epa = c->host_ctr->n_items;
-    out->n_epa_overflow = c->host_ctr->epa_count[2];
+    out->n_epa_overflow = c->host_ctr->epa_count[Q_WARP_LONG] + c->host_ctr->epa_count[Q_WARP];
     out->gjk_iters = c->host_ctr->gjk_iters;
     out->epa_iters = c->host_ctr->epa_iters;
     out->kernels_launched = c->launches;
@@ -1215,17 +1273,14 @@ int ncg_proximity_batch_host(ncg_ctx* c, const ncg_batch* b, float margin, uint8
 // ncg_contact_batch_noalloc runs the contact pipeline on a fixed scratch array
 // in the library's device image instead of context-owned allocations.  Layout
 // of the array: counters (512 B), EPA work items, routing lists and stage
-// queues (6 x 4 B per pair), NA_TIER_B_SLABS tier-B EPA slabs, one tier-C slab.
+// queues (7 x 4 B per pair), one tier-D EPA slab.
 namespace {
 constexpr uint64_t NA_MAX_PAIRS = NCG_NOALLOC_MAX_PAIRS;
-constexpr int NA_TIER_B_SLABS = 32;
-constexpr size_t NA_SLAB_B_BYTES =
-    (EpaStore::bytes(EpaTier<2>::VC, EpaTier<2>::FC, EpaTier<2>::SC, EpaTier<2>::TC) + 255) & ~size_t(255);
 constexpr size_t NA_SLAB_BYTES =
     (EpaStore::bytes(EpaTier<3>::VC, EpaTier<3>::FC, EpaTier<3>::SC, EpaTier<3>::TC) + 255) & ~size_t(255);
 constexpr size_t NA_ITEMS_BYTES = sizeof(EpaItem) * NA_MAX_PAIRS;
-constexpr size_t NA_LISTS_BYTES = 6 * 4 * NA_MAX_PAIRS;
-constexpr size_t NA_BYTES = CTR_SLOT + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_TIER_B_SLABS * NA_SLAB_B_BYTES + NA_SLAB_BYTES;
+constexpr size_t NA_LISTS_BYTES = (2 + N_EPA_QUEUES) * 4 * NA_MAX_PAIRS;
+constexpr size_t NA_BYTES = CTR_SLOT + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_SLAB_BYTES;
 }  // namespace
 
 // Host code must not use this name as an address: it is only a host-side stand-in.
@@ -1236,7 +1291,8 @@ namespace {
 struct NoallocDevice {
     bool ready;
     char* base;  // device address of g_noalloc_scratch on this device
-    int num_sms, occ_thread, occ_warp, occ_epa0, occ_ethread;
+    int num_sms;
+    Limits lim;
 };
 std::mutex g_noalloc_mu;
 constexpr int NA_MAX_DEVICES = 64;
@@ -1254,15 +1310,7 @@ int noalloc_setup(int dev, NoallocDevice& out) {
         d.base = (char*)p;
         if (!cuda_ok(cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev), "device attribute"))
             return NCG_ECUDA;
-        cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<1>());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_thread, k_gjk_thread, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_warp, k_gjk_warp, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_epa0, k_epa, 32, tier_bytes<1>());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.occ_ethread, k_epa_thread, 128, 0);
-        if (d.occ_ethread < 1) d.occ_ethread = 1;
-        if (d.occ_thread < 1) d.occ_thread = 1;
-        if (d.occ_warp < 1) d.occ_warp = 1;
-        if (d.occ_epa0 < 1) d.occ_epa0 = 1;
+        d.lim = launch_limits();
         if (!cuda_ok(cudaGetLastError(), "noalloc set-up")) return NCG_ECUDA;
         d.ready = true;
     }
@@ -1302,14 +1350,13 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     s.items = (EpaItem*)p; p += NA_ITEMS_BYTES;
     s.bucket = (uint8_t*)p; p += 4 * NA_MAX_PAIRS;
     s.sorted = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
-    for (int q = 0; q < 4; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS; }
+    for (int q = 0; q < N_EPA_QUEUES; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS; }
     s.slabs[0] = p;
-    s.slab_bytes[0] = NA_SLAB_B_BYTES;
-    s.n_slabs[0] = NA_TIER_B_SLABS;
-    p += NA_TIER_B_SLABS * NA_SLAB_B_BYTES;
-    s.slabs[1] = p;
-    s.slab_bytes[1] = NA_SLAB_BYTES;
-    s.n_slabs[1] = 1;
+    s.slab_bytes[0] = NA_SLAB_BYTES;
+    s.n_slabs[0] = 1;
+    s.slabs[1] = nullptr;
+    s.slab_bytes[1] = 0;
+    s.n_slabs[1] = 0;
 
     QueryParams qp;
     qp.query = Q_CONTACT;
@@ -1327,11 +1374,12 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     unsigned n = (unsigned)b->n_pairs;
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
     k_bucket<<<(n + 255) / 256, 256, 0, st>>>(bb, s);
-    k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s, 0);
-    k_gjk_thread<<<d.num_sms * d.occ_thread, 128, 0, st>>>(bb, qp, o, s, 1);
-    k_epa_thread<<<d.num_sms * d.occ_ethread, 128, 0, st>>>(bb, qp, o, s);
-    k_epa<<<d.num_sms * d.occ_epa0, 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>());
-    k_epa<<<NA_TIER_B_SLABS, 32, 0, st>>>(bb, qp, o, s, caps<2>());
-    k_epa<<<1, 32, 0, st>>>(bb, qp, o, s, caps<3>());
+    k_gjk_thread<<<d.num_sms * d.lim.occ_thread, 128, 0, st>>>(bb, qp, o, s, 0);
+    k_gjk_thread<<<d.num_sms * d.lim.occ_thread, 128, 0, st>>>(bb, qp, o, s, 1);
+    k_epa_thread<<<d.num_sms * d.lim.occ_ethread, 128, 0, st>>>(bb, qp, o, s);
+    // warp stages in shared memory (128, then 1280 vertices), then the one global slab
+    k_epa<<<d.num_sms * d.lim.occ_smem[0], 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>(Q_WARP_LONG, Q_WARP, 3, -1));
+    k_epa<<<d.num_sms * d.lim.occ_smem[1], 32, tier_bytes<2>(), st>>>(bb, qp, o, s, caps<2>(3, -1, 4, -1));
+    k_epa<<<1, 32, 0, st>>>(bb, qp, o, s, caps<3>(4, -1, -1, 0));
     return cuda_ok(cudaGetLastError(), "noalloc kernel launch") ? NCG_OK : NCG_ECUDA;
 }

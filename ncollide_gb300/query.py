@@ -63,8 +63,7 @@ class Context:
         """Launch tuning (ncg_ctx_set_tuning); results do not depend on it."""
         if isinstance(key, str):
             key = {"hull_gjk_warp": N.TUNE_HULL_GJK_WARP, "gjk_blocks": N.TUNE_GJK_BLOCKS,
-                   "epa_blocks": N.TUNE_EPA_BLOCKS, "l1_carveout": N.TUNE_L1_CARVEOUT,
-                   "tier_b_warps": N.TUNE_TIER_B_WARPS}[key]
+                   "epa_blocks": N.TUNE_EPA_BLOCKS, "l1_carveout": N.TUNE_L1_CARVEOUT}[key]
         N.check(self._L.ncg_ctx_set_tuning(self._p, int(key), int(value)), "ncg_ctx_set_tuning")
 
     def set_warm_start(self, mode):
