@@ -701,19 +701,42 @@ def main():
                  eps=-1.0 if args.tolerance == "precise" else 0.0,
                  epa_tol=1e-6 if args.tolerance == "precise" else 0.0)
     bytes_pp, in_pp, out_pp, flops_pp = algorithmic(batch, rs.counters)
-    units = {"classify": batch.n_pairs, "gjk_thread": stats.get("n_pairs", 0), "gjk_warp": stats.get("n_pairs", 0),
-             "epa_thread": stats["n_epa"], "epa_warp": stats["n_epa_overflow"],
-             "epa_wide": stats["n_epa_overflow"]}.get(dom, batch.n_pairs)
+    # algorithmic bytes per unit of the dominant stage: a pair for GJK (inputs
+    # read once, outputs written once); an EPA item for the EPA stages (the
+    # 160-byte work item, the pair's poses, shape records and indices, the
+    # hull points of both shapes read once, and the outputs)
+    epa = rs.counters[:, 1] > 0
+    hull_pts = (sample.shapes["hull_n"][sample.g1].astype(np.float64) * (sample.shapes["kind"][sample.g1] == 5) +
+                sample.shapes["hull_n"][sample.g2].astype(np.float64) * (sample.shapes["kind"][sample.g2] == 5))
+    epa_item_bytes = 160.0 + 136.0 + 61.0 + (16.0 * hull_pts[epa].mean() if epa.any() else 0.0)
+    units, unit_bytes, unit_name = {
+        "classify": (batch.n_pairs, 72.0, "pair"),
+        "gjk_thread": (batch.n_pairs, bytes_pp, "pair"), "gjk_warp": (batch.n_pairs, bytes_pp, "pair"),
+        "epa_thread": (stats["n_epa"], epa_item_bytes, "EPA item"),
+        "epa_warp": (stats["n_epa_overflow"], epa_item_bytes, "EPA item"),
+        "epa_wide": (stats["n_epa_overflow"], epa_item_bytes, "EPA item")}.get(dom, (batch.n_pairs, bytes_pp, "pair"))
     dom_s = mean_stage[dom] / 1e3
-    achieved = units * bytes_pp / dom_s / 1e9
+    achieved = units * unit_bytes / dom_s / 1e9
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json"))).get("k_" + dom)
+        if tr:
+            traffic = {"bytes_per_launch": tr["dram_bytes_per_epa_item"] * units,
+                       "bytes_per_unit": tr["dram_bytes_per_epa_item"],
+                       "source": tr["source"] + "; scaled by this launch's EPA items"}
+    except (OSError, ValueError, KeyError):
+        traffic = None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
-                "traffic": None, "units_per_launch": int(units), "bytes_per_unit": bytes_pp,
+                "frac": achieved / hbm_peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)",
+                "traffic": traffic["bytes_per_launch"] if traffic else None, "traffic_detail": traffic,
+                "units_per_launch": int(units), "unit_of_work": unit_name, "bytes_per_unit": unit_bytes,
                 "mean_launch_ms": mean_stage[dom], "stage_ms": mean_stage,
+                "note": "latency-bound: the dominant stage moves far more DRAM bytes than its algorithmic "
+                        "bytes (local-memory EPA stores) yet uses a small fraction of the bandwidth",
                 "fp32": {"achieved_tflops": batch.n_pairs * flops_pp / (ms / 1e3 / args.steps) / 1e12,
                          "peak_tflops": fp32_peak, "frac": batch.n_pairs * flops_pp / (ms / 1e3 / args.steps) /
                          1e12 / fp32_peak, "flops_per_pair": flops_pp,
-                         "note": "whole step; peak = SMs x 128 x 2 x max SM clock"}}
+                         "note": "whole step, of measured clock peak: SMs x 128 x 2 x max SM clock"}}
 
     cpu = None
     acc = None
