@@ -619,6 +619,7 @@ def main():
         torch.cuda.synchronize()
         barrier()
     ms = e0.elapsed_time(e1)
+    stats = ctx.stats()  # of the last timed step
     if args.kernels_only:
         print(json.dumps({"kernels_only": True, "pairs": batch.n_pairs, "ms_per_step": ms / args.steps,
                           "stage_ms": {k: v / args.steps for k, v in stage_sums.items()}}), flush=True)
@@ -647,7 +648,6 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * batch.n_pairs * args.steps / (ms / 1e3)
-    stats = ctx.stats()
 
     # ---- e2e through the host entry point (pinned host buffers)
     e2e = None
