@@ -132,7 +132,8 @@ enum ncg_dispatch { NCG_DISPATCH_SUPPORT_MAP = 0, NCG_DISPATCH_QUERY = 1 };
 /* Warm-start sources for the first GJK direction. */
 enum ncg_warm_start {
     NCG_WARM_NONE = 0,      /* reference default: normalize(t2 - t1) (contact/proximity) */
-    NCG_WARM_INIT_DIR = 1,  /* batch->init_dir (the *_with_params init_dir argument)      */
+    NCG_WARM_INIT_DIR = 1,  /* batch->init_dir (the *_with_params init_dir argument); an
+                               all-zero entry means None for that pair                    */
     NCG_WARM_MLP = 2        /* the context's learned model predicts the direction        */
 };
 

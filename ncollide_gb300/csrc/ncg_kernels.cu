@@ -243,23 +243,24 @@ NCG_DEV void write_bad(const QueryParams& qp, const Outputs& o, uint32_t i) {
     write_outputs(qp, o, i, r, zero3<float>(), NCG_STATUS_BAD_INPUT, 0);
 }
 
-// First search direction of each *_with_params wrapper.
+// First search direction of each *_with_params wrapper.  An all-zero
+// init_dir entry means None (no unit vector is zero): the default is used.
 NCG_DEV vec3<float> initial_dir(const QueryParams& qp, const ncg_batch& b, uint32_t i, const PairGeom& g) {
     vec3<float> d;
     float n;
+    vec3<float> given{0.0f, 0.0f, 0.0f};
+    bool has = false;
+    if (qp.use_init_dir && b.init_dir) {
+        const float* p = b.init_dir + 3 * (size_t)i;
+        given = {p[0], p[1], p[2]};
+        has = !(given.x == 0.0f && given.y == 0.0f && given.z == 0.0f);
+    }
     if (qp.query == Q_CONTACT || qp.query == Q_PROXIMITY) {
-        if (qp.use_init_dir && b.init_dir) {
-            const float* p = b.init_dir + 3 * (size_t)i;
-            return {p[0], p[1], p[2]};
-        }
+        if (has) return given;
         if (try_normalize(g.m2.t - g.m1.t, qp.tol.init_eps, d, n)) return d;
         return {1.0f, 0.0f, 0.0f};
     }
-    vec3<float> d0 = g.m1.t - g.m2.t;
-    if (qp.use_init_dir && b.init_dir) {
-        const float* p = b.init_dir + 3 * (size_t)i;
-        d0 = {p[0], p[1], p[2]};
-    }
+    vec3<float> d0 = has ? given : g.m1.t - g.m2.t;
     if (try_normalize(d0, qp.tol.init_eps, d, n)) return d;
     return {1.0f, 0.0f, 0.0f};
 }

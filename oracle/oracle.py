@@ -28,7 +28,7 @@ _lib = None
 
 def build(force=False):
     """Compiles the oracle with the committed Makefile (g++ only)."""
-    srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "ncg_oracle.hpp")]
+    srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "ncg_oracle.hpp", "ncg_oracle_toi.hpp", "dw.hpp")]
     if not force and os.path.exists(LIB_PATH):
         if os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
             return LIB_PATH
@@ -48,6 +48,9 @@ def lib():
                                        vp, vp, vp, vp]
         L.ncgo_query_f64in.restype = i32
         L.ncgo_simplex_kat.argtypes = [i32, vp, vp, vp, vp]
+        L.ncgo_toi.argtypes = [i32, i32, f64, f64, f64, i32, vp, u32, vp, u64, u64, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                               vp]
+        L.ncgo_toi.restype = i32
         L.ncgo_simplex_kat.restype = i32
         _lib = L
     return _lib
@@ -155,3 +158,37 @@ def simplex_kat(points, policy=F32):
 
 def pose8(translation=(0, 0, 0), quaternion=(0, 0, 0, 1)):
     return list(quaternion) + list(translation) + [0.0]
+
+
+TOI_OUT_OF_ITERATIONS, TOI_CONVERGED, TOI_FAILED, TOI_PENETRATING = 0, 1, 2, 3
+
+
+def toi(batch, vel1, vel2, policy=F32, dispatch=0, max_toi=float("inf"), target_distance=0.0, eps=0.0, threads=None):
+    """Linear time of impact per pair (time_of_impact_support_map_support_map;
+    dispatch=1: Ball-Ball pairs by time_of_impact_ball_ball).  Returns a dict
+    with toi, witness1, witness2, normal1, normal2 (local frames), status
+    (TOIStatus), some (tag), gjk_status, iters."""
+    L = lib()
+    n = batch.n_pairs
+    threads = threads if threads is not None else (os.cpu_count() or 1)
+    out = np.zeros((n, 16), np.float64)
+    tag = np.zeros(n, np.uint8)
+    status = np.zeros(n, np.uint32)
+    counters = np.zeros((n, 8), np.uint32)
+    shapes = np.ascontiguousarray(batch.shapes)
+    pts = np.ascontiguousarray(batch.hull_points, np.float32)
+    m1 = np.ascontiguousarray(batch.m1, np.float32)
+    m2 = np.ascontiguousarray(batch.m2, np.float32)
+    g1 = np.ascontiguousarray(batch.g1, np.uint32)
+    g2 = np.ascontiguousarray(batch.g2, np.uint32)
+    v1 = np.ascontiguousarray(vel1, np.float32).reshape(n, 3)
+    v2 = np.ascontiguousarray(vel2, np.float32).reshape(n, 3)
+    mt = float(np.finfo(np.float32).max) if not np.isfinite(max_toi) else float(max_toi)
+    rc = L.ncgo_toi(policy, dispatch, mt, float(target_distance), float(eps), int(threads), _p(shapes), len(shapes),
+                    _p(pts), pts.shape[0], n, _p(m1), _p(g1), _p(m2), _p(g2), _p(v1), _p(v2), _p(out), _p(tag),
+                    _p(status), _p(counters))
+    if rc != 0:
+        raise ValueError(f"oracle rejected the call (rc={rc})")
+    return {"toi": out[:, 0], "witness1": out[:, 1:4], "witness2": out[:, 4:7], "normal1": out[:, 7:10],
+            "normal2": out[:, 10:13], "status": out[:, 13].astype(np.int32), "some": tag, "gjk_status": status,
+            "iters": counters[:, 0]}

@@ -8,6 +8,7 @@
 
 #include "../include/ncg.h"
 #include "ncg_oracle.hpp"
+#include "ncg_oracle_toi.hpp"
 
 using namespace ncgo;
 
@@ -89,13 +90,18 @@ template <class N> Iso<N> pose1(const InF32& in, uint64_t i) { return load_pose<
 template <class N> Iso<N> pose2(const InF32& in, uint64_t i) { return load_pose<N>(in.m2[i]); }
 template <class N> Iso<N> pose1(const InF64& in, uint64_t i) { return load_pose<N>(in.m1 + 8 * i); }
 template <class N> Iso<N> pose2(const InF64& in, uint64_t i) { return load_pose<N>(in.m2 + 8 * i); }
+// An all-zero init_dir entry means "no init_dir" (the reference's None): no
+// unit vector is zero, so this extends the reference's inputs without changing
+// any of them (a cached direction a proximity detector has dropped).
 template <class N> bool init_dir(const InF32& in, uint64_t i, V3<N>* d) {
     if (!in.init_dir) return false;
+    if (in.init_dir[3 * i] == 0.0f && in.init_dir[3 * i + 1] == 0.0f && in.init_dir[3 * i + 2] == 0.0f) return false;
     *d = V3<N>{N(in.init_dir[3 * i]), N(in.init_dir[3 * i + 1]), N(in.init_dir[3 * i + 2])};
     return true;
 }
 template <class N> bool init_dir(const InF64& in, uint64_t i, V3<N>* d) {
     if (!in.init_dir) return false;
+    if (in.init_dir[3 * i] == 0.0 && in.init_dir[3 * i + 1] == 0.0 && in.init_dir[3 * i + 2] == 0.0) return false;
     *d = V3<N>{N(in.init_dir[3 * i]), N(in.init_dir[3 * i + 1]), N(in.init_dir[3 * i + 2])};
     return true;
 }
@@ -189,9 +195,96 @@ int dispatch(int policy, const In& in, uint64_t n, int query, double param, doub
     }
 }
 
+template <class N, class S>
+void toi_range(const InF32& in, const float* vel1, const float* vel2, int dispatch, S max_toi, N target,
+               const Tol<S>& tol, uint64_t lo, uint64_t hi, const Outs& o) {
+    for (uint64_t i = lo; i < hi; ++i) {
+        Counters cnt;
+        Shape<N> s1, s2;
+        TOIOut<S> r;
+        bool ok = load_shape<N>(in, in.g1[i], &s1) && load_shape<N>(in, in.g2[i], &s2);
+        if (!ok) {
+            cnt.status |= ST_BAD_INPUT;
+        } else {
+            Iso<N> m1 = pose1<N>(in, i), m2 = pose2<N>(in, i);
+            V3<N> v1{N(vel1[3 * i]), N(vel1[3 * i + 1]), N(vel1[3 * i + 2])};
+            V3<N> v2{N(vel2[3 * i]), N(vel2[3 * i + 1]), N(vel2[3 * i + 2])};
+            if (dispatch == 1 && s1.kind == BALL && s2.kind == BALL)
+                r = toi_ball_ball<N, S>(m1, v1, s1.p0, m2, v2, s2.p0, max_toi, target);
+            else
+                r = toi_support_map<N, S>(m1, v1, s1, m2, v2, s2, max_toi, target, tol, &cnt);
+        }
+        if (o.out16) {
+            double* w = o.out16 + 16 * i;
+            w[0] = double(r.toi);
+            const V3<S>* v[4] = {&r.w1, &r.w2, &r.n1, &r.n2};
+            for (int k = 0; k < 4; ++k) {
+                w[1 + 3 * k] = double(v[k]->x);
+                w[2 + 3 * k] = double(v[k]->y);
+                w[3 + 3 * k] = double(v[k]->z);
+            }
+            w[13] = r.status;
+            w[14] = w[15] = 0.0;
+        }
+        if (o.tag) o.tag[i] = r.some ? 1 : 0;
+        if (o.status) o.status[i] = cnt.status;
+        if (o.counters8) {
+            uint32_t* c = o.counters8 + 8 * i;
+            for (int k = 0; k < 8; ++k) c[k] = 0;
+            c[0] = cnt.gjk_iters;
+            c[2] = cnt.support_calls;
+            c[3] = cnt.hull_points_scanned;
+        }
+    }
+}
+
+template <class N, class S>
+int toi_run(const InF32& in, const float* vel1, const float* vel2, uint64_t n, int dispatch, double max_toi,
+            double target, double eps, int nt, const Outs& o) {
+    double e = eps > 0 ? eps : (double)std::numeric_limits<N>::epsilon();
+    Tol<S> tol = eps < 0 ? make_tol_precise<S>(0.0) : make_tol<S>(e, 0.0);
+    S mt = max_toi >= (double)std::numeric_limits<float>::max() ? std::numeric_limits<S>::max() : S(max_toi);
+    N tg = N(target);
+    if (nt <= 1 || n < 64) {
+        toi_range<N, S>(in, vel1, vel2, dispatch, mt, tg, tol, 0, n, o);
+        return 0;
+    }
+    std::vector<std::thread> th;
+    uint64_t chunk = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t) {
+        uint64_t lo = t * chunk, hi = std::min<uint64_t>(n, lo + chunk);
+        if (lo >= hi) break;
+        th.emplace_back([&, lo, hi] { toi_range<N, S>(in, vel1, vel2, dispatch, mt, tg, tol, lo, hi, o); });
+    }
+    for (auto& x : th) x.join();
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Linear time of impact (time_of_impact_support_map_support_map; with
+// dispatch 1 Ball-Ball pairs take time_of_impact_ball_ball as
+// query::time_of_impact does).  vel1, vel2: 3 floats per pair.  max_toi at or
+// above FLT_MAX means unbounded.  out16: toi, witness1[3], witness2[3],
+// normal1[3], normal2[3] (local frames), TOIStatus; tag 1 = Some.
+// counters8[0] = ray-cast iterations.
+int ncgo_toi(int policy, int dispatch, double max_toi, double target_distance, double eps, int n_threads,
+             const ncg_shape* shapes, uint32_t n_shapes, const float* hull_points, uint64_t n_hull_points,
+             uint64_t n_pairs, const ncg_pose* m1, const uint32_t* g1, const ncg_pose* m2, const uint32_t* g2,
+             const float* vel1, const float* vel2, double* out16, uint8_t* tag, uint32_t* status,
+             uint32_t* counters8) {
+    if (!(target_distance >= 0.0) || !(max_toi >= 0.0)) return NCG_EINVAL;
+    InF32 in{shapes, n_shapes, hull_points, n_hull_points, m1, g1, m2, g2, nullptr};
+    Outs o{out16, tag, status, counters8};
+    switch (policy) {
+    case POLICY_F32: return toi_run<float, float>(in, vel1, vel2, n_pairs, dispatch, max_toi, target_distance, eps, n_threads, o);
+    case POLICY_F64: return toi_run<double, double>(in, vel1, vel2, n_pairs, dispatch, max_toi, target_distance, eps, n_threads, o);
+    case POLICY_MIXED: return toi_run<float, dw>(in, vel1, vel2, n_pairs, dispatch, max_toi, target_distance, eps, n_threads, o);
+    default: return NCG_EINVAL;
+    }
+}
 
 // policy: 0 = reference f32, 1 = reference f64, 2 = f32 supports + double-word sub-solve.
 // query:  0 = contact (support-map pairs), 1 = distance, 2 = proximity,

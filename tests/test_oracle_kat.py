@@ -115,3 +115,52 @@ def test_margin_negative_is_rejected():
     c = (1, (1.0, 1.0, 1.0), None)
     with pytest.raises(ValueError):
         O.query_f64([(O.pose8(), c, O.pose8((5, 0, 0)), c)], O.PROXIMITY, O.F64, param=-1.0)
+
+
+def _toi_batch(pairs):
+    from ncollide_gb300 import shapes as S
+    shp = np.zeros(2 * len(pairs), S.SHAPE_DTYPE)
+    m1 = np.zeros((len(pairs), 8), np.float32)
+    m2 = np.zeros((len(pairs), 8), np.float32)
+    for i, (t1, s1, t2, s2) in enumerate(pairs):
+        for j, (t, sh, m) in enumerate(((t1, s1, m1), (t2, s2, m2))):
+            shp[2 * i + j]["kind"] = sh[0]
+            shp[2 * i + j]["p"] = list(sh[1]) + [0.0] * (4 - len(sh[1]))
+            m[i, 3] = 1.0
+            m[i, 4:7] = t
+    g1 = np.arange(0, 2 * len(pairs), 2, dtype=np.uint32)
+    return S.PairBatch(shp, np.zeros((1, 4), np.float32), m1, g1, m2, g1 + 1)
+
+
+def test_time_of_impact_ball_cuboid():
+    k = GOLD["time_of_impact3_ball_cuboid"]
+    ball, cub = (0, (k["ball"]["radius"],)), (1, tuple(k["cuboid"]["half_extents"]))
+    b = _toi_batch([(cs["ball_translation"], ball, k["cuboid"]["translation"], cub) for cs in k["cases"]])
+    v1 = np.array([cs["ball_vel"] for cs in k["cases"]], np.float32)
+    v2 = np.array([cs["box_vel"] for cs in k["cases"]], np.float32)
+    r = O.toi(b, v1, v2, O.F64, dispatch=1)
+    assert r["some"][0] == 1 and r["toi"][0] == 0.0
+    want = (np.sqrt(3.0) - 1.0) / np.linalg.norm(v1[1].astype(np.float64) - v2[1])
+    assert r["some"][1] == 1 and abs(r["toi"][1] - want) <= np.finfo(np.float64).eps  # relative_eq!
+    assert r["some"][2] == 0
+    for pol in (O.F32, O.MIXED):
+        rp = O.toi(b, v1, v2, pol, dispatch=1)
+        assert list(rp["some"]) == [1, 1, 0] and rp["toi"][0] == 0.0
+
+
+def test_time_of_impact_ball_ball_analytic():
+    k = GOLD["ball_ball_toi"]
+    ball = (0, (k["radius"],))
+    b = _toi_batch([(k["m1_translation"], ball, k["m2_translation"], ball)])
+    r = O.toi(b, np.array([k["vel1"]], np.float32), np.array([k["vel2"]], np.float32), O.F64, dispatch=1)
+    assert r["some"][0] == 1 and r["toi"][0] == k["toi"]
+
+
+def test_time_of_impact_still_objects():
+    k = GOLD["still_objects_toi"]
+    c = (1, tuple(k["half_extents"]))
+    b = _toi_batch([(k["m1_translation"], c, k["m2_translation"], c)] * len(k["cases"]))
+    v1 = np.array([[0.0, cs["vel1_y"], 0.0] for cs in k["cases"]], np.float32)
+    for pol in (O.F32, O.MIXED):
+        r = O.toi(b, v1, np.zeros_like(v1), pol, dispatch=1)
+        assert [bool(x) for x in r["some"]] == [cs["some"] for cs in k["cases"]]

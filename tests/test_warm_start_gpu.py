@@ -121,3 +121,24 @@ def test_previous_frame_reuse_cuts_closest_points_iterations(ctx_factory):
     a = (cp["iters"].cpu().numpy().view(np.uint32) & 0xffff).mean()
     w = (cw["iters"].cpu().numpy().view(np.uint32) & 0xffff).mean()
     assert w <= 1.02 * a, (w, a)
+
+
+def test_proximity_detector_sep_axis_cache_bit_exact(ctx_factory):
+    """SupportMapSupportMapProximityDetector (support_map_support_map_proximity_detector.rs:32-60)
+    keeps the returned separating axis for the next update, or None after an
+    intersection; a batch expresses None as an all-zero init_dir entry."""
+    ctx = ctx_factory(tolerance=N.TOL_PRECISE, warm_start=N.WARM_INIT_DIR)
+    rng = np.random.default_rng(5)
+    f = W.mixed_convex(4096, seed=35)
+    cache = np.zeros((f.n_pairs, 3), np.float32)  # None for every pair at the first update
+    margin = 0.05
+    for _ in range(3):
+        b = f.with_init_dir(cache)
+        got = _host(Q.proximity_batch(ctx, Q.DeviceBatch.from_host(b), margin, with_iters=True))
+        torch.cuda.synchronize()
+        r = O.query(b, O.PROXIMITY, O.MIXED, param=margin, eps=-1.0, epa_tol=1e-6)
+        assert np.array_equal(got["proximity"], r.tag)
+        assert np.array_equal(got["dir"], r.dir.astype(np.float32))
+        assert np.array_equal(got["iters"].view(np.uint32) & 0xffff, r.counters[:, 0])
+        cache = np.where((got["proximity"] == 0)[:, None], 0.0, got["dir"]).astype(np.float32)
+        f = W.advance_frame(f, rng)
