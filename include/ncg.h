@@ -14,6 +14,8 @@
  *   distance   src/query/distance/distance_support_map_support_map.rs:8-53
  *   proximity  src/query/proximity/proximity_support_map_support_map.rs:10-75
  *   closest    src/query/closest_points/closest_points_support_map_support_map.rs:9-67
+ *   toi        src/query/time_of_impact/time_of_impact.rs:63-90,
+ *              src/query/time_of_impact/time_of_impact_support_map_support_map.rs:10-127
  * The per-pair arithmetic is gjk::closest_points (src/query/algorithms/gjk.rs:76-177)
  * with VoronoiSimplex (voronoi_simplex3.rs) and EPA (epa3.rs:219-454).
  */
@@ -105,6 +107,25 @@ enum ncg_closest_points { NCG_CP_INTERSECTING = 0, NCG_CP_WITHIN_MARGIN = 1, NCG
 #define NCG_STATUS_EPA_PRECISION_LIMIT (1u << 8) /* NCG_TOL_PRECISE: EPA's expansion would have
                                                     returned None (f32 noise on sliver faces); the
                                                     contact is the best face found so far */
+
+/* query::TOI<f32> (src/query/time_of_impact/time_of_impact.rs:29-42):
+ * witnesses and normals in the shapes' local frames; valid when has_toi. */
+typedef struct ncg_toi {
+    float toi;
+    float witness1[3];
+    float witness2[3];
+    float normal1[3];
+    float normal2[3];
+    uint32_t status; /* enum ncg_toi_status */
+} ncg_toi;
+
+/* TOIStatus (time_of_impact.rs:7-26), same discriminants. */
+enum ncg_toi_status {
+    NCG_TOI_OUT_OF_ITERATIONS = 0,
+    NCG_TOI_CONVERGED = 1,
+    NCG_TOI_FAILED = 2,
+    NCG_TOI_PENETRATING = 3
+};
 
 /* Return codes. */
 #define NCG_OK          0
@@ -268,6 +289,19 @@ int ncg_proximity_batch(ncg_ctx* ctx, const ncg_batch* batch, float margin,
  * out_points: 6 floats per pair (p1, p2), valid when tag == NCG_CP_WITHIN_MARGIN. */
 int ncg_closest_points_batch(ncg_ctx* ctx, const ncg_batch* batch, float prediction,
                              uint8_t* out_tag, float* out_points, uint32_t* status,
+                             uint32_t* iters, void* stream);
+
+/* query::time_of_impact for every pair (time_of_impact.rs:63-90 over
+ * time_of_impact_support_map_support_map.rs:10-127; Ball-Ball pairs take
+ * time_of_impact_ball_ball.rs:9-62 under NCG_DISPATCH_QUERY).  vel1, vel2:
+ * 3 floats per pair (linear velocities).  max_toi >= FLT_MAX (or +inf) means
+ * unbounded.  Returns NCG_EINVAL when max_toi or target_distance is negative
+ * or NaN.  has_toi[i] = 1 for Some; out[i] is then the TOI.  iters nullable:
+ * ray-cast iterations plus, for a dilated toi of zero, the GJK iterations of
+ * the closest-points refinement. */
+int ncg_time_of_impact_batch(ncg_ctx* ctx, const ncg_batch* batch, const float* vel1,
+                             const float* vel2, float max_toi, float target_distance,
+                             ncg_toi* out, uint8_t* has_toi, uint32_t* status,
                              uint32_t* iters, void* stream);
 
 /* ---- the same on host memory (synchronous; copies in and out) -------------- */

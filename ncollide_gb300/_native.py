@@ -33,11 +33,12 @@ EXPORTED = [
     "ncg_proximity_batch_host", "ncg_ctx_set_profiling", "ncg_get_stage_ms", "ncg_contact_batch_noalloc",
     "ncg_ctx_set_dispatch", "ncg_ctx_set_tuning", "ncg_contact_graph_create", "ncg_graph_launch",
     "ncg_graph_destroy", "ncg_mlp_n_params", "ncg_ctx_set_mlp_params", "ncg_mlp_features", "ncg_mlp_infer",
-    "ncg_mlp_grad", "ncg_mlp_adam",
+    "ncg_mlp_grad", "ncg_mlp_adam", "ncg_time_of_impact_batch",
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
 TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT = range(4)
 DISPATCH_SUPPORT_MAP, DISPATCH_QUERY = 0, 1
+TOI_OUT_OF_ITERATIONS, TOI_CONVERGED, TOI_FAILED, TOI_PENETRATING = range(4)
 STATUS_UNSUPPORTED_FEATURE = 1 << 7
 STATUS_EPA_PRECISION_LIMIT = 1 << 8
 NOALLOC_MAX_PAIRS = 32768
@@ -96,6 +97,7 @@ def load(build_if_missing=True):
     L.ncg_get_stage_ms.argtypes = [vp, vp, i32]
     L.ncg_contact_batch_noalloc.argtypes = [P(NcgBatch), f32, i32, vp, vp, vp, vp, vp]
     L.ncg_ctx_set_tuning.argtypes = [vp, i32, i32]
+    L.ncg_time_of_impact_batch.argtypes = [vp, P(NcgBatch), vp, vp, f32, f32, vp, vp, vp, vp, vp]
     L.ncg_contact_graph_create.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp, vp, P(vp)]
     L.ncg_graph_launch.argtypes = [vp, vp]
     L.ncg_graph_destroy.argtypes = [vp]

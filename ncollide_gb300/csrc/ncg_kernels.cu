@@ -35,6 +35,7 @@
 #include "../../include/ncg.h"
 #include "ncg_core.cuh"
 #include "ncg_mlp.h"
+#include "ncg_toi.h"
 #include "ncg_epa.cuh"
 #include "ncg_query.cuh"
 
@@ -1152,6 +1153,32 @@ int ncg_closest_points_batch(ncg_ctx* c, const ncg_batch* b, float prediction, u
     if (!out_tag) { g_last_error = "null output"; return NCG_EINVAL; }
     Outputs o{nullptr, out_tag, nullptr, nullptr, out_points, status, iters};
     return run_query(c, b, Q_CLOSEST, prediction, o, (cudaStream_t)stream);
+}
+
+int ncg_time_of_impact_batch(ncg_ctx* c, const ncg_batch* b, const float* vel1, const float* vel2, float max_toi,
+                             float target_distance, ncg_toi* out, uint8_t* has_toi, uint32_t* status, uint32_t* iters,
+                             void* stream) {
+    if (!(max_toi >= 0.0f) || !(target_distance >= 0.0f)) {
+        g_last_error = "max_toi and target_distance must be >= 0";
+        return NCG_EINVAL;
+    }
+    if (!c || !b) { g_last_error = "null context or batch"; return NCG_EINVAL; }
+    if (b->n_pairs == 0) return NCG_OK;
+    if (b->n_pairs > 0xffffffffull) { g_last_error = "more than 2^32-1 pairs"; return NCG_EINVAL; }
+    if (!b->shapes || !b->m1 || !b->m2 || !b->g1 || !b->g2 || !vel1 || !vel2 || !out || !has_toi || !status) {
+        g_last_error = "null required pointer";
+        return NCG_EINVAL;
+    }
+    if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    const Tol tol = make_tol(c->tol_mode);
+    int rc = toi_launch(*b, tol, c->dispatch, vel1, vel2, max_toi, target_distance, out, has_toi, status, iters,
+                        c->num_sms, (cudaStream_t)stream);
+    if (rc != NCG_OK) return rc;
+    c->launches = 1;
+    c->graph_launches = 1;
+    c->last = ncg_stats{};
+    c->last.n_pairs = b->n_pairs;
+    return NCG_OK;
 }
 
 }  // extern "C"

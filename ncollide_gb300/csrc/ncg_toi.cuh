@@ -1,0 +1,278 @@
+// ncg_toi.cuh — device side of the linear time of impact: the GJK ray cast on
+// the Minkowski difference of two support maps (optionally with the first
+// shape dilated by the target distance) and the analytic Ball-Ball case.
+//
+// Same arithmetic split as the GJK loop (ncg_core.cuh): support points, the
+// ray origin and the CSO points in f32; the simplex sub-solve, the ray
+// parameter, the bounds and the search direction in double-word.
+//
+// Reference (ncollide 0.33):
+//   src/query/algorithms/gjk.rs:196-345            directional_distance, minkowski_ray_cast
+//   src/query/ray/ray_plane.rs:9-39                line_toi_with_plane, ray_toi_with_plane
+//   src/query/algorithms/special_support_maps.rs:32-59   DilatedShape
+//   src/shape/ball.rs:36-48, capsule.rs:72-84, support_map.rs:18-35   support_point_toward
+//   src/query/time_of_impact/time_of_impact_support_map_support_map.rs:10-127
+//   src/query/time_of_impact/time_of_impact_ball_ball.rs:9-62, src/query/ray/ray_ball.rs:77-121
+//   src/query/time_of_impact/time_of_impact.rs:63-90 (Ball-Ball dispatch)
+#pragma once
+
+#include "ncg_core.cuh"
+
+namespace ncg {
+
+enum { TOI_OUT_OF_ITERATIONS = 0, TOI_CONVERGED = 1, TOI_FAILED = 2, TOI_PENETRATING = 3 };
+
+struct ToiResult {
+    bool some;
+    real toi;
+    vec3<float> w1, w2, n1, n2;  // the shapes' local frames
+    int status;
+};
+
+// SupportMap::support_point_toward with a unit direction: Ball and Capsule
+// use it as given, the other shapes go through local_support_point.
+template <class Scan>
+NCG_DEV vec3<float> support_point_toward(const Pose& m, const Shape& s, vec3<float> u, const Scan& scan) {
+    if (s.kind == KIND_CONSTANT_ORIGIN) return zero3<float>();
+    if (s.kind == NCG_BALL) return m.t + u * s.p0;
+    vec3<float> l = qrot_inv(m.q, u);
+    if (s.kind == NCG_CAPSULE) {
+        vec3<float> r{0.0f, copysignf(s.p0, l.y), 0.0f};
+        return qrot(m.q, r + l * s.p1) + m.t;
+    }
+    return qrot(m.q, local_support(s, l, scan)) + m.t;
+}
+
+// CSOPoint::from_shapes with the first shape optionally a DilatedShape:
+// its support point is support_point_toward(normalize(d)) + normalize(d) * r.
+template <class Scan>
+NCG_DEV CSO cso_dilated(const PairGeom& g, float radius, bool dilated, vec3<float> d, const Scan& scan) {
+    vec3<float> a;
+    if (dilated) {
+        vec3<float> u = d / vnorm(d);
+        a = support_point_toward(g.m1, g.g1, u, scan) + u * radius;
+    } else {
+        a = support_point(g.m1, g.g1, d, scan);
+    }
+    vec3<float> b = support_point(g.m2, g.g2, -d, scan);
+    return CSO{a - b, a, b};
+}
+
+// ray_toi_with_plane over line_toi_with_plane; relative_eq!(denom, 0) is |denom| <= eps.
+NCG_DEV bool ray_toi_with_plane(vec3<real> center, vec3<real> normal, vec3<real> orig, vec3<real> dir, real eps,
+                                real& t) {
+    vec3<real> dpos = center - orig;
+    real denom = dot(normal, dir);
+    if (fabs(denom) <= eps) return false;
+    real tt = dot(normal, dpos) / denom;
+    if (tt >= real(0.0f)) {
+        t = tt;
+        return true;
+    }
+    return false;
+}
+
+struct RayHit {
+    bool hit;
+    real toi;
+    vec3<real> normal;
+};
+
+// minkowski_ray_cast of the ray (origin 0, ray_dir, max_toi = the largest
+// float) against m1 * g1 - m2 * g2.  `iters` counts loop entries.
+template <class Scan>
+NCG_DEV RayHit minkowski_ray_cast(const PairGeom& g, float radius, bool dilated, vec3<real> ray_dir, Simplex& sx,
+                                  const Tol& tol, const Scan& scan, uint32_t& iters, uint32_t& status, int max_iter) {
+    RayHit out;
+    out.hit = false;
+    out.toi = real(0.0f);
+    out.normal = zero3<real>();
+    const real eps = from_host(tol.eps), eps_tol = from_host(tol.eps_tol), eps_rel = from_host(tol.eps_rel);
+    const real ray_length = vnorm(ray_dir);
+    if (ray_length <= eps) return out;
+    real ltoi = real(0.0f);
+    vec3<float> origin = zero3<float>();
+    const vec3<real> rdir = ray_dir / ray_length;
+    vec3<real> dir = -rdir;
+    vec3<real> ldir = dir;
+    CSO sp = cso_dilated(g, radius, dilated, to_f(dir), scan);
+    sp.p = sp.p - origin;
+    sx.reset(sp);
+    vec3<real> proj = sx.project_origin_and_reduce(tol, status);
+    real max_bound = dw_max();
+    bool last_chance = false;
+    int niter = 0;
+    for (;;) {
+        iters++;
+        const real old_max_bound = max_bound;
+        {
+            vec3<real> u;
+            real n;
+            if (try_normalize(-proj, eps_tol, u, n)) { dir = u; max_bound = n; }
+            else { out.hit = true; out.toi = ltoi / ray_length; out.normal = ldir; return out; }
+        }
+        CSO c;
+        if (max_bound >= old_max_bound) {
+            // upper-bound inconsistency: the projection itself is the support point
+            last_chance = true;
+            vec3<float> p = to_f(proj + to_r(origin));
+            c = CSO{p, p, zero3<float>()};
+        } else {
+            c = cso_dilated(g, radius, dilated, to_f(dir), scan);
+        }
+        if (last_chance && ltoi > real(0.0f)) { out.hit = true; out.toi = ltoi / ray_length; out.normal = ldir; return out; }
+        real t;
+        if (ray_toi_with_plane(to_r(c.p), dir, to_r(origin), rdir, eps, t)) {
+            if (dot(dir, rdir) < real(0.0f) && t > real(0.0f)) {
+                // a new lower bound: the ray origin moves
+                ldir = dir;
+                ltoi = ltoi + t;
+                if (ltoi / ray_length > dw_max()) return out;
+                const vec3<float> shift = to_f(rdir * t);
+                origin = origin + shift;
+                max_bound = dw_max();
+                for (int k = 0; k <= sx.dim; ++k) sx.v[k].p = sx.v[k].p - shift;
+                last_chance = false;
+            }
+        } else if (dot(dir, rdir) > eps_tol) {
+            return out;  // the ray misses
+        }
+        if (last_chance) return out;
+        const real min_bound = -dot(dir, to_r(c.p) - to_r(origin));
+        if (min_bound != min_bound) status |= NCG_STATUS_BAD_INPUT;
+        if (max_bound - min_bound <= eps_rel * max_bound) return out;
+        c.p = c.p - origin;
+        (void)sx.add_point(c, tol);
+        proj = sx.project_origin_and_reduce(tol, status);
+        if (sx.dim == 3) {
+            if (min_bound >= eps_tol) return out;
+            out.hit = true;
+            out.toi = ltoi / ray_length;
+            out.normal = ldir;
+            return out;
+        }
+        niter += 1;
+        if (niter == max_iter) {
+            status |= NCG_STATUS_GJK_MAX_ITER;
+            return out;
+        }
+    }
+}
+
+// time_of_impact_support_map_support_map.  max_toi and target_distance >= 0.
+template <class Scan>
+NCG_DEV ToiResult toi_support_map(const PairGeom& g, vec3<float> vel1, vec3<float> vel2, real max_toi, float target,
+                                  const Tol& tol, const Scan& scan, uint32_t& iters, uint32_t& status, int max_iter) {
+    ToiResult o;
+    o.some = false;
+    o.toi = real(0.0f);
+    o.w1 = o.w2 = o.n1 = o.n2 = zero3<float>();
+    o.status = TOI_CONVERGED;
+    const vec3<float> dvel = vel2 - vel1;
+    const bool dilated = target != 0.0f;
+    Simplex sx;
+    RayHit rc = minkowski_ray_cast(g, target, dilated, to_r(dvel), sx, tol, scan, iters, status, max_iter);
+    if (!rc.hit) return o;
+    // directional_distance: the witness points are the simplex's unless the toi is zero
+    vec3<real> w1 = zero3<real>(), w2 = zero3<real>();
+    if (!(rc.toi == real(0.0f))) gjk_result(sx, sx.dim == 3, w1, w2);
+    if (rc.toi > max_toi) return o;
+    o.some = true;
+    o.toi = rc.toi;
+    vec3<real> normal = rc.normal;
+    int st = TOI_CONVERGED;
+    if (dilated && rc.toi == real(0.0f)) {
+        // closest points of the undilated shapes within target, GJK started on the normal
+        vec3<float> d;
+        float dn;
+        if (!try_normalize(to_f(normal), FLT_EPSILON, d, dn)) d = mk(1.0f, 0.0f, 0.0f);
+        sx.reset(cso_support(g, d, scan));
+        GjkOut r = gjk(g, real(target), true, sx, tol, scan, iters, status, max_iter);
+        if (r.kind == GJK_CLOSEST_POINTS) {
+            vec3<real> dp = r.p2 - r.p1;
+            const vec3<float> nn = to_f(dp / vnorm(dp));
+            o.n1 = qrot_inv(g.m1.q, nn);
+            o.n2 = qrot_inv(g.m2.q, -nn);
+            o.w1 = qrot_inv(g.m1.q, to_f(w1) - g.m1.t);
+            o.w2 = qrot_inv(g.m2.q, to_f(w2) - g.m2.t);
+            o.status = TOI_CONVERGED;
+            return o;
+        }
+        if (r.kind == GJK_INTERSECTION) st = TOI_PENETRATING;
+    } else if (!dilated) {
+        st = rc.toi == real(0.0f) ? TOI_PENETRATING : TOI_CONVERGED;
+    }
+    const vec3<float> nf = to_f(normal);
+    o.n1 = qrot_inv(g.m1.q, nf);
+    o.n2 = qrot_inv(g.m2.q, -nf);
+    vec3<float> lw1 = qrot_inv(g.m1.q, to_f(w1) - g.m1.t);
+    if (dilated) lw1 = lw1 - o.n1 * target;
+    o.w1 = lw1;
+    o.w2 = qrot_inv(g.m2.q, to_f(w2) - g.m2.t);
+    o.status = st;
+    return o;
+}
+
+// ray_toi_with_ball (solid, ray origin 0): 0 miss, 1 hit, 2 origin inside.
+NCG_DEV int ray_toi_with_ball(vec3<real> center, real radius, vec3<real> dir, real& t) {
+    const vec3<real> dcenter = -center;
+    const real a = norm_sq(dir);
+    const real b = dot(dcenter, dir);
+    const real c = norm_sq(dcenter) - radius * radius;
+    if (a == real(0.0f)) {
+        if (c > real(0.0f)) return 0;
+        t = real(0.0f);
+        return 2;
+    }
+    if (c > real(0.0f) && b > real(0.0f)) return 0;
+    const real delta = b * b - a * c;
+    if (delta < real(0.0f)) return 0;
+    const real tt = (-b - sqrt(delta)) / a;
+    if (tt <= real(0.0f)) {
+        t = real(0.0f);
+        return 2;
+    }
+    t = tt;
+    return 1;
+}
+
+// time_of_impact_ball_ball on the balls' centres, then the dispatcher's
+// rotation of witnesses and normals into the balls' frames.
+NCG_DEV ToiResult toi_ball_ball(const Pose& m1, vec3<float> vel1, float r1, const Pose& m2, vec3<float> vel2,
+                                float r2, real max_toi, float target) {
+    ToiResult o;
+    o.some = false;
+    o.toi = real(0.0f);
+    o.w1 = o.w2 = o.n1 = o.n2 = zero3<float>();
+    o.status = TOI_CONVERGED;
+    const vec3<real> vel = to_r(vel1) - to_r(vel2);
+    const real rsum = real(r1) + real(r2);
+    const real radius = rsum + real(target);
+    const vec3<real> center = to_r(m1.t) - to_r(m2.t);
+    const vec3<real> dir = -vel;
+    real toi;
+    const int hit = ray_toi_with_ball(center, radius, dir, toi);
+    if (!hit) return o;
+    if (toi > max_toi) return o;
+    o.some = true;
+    o.toi = toi;
+    const vec3<real> dpt = dir * toi - center;
+    vec3<real> n1, n2, w1, w2;
+    if (radius == real(0.0f)) {
+        n1 = n2 = mk(real(1.0f), real(0.0f), real(0.0f));
+        w1 = w2 = zero3<real>();
+    } else {
+        n1 = dpt / radius;
+        n2 = -n1;
+        w1 = n1 * real(r1);
+        w2 = n2 * real(r2);
+    }
+    o.status = (hit == 2 && norm_sq(center) < rsum * rsum) ? TOI_PENETRATING : TOI_CONVERGED;
+    o.w1 = qrot_inv(m1.q, to_f(w1));
+    o.w2 = qrot_inv(m2.q, to_f(w2));
+    o.n1 = qrot_inv(m1.q, to_f(n1));
+    o.n2 = qrot_inv(m2.q, to_f(n2));
+    return o;
+}
+
+}  // namespace ncg

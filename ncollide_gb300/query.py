@@ -254,6 +254,31 @@ def closest_points_batch(ctx: Context, db: DeviceBatch, prediction=0.0, with_ite
     return out
 
 
+def time_of_impact_batch(ctx: Context, db: DeviceBatch, vel1, vel2, max_toi=float("inf"), target_distance=0.0,
+                         with_iters=False, stream=None):
+    """query::time_of_impact for every pair: vel1, vel2 [N,3] float32 device
+    tensors (linear velocities).  Returns has_toi (1 = Some), toi, witness1,
+    witness2, normal1, normal2 (local frames), toi_status (TOIStatus), status
+    (NCG_STATUS_* bits) and, with with_iters, the ray-cast iterations."""
+    n, dev = db.n_pairs, db.m1.device
+    vel1 = vel1.to(dev, torch.float32).contiguous()
+    vel2 = vel2.to(dev, torch.float32).contiguous()
+    if n and (tuple(vel1.shape) != (n, 3) or tuple(vel2.shape) != (n, 3)):
+        raise ValueError("vel1 and vel2 must be [n_pairs, 3]")
+    rec = _empty(n, (14,), torch.float32, dev)
+    has = _empty(n, (), torch.uint8, dev)
+    status = _empty(n, (), torch.int32, dev)
+    iters = _empty(n, (), torch.int32, dev) if with_iters else None
+    cb = db.c_struct()
+    N.check(ctx._L.ncg_time_of_impact_batch(ctx.handle, ctypes.byref(cb), _ptr(vel1), _ptr(vel2),
+                                            ctypes.c_float(max_toi), ctypes.c_float(target_distance), _ptr(rec),
+                                            _ptr(has), _ptr(status), _ptr(iters), _stream(stream)),
+            "ncg_time_of_impact_batch")
+    return {"has_toi": has, "toi": rec[:, 0], "witness1": rec[:, 1:4], "witness2": rec[:, 4:7],
+            "normal1": rec[:, 7:10], "normal2": rec[:, 10:13], "toi_status": rec[:, 13].view(torch.int32),
+            "status": status, "iters": iters, "_keep": (vel1, vel2)}
+
+
 def _host_struct(b: PairBatch, keep):
     arrs = {"shapes": np.ascontiguousarray(b.shapes), "hull": np.ascontiguousarray(b.hull_points, np.float32),
             "m1": np.ascontiguousarray(b.m1, np.float32), "g1": np.ascontiguousarray(b.g1, np.uint32),

@@ -216,3 +216,27 @@ def advance_frame(batch, rng, sigma_t=0.01, sigma_r=0.02):
         out.append(m)
     return PairBatch(batch.shapes, batch.hull_points, out[0], batch.g1, out[1], batch.g2,
                      batch.init_dir, batch.scale, dict(batch.meta))
+
+
+def toi_sweeps(n=1 << 20, seed=7, kinds=MIXED_KINDS, hull_n=(8, 1024), dmax=3.0, cone_deg=30.0):
+    """Linear sweeps for the time of impact: mixed convex pairs placed up to
+    dmax times their summed circumradii apart, the first shape moving towards
+    the second within a cone of half-angle cone_deg at speed U[0.5, 2] x the
+    summed circumradii, the second drifting at a tenth of that.  Returns
+    (batch, vel1 [n,3], vel2 [n,3])."""
+    b = mixed_convex(n, seed=seed, kinds=kinds, hull_n=hull_n, dmax=dmax)
+    b.meta.update({"workload": "toi_sweeps", "dmax": dmax, "cone_deg": cone_deg})
+    rng = np.random.default_rng(seed + 7919)
+    d = (b.m2[:, 4:7] - b.m1[:, 4:7]).astype(np.float64)
+    dn = np.linalg.norm(d, axis=1, keepdims=True)
+    d = np.where(dn > 0, d / np.maximum(dn, 1e-30), random_unit_vectors(rng, n))
+    jitter = random_unit_vectors(rng, n)
+    jitter -= (jitter * d).sum(1, keepdims=True) * d
+    jn = np.linalg.norm(jitter, axis=1, keepdims=True)
+    jitter = jitter / np.maximum(jn, 1e-30)
+    ang = np.radians(cone_deg) * np.sqrt(rng.uniform(0.0, 1.0, (n, 1)))
+    aim = d * np.cos(ang) + jitter * np.sin(ang)
+    speed = rng.uniform(0.5, 2.0, (n, 1)) * b.scale[:, None]
+    vel1 = (aim * speed).astype(np.float32)
+    vel2 = (random_unit_vectors(rng, n) * speed * 0.1).astype(np.float32)
+    return b, vel1, vel2
