@@ -504,6 +504,60 @@ def cuboid_small(args, local, tolerance):
             "has_contact_mismatch_vs_f64": int((has != r64.tag).sum())}
 
 
+def time_of_impact_report(args, local, tolerance, dispatch):
+    """query::time_of_impact over 2^20 linear sweeps (toi_sweeps, seed 7):
+    GPU throughput with inputs resident, the CPU reference path (oracle, f32)
+    on a 65,536-sweep sample with every host core, and agreement with f64."""
+    import torch
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import workloads as W
+    from oracle import oracle as O
+    n = args.toi_pairs
+    b, v1, v2 = W.toi_sweeps(n, seed=7)
+    dev = f"cuda:{local}"
+    db = Q.DeviceBatch.from_host(b, device=dev)
+    tv1, tv2 = torch.from_numpy(v1).to(dev), torch.from_numpy(v2).to(dev)
+    ctx = Q.Context(local, tolerance=tolerance, dispatch=dispatch)
+    for _ in range(3):
+        o = Q.time_of_impact_batch(ctx, db, tv1, tv2, with_iters=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        o = Q.time_of_impact_batch(ctx, db, tv1, tv2, with_iters=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    has = o["has_toi"].cpu().numpy()
+    toi = o["toi"].cpu().numpy()
+    iters = o["iters"].cpu().numpy()
+    ctx.close()
+    sample = min(65536, n)
+    idx = np.arange(sample)
+    sb = b.subset(idx)
+    threads = os.cpu_count() or 1
+    qd = 1 if dispatch == "query" else 0
+    t0 = time.perf_counter()
+    r32 = O.toi(sb, v1[idx], v2[idx], O.F32, dispatch=qd, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    r64 = O.toi(sb, v1[idx], v2[idx], O.F64, dispatch=qd, threads=threads)
+    m = (has[idx] == 1) & (r64["some"] == 1)
+    rel = np.abs(toi[idx][m] - r64["toi"][m]) / np.maximum(np.abs(r64["toi"][m]), 1e-30)
+    m32 = (r32["some"] == 1) & (r64["some"] == 1)
+    rel32 = np.abs(r32["toi"][m32] - r64["toi"][m32]) / np.maximum(np.abs(r64["toi"][m32]), 1e-30)
+    return {"workload": f"toi_sweeps {n} pairs, seed 7, max_toi inf, target_distance 0", "dispatch": dispatch,
+            "pairs_per_s": n / (ms / 1e3), "ms_per_step": ms, "some_fraction": float(has.mean()),
+            "ray_cast_iters_per_pair": float(iters.astype(np.float64).mean()),
+            "cpu_reference_path_pairs_per_s": sample / cpu_s, "cpu_cores": threads,
+            "cpu_sample": f"first {sample} sweeps, f32 reference path (oracle)",
+            "some_mismatch_vs_f64": int((has[idx] != r64["some"]).sum()),
+            "some_mismatch_f32_reference_vs_f64": int((r32["some"] != r64["some"]).sum()),
+            "toi_rel_err_vs_f64_p50_p99": [float(np.percentile(rel, 50)), float(np.percentile(rel, 99))] if rel.size else None,
+            "toi_rel_err_f32_reference_vs_f64_p50_p99":
+                [float(np.percentile(rel32, 50)), float(np.percentile(rel32, 99))] if rel32.size else None}
+
+
 def cpu_baseline(batch, threads, query):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -565,7 +619,9 @@ def main():
     ap.add_argument("--mlp-epochs", type=int, default=20)
     ap.add_argument("--no-mlp", action="store_true")
     ap.add_argument("--stress-pairs", type=int, default=1 << 20)
-    ap.add_argument("--no-extras", action="store_true", help="skip the precision-stress and cuboid reports")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the precision-stress, cuboid and time-of-impact reports")
+    ap.add_argument("--toi-pairs", type=int, default=1 << 20, help="sweeps of the time-of-impact report")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profiling: stop after the timed device steps (no second dispatch, no e2e, no report)")
     args = ap.parse_args()
@@ -746,10 +802,11 @@ def main():
         out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
         acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs), qo)
 
-    stress = cuboids = None
+    stress = cuboids = toi_rep = None
     if not args.no_extras:
         stress = precision_stress(args, local, args.tolerance)
         cuboids = cuboid_small(args, local, args.tolerance)
+        toi_rep = time_of_impact_report(args, local, args.tolerance, args.dispatch)
     learned = mlp_params = None
     if not args.no_mlp:
         mlp_params, learned = learned_warm_start(args, local, args.tolerance, args.dispatch, db, batch)
@@ -768,7 +825,7 @@ def main():
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc, "warm_start_coherent": coherent,
             "warm_start_learned": learned,
-            "precision_stress": stress, "cuboid_pairs_65536": cuboids,
+            "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
             "epa": {"pairs": stats["n_epa"], "warp_stage_pairs": stats["n_epa_overflow"],

@@ -38,6 +38,7 @@
 #include "ncg_toi.h"
 #include "ncg_epa.cuh"
 #include "ncg_query.cuh"
+#include "ncg_sort.cuh"
 
 using namespace ncg;
 
@@ -78,17 +79,6 @@ struct __align__(16) EpaItem {
     uint8_t dim, mode, flip, pad;
     float v[4][9];
 };
-
-// Pairs are counting-sorted into cost buckets before GJK so that the threads
-// of a warp run pairs of one shape-kind combination (analytic pairs) or of
-// similar hull sizes (ConvexHull pairs): the hull arg-max scans of a warp then
-// take about the same time.  Buckets 0-24: analytic kind pairs (k1 * 5 + k2,
-// k1 <= k2); 25-36: ConvexHull pairs by floor(log2(points scanned)), largest
-// first.
-constexpr int NB_ANALYTIC = 25;
-constexpr int NB_HULL = 12;
-constexpr int NB = NB_ANALYTIC + NB_HULL;
-constexpr uint8_t NO_BUCKET = 0xff;
 
 // EPA queues: 0 the thread stage; 1 and 2 the first warp stage (1: pairs of two
 // curved shapes, whose polytopes grow longest, drained first; 2: the rest);
@@ -371,33 +361,6 @@ NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& 
     if (writer) write_outputs(qp, o, i, r, d, status, pack_iters(iters, 0));
 }
 
-NCG_DEV int pair_bucket(const Shape& a, const Shape& c) {
-    if (a.kind == NCG_CONVEX_HULL || c.kind == NCG_CONVEX_HULL) {
-        uint32_t n = (a.kind == NCG_CONVEX_HULL ? a.n : 0u) + (c.kind == NCG_CONVEX_HULL ? c.n : 0u);
-        int lg = 31 - __clz(n);  // n >= 1: load_shape rejects empty hulls
-        lg = lg < 3 ? 3 : (lg > 3 + NB_HULL - 1 ? 3 + NB_HULL - 1 : lg);
-        return NB_ANALYTIC + (3 + NB_HULL - 1 - lg);
-    }
-    uint32_t k1 = a.kind < c.kind ? a.kind : c.kind, k2 = a.kind < c.kind ? c.kind : a.kind;
-    return (int)(k1 * 5u + k2);
-}
-
-// Warp-aggregated add to a per-bucket counter; returns this thread's slot.
-NCG_DEV uint32_t bucket_slot(uint32_t* ctr, int key, bool active) {
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned act = __ballot_sync(0xffffffffu, active);
-    uint32_t slot = 0;
-    if (active) {
-        const unsigned peers = __match_any_sync(act, key);
-        const int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if ((int)lane == leader) base = atomicAdd(&ctr[key], (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader);
-        slot = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-    }
-    return slot;
-}
-
 // Validates every pair, writes the outputs of bad ones and counts the buckets.
 __global__ void k_classify(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -412,25 +375,10 @@ __global__ void k_classify(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
     (void)bucket_slot(s.ctr->bucket_n, key < 0 ? 0 : key, key >= 0);
 }
 
-// Scatters the pairs into `sorted`, bucket by bucket (order inside a bucket is
-// arbitrary: every pair's result depends on the pair alone).
+// Scatters the pairs into `sorted`, bucket by bucket.
 __global__ void k_bucket(ncg_batch b, Scratch s) {
-    __shared__ uint32_t base[NB];
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (int k = 0; k < NB; ++k) {
-            base[k] = acc;
-            acc += s.ctr->bucket_n[k];
-            if (k == NB_ANALYTIC - 1 && blockIdx.x == 0) s.ctr->n_analytic = acc;
-        }
-        if (blockIdx.x == 0) s.ctr->n_hull = acc - base[NB_ANALYTIC];
-    }
-    __syncthreads();
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int key = i < b.n_pairs ? (int)s.bucket[i] : (int)NO_BUCKET;
-    const bool active = key != NO_BUCKET;
-    const uint32_t slot = bucket_slot(s.ctr->bucket_fill, active ? key : 0, active);
-    if (active) s.sorted[base[key] + slot] = (uint32_t)i;
+    scatter_by_bucket(b.n_pairs, s.bucket, s.ctr->bucket_n, s.ctr->bucket_fill, s.sorted, &s.ctr->n_analytic,
+                      &s.ctr->n_hull);
 }
 
 NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
@@ -1170,12 +1118,25 @@ int ncg_time_of_impact_batch(ncg_ctx* c, const ncg_batch* b, const float* vel1, 
         return NCG_EINVAL;
     }
     if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    if (!ensure_scratch(c, b->n_pairs)) return NCG_ENOMEM;
+    const Scratch s = carve_scratch(c);
     const Tol tol = make_tol(c->tol_mode);
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset counters")) return NCG_ECUDA;
+    uint32_t launches = 0;
+    // the TOI counters and the refinement queue live in the EPA item area
+    // (unused here; 160 bytes per pair); the ray-cast iterations are summed
+    // into the statistics' GJK iteration count
     int rc = toi_launch(*b, tol, c->dispatch, vel1, vel2, max_toi, target_distance, out, has_toi, status, iters,
-                        c->num_sms, (cudaStream_t)stream);
+                        ToiScratch{s.bucket, s.sorted, s.items, reinterpret_cast<char*>(s.items) + 512,
+                                   &s.ctr->gjk_iters},
+                        c->num_sms, st, &launches);
     if (rc != NCG_OK) return rc;
-    c->launches = 1;
-    c->graph_launches = 1;
+    if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st),
+                 "copy counters"))
+        return NCG_ECUDA;
+    c->launches = launches;
+    c->graph_launches = launches;
     c->last = ncg_stats{};
     c->last.n_pairs = b->n_pairs;
     return NCG_OK;

@@ -29,14 +29,19 @@ struct ToiResult {
     int status;
 };
 
-// SupportMap::support_point_toward with a unit direction: Ball and Capsule
-// use it as given, the other shapes go through local_support_point.
+// The first shape's support point: support_point(m, s, d), or with `toward`
+// SupportMap::support_point_toward(m, s, d) for a unit d (Ball and Capsule
+// use d as given; the other shapes go through local_support_point).  One
+// inlined support switch serves both.
 template <class Scan>
-NCG_DEV vec3<float> support_point_toward(const Pose& m, const Shape& s, vec3<float> u, const Scan& scan) {
+NCG_DEV vec3<float> support_point_ex(const Pose& m, const Shape& s, vec3<float> d, bool toward, const Scan& scan) {
     if (s.kind == KIND_CONSTANT_ORIGIN) return zero3<float>();
-    if (s.kind == NCG_BALL) return m.t + u * s.p0;
-    vec3<float> l = qrot_inv(m.q, u);
-    if (s.kind == NCG_CAPSULE) {
+    if (s.kind == NCG_BALL) {
+        vec3<float> u = toward ? d : d / vnorm(d);
+        return m.t + u * s.p0;
+    }
+    vec3<float> l = qrot_inv(m.q, d);
+    if (toward && s.kind == NCG_CAPSULE) {
         vec3<float> r{0.0f, copysignf(s.p0, l.y), 0.0f};
         return qrot(m.q, r + l * s.p1) + m.t;
     }
@@ -47,13 +52,10 @@ NCG_DEV vec3<float> support_point_toward(const Pose& m, const Shape& s, vec3<flo
 // its support point is support_point_toward(normalize(d)) + normalize(d) * r.
 template <class Scan>
 NCG_DEV CSO cso_dilated(const PairGeom& g, float radius, bool dilated, vec3<float> d, const Scan& scan) {
-    vec3<float> a;
-    if (dilated) {
-        vec3<float> u = d / vnorm(d);
-        a = support_point_toward(g.m1, g.g1, u, scan) + u * radius;
-    } else {
-        a = support_point(g.m1, g.g1, d, scan);
-    }
+    vec3<float> u = d;
+    if (dilated) u = d / vnorm(d);
+    vec3<float> a = support_point_ex(g.m1, g.g1, u, dilated, scan);
+    if (dilated) a = a + u * radius;
     vec3<float> b = support_point(g.m2, g.g2, -d, scan);
     return CSO{a - b, a, b};
 }
@@ -79,7 +81,10 @@ struct RayHit {
 };
 
 // minkowski_ray_cast of the ray (origin 0, ray_dir, max_toi = the largest
-// float) against m1 * g1 - m2 * g2.  `iters` counts loop entries.
+// float) against m1 * g1 - m2 * g2.  `iters` counts loop entries.  The loop is
+// rotated so that the support mapping and the simplex sub-solve each have a
+// single call site (the first pass takes the reference's initial support
+// point and simplex reset): inlined twice they overflow the instruction cache.
 template <class Scan>
 NCG_DEV RayHit minkowski_ray_cast(const PairGeom& g, float radius, bool dilated, vec3<real> ray_dir, Simplex& sx,
                                   const Tol& tol, const Scan& scan, uint32_t& iters, uint32_t& status, int max_iter) {
@@ -95,24 +100,13 @@ NCG_DEV RayHit minkowski_ray_cast(const PairGeom& g, float radius, bool dilated,
     const vec3<real> rdir = ray_dir / ray_length;
     vec3<real> dir = -rdir;
     vec3<real> ldir = dir;
-    CSO sp = cso_dilated(g, radius, dilated, to_f(dir), scan);
-    sp.p = sp.p - origin;
-    sx.reset(sp);
-    vec3<real> proj = sx.project_origin_and_reduce(tol, status);
-    real max_bound = dw_max();
-    bool last_chance = false;
+    vec3<real> proj = zero3<real>();
+    real max_bound = dw_max(), old_max_bound = dw_max();
+    bool last_chance = false, first = true;
     int niter = 0;
     for (;;) {
-        iters++;
-        const real old_max_bound = max_bound;
-        {
-            vec3<real> u;
-            real n;
-            if (try_normalize(-proj, eps_tol, u, n)) { dir = u; max_bound = n; }
-            else { out.hit = true; out.toi = ltoi / ray_length; out.normal = ldir; return out; }
-        }
         CSO c;
-        if (max_bound >= old_max_bound) {
+        if (!first && max_bound >= old_max_bound) {
             // upper-bound inconsistency: the projection itself is the support point
             last_chance = true;
             vec3<float> p = to_f(proj + to_r(origin));
@@ -120,54 +114,73 @@ NCG_DEV RayHit minkowski_ray_cast(const PairGeom& g, float radius, bool dilated,
         } else {
             c = cso_dilated(g, radius, dilated, to_f(dir), scan);
         }
-        if (last_chance && ltoi > real(0.0f)) { out.hit = true; out.toi = ltoi / ray_length; out.normal = ldir; return out; }
-        real t;
-        if (ray_toi_with_plane(to_r(c.p), dir, to_r(origin), rdir, eps, t)) {
-            if (dot(dir, rdir) < real(0.0f) && t > real(0.0f)) {
-                // a new lower bound: the ray origin moves
-                ldir = dir;
-                ltoi = ltoi + t;
-                if (ltoi / ray_length > dw_max()) return out;
-                const vec3<float> shift = to_f(rdir * t);
-                origin = origin + shift;
-                max_bound = dw_max();
-                for (int k = 0; k <= sx.dim; ++k) sx.v[k].p = sx.v[k].p - shift;
-                last_chance = false;
+        real min_bound = real(0.0f);
+        if (!first) {
+            if (last_chance && ltoi > real(0.0f)) { out.hit = true; out.toi = ltoi / ray_length; out.normal = ldir; return out; }
+            real t;
+            if (ray_toi_with_plane(to_r(c.p), dir, to_r(origin), rdir, eps, t)) {
+                if (dot(dir, rdir) < real(0.0f) && t > real(0.0f)) {
+                    // a new lower bound: the ray origin moves
+                    ldir = dir;
+                    ltoi = ltoi + t;
+                    if (ltoi / ray_length > dw_max()) return out;
+                    const vec3<float> shift = to_f(rdir * t);
+                    origin = origin + shift;
+                    max_bound = dw_max();
+                    for (int k = 0; k <= sx.dim; ++k) sx.v[k].p = sx.v[k].p - shift;
+                    last_chance = false;
+                }
+            } else if (dot(dir, rdir) > eps_tol) {
+                return out;  // the ray misses
             }
-        } else if (dot(dir, rdir) > eps_tol) {
-            return out;  // the ray misses
+            if (last_chance) return out;
+            min_bound = -dot(dir, to_r(c.p) - to_r(origin));
+            if (min_bound != min_bound) status |= NCG_STATUS_BAD_INPUT;
+            if (max_bound - min_bound <= eps_rel * max_bound) return out;
         }
-        if (last_chance) return out;
-        const real min_bound = -dot(dir, to_r(c.p) - to_r(origin));
-        if (min_bound != min_bound) status |= NCG_STATUS_BAD_INPUT;
-        if (max_bound - min_bound <= eps_rel * max_bound) return out;
         c.p = c.p - origin;
-        (void)sx.add_point(c, tol);
+        if (first) sx.reset(c);
+        else (void)sx.add_point(c, tol);
         proj = sx.project_origin_and_reduce(tol, status);
-        if (sx.dim == 3) {
-            if (min_bound >= eps_tol) return out;
-            out.hit = true;
-            out.toi = ltoi / ray_length;
-            out.normal = ldir;
-            return out;
+        if (!first) {
+            if (sx.dim == 3) {
+                if (min_bound >= eps_tol) return out;
+                out.hit = true;
+                out.toi = ltoi / ray_length;
+                out.normal = ldir;
+                return out;
+            }
+            niter += 1;
+            if (niter == max_iter) {
+                status |= NCG_STATUS_GJK_MAX_ITER;
+                return out;
+            }
         }
-        niter += 1;
-        if (niter == max_iter) {
-            status |= NCG_STATUS_GJK_MAX_ITER;
-            return out;
-        }
+        first = false;
+        iters++;
+        old_max_bound = max_bound;
+        vec3<real> u;
+        real n;
+        if (try_normalize(-proj, eps_tol, u, n)) { dir = u; max_bound = n; }
+        else { out.hit = true; out.toi = ltoi / ray_length; out.normal = ldir; return out; }
     }
 }
 
 // time_of_impact_support_map_support_map.  max_toi and target_distance >= 0.
+// With a dilated first shape and a toi of zero the result needs the closest
+// points of the undilated shapes: `refine` is then set, `ref_dir` holds the
+// world-space normal and toi_refine finishes the pair (a second pass, so that
+// the GJK loop is not inlined next to the ray cast).
 template <class Scan>
 NCG_DEV ToiResult toi_support_map(const PairGeom& g, vec3<float> vel1, vec3<float> vel2, real max_toi, float target,
-                                  const Tol& tol, const Scan& scan, uint32_t& iters, uint32_t& status, int max_iter) {
+                                  const Tol& tol, const Scan& scan, uint32_t& iters, uint32_t& status, int max_iter,
+                                  bool& refine, vec3<float>& ref_dir) {
     ToiResult o;
     o.some = false;
     o.toi = real(0.0f);
     o.w1 = o.w2 = o.n1 = o.n2 = zero3<float>();
     o.status = TOI_CONVERGED;
+    refine = false;
     const vec3<float> dvel = vel2 - vel1;
     const bool dilated = target != 0.0f;
     Simplex sx;
@@ -179,37 +192,52 @@ NCG_DEV ToiResult toi_support_map(const PairGeom& g, vec3<float> vel1, vec3<floa
     if (rc.toi > max_toi) return o;
     o.some = true;
     o.toi = rc.toi;
-    vec3<real> normal = rc.normal;
-    int st = TOI_CONVERGED;
+    const vec3<float> nf = to_f(rc.normal);
     if (dilated && rc.toi == real(0.0f)) {
-        // closest points of the undilated shapes within target, GJK started on the normal
-        vec3<float> d;
-        float dn;
-        if (!try_normalize(to_f(normal), FLT_EPSILON, d, dn)) d = mk(1.0f, 0.0f, 0.0f);
-        sx.reset(cso_support(g, d, scan));
-        GjkOut r = gjk(g, real(target), true, sx, tol, scan, iters, status, max_iter);
-        if (r.kind == GJK_CLOSEST_POINTS) {
-            vec3<real> dp = r.p2 - r.p1;
-            const vec3<float> nn = to_f(dp / vnorm(dp));
-            o.n1 = qrot_inv(g.m1.q, nn);
-            o.n2 = qrot_inv(g.m2.q, -nn);
-            o.w1 = qrot_inv(g.m1.q, to_f(w1) - g.m1.t);
-            o.w2 = qrot_inv(g.m2.q, to_f(w2) - g.m2.t);
-            o.status = TOI_CONVERGED;
-            return o;
-        }
-        if (r.kind == GJK_INTERSECTION) st = TOI_PENETRATING;
-    } else if (!dilated) {
-        st = rc.toi == real(0.0f) ? TOI_PENETRATING : TOI_CONVERGED;
+        refine = true;
+        ref_dir = nf;
+        return o;
     }
-    const vec3<float> nf = to_f(normal);
     o.n1 = qrot_inv(g.m1.q, nf);
     o.n2 = qrot_inv(g.m2.q, -nf);
     vec3<float> lw1 = qrot_inv(g.m1.q, to_f(w1) - g.m1.t);
     if (dilated) lw1 = lw1 - o.n1 * target;
     o.w1 = lw1;
     o.w2 = qrot_inv(g.m2.q, to_f(w2) - g.m2.t);
-    o.status = st;
+    o.status = dilated ? TOI_CONVERGED : (rc.toi == real(0.0f) ? TOI_PENETRATING : TOI_CONVERGED);
+    return o;
+}
+
+// The zero-toi case of a dilated first shape: closest points of the undilated
+// shapes within `target`, GJK started on the ray cast's normal nf (world
+// frame).  The witness points of a zero toi are the origin.
+template <class Scan>
+NCG_DEV ToiResult toi_refine(const PairGeom& g, vec3<float> nf, float target, const Tol& tol, const Scan& scan,
+                             uint32_t& iters, uint32_t& status, int max_iter) {
+    ToiResult o;
+    o.some = true;
+    o.toi = real(0.0f);
+    vec3<float> d;
+    float dn;
+    if (!try_normalize(nf, FLT_EPSILON, d, dn)) d = mk(1.0f, 0.0f, 0.0f);
+    Simplex sx;
+    sx.reset(cso_support(g, d, scan));
+    GjkOut r = gjk(g, real(target), true, sx, tol, scan, iters, status, max_iter);
+    const vec3<float> zf = zero3<float>();
+    o.w2 = qrot_inv(g.m2.q, zf - g.m2.t);
+    if (r.kind == GJK_CLOSEST_POINTS) {
+        vec3<real> dp = r.p2 - r.p1;
+        const vec3<float> nn = to_f(dp / vnorm(dp));
+        o.n1 = qrot_inv(g.m1.q, nn);
+        o.n2 = qrot_inv(g.m2.q, -nn);
+        o.w1 = qrot_inv(g.m1.q, zf - g.m1.t);
+        o.status = TOI_CONVERGED;
+        return o;
+    }
+    o.n1 = qrot_inv(g.m1.q, nf);
+    o.n2 = qrot_inv(g.m2.q, -nf);
+    o.w1 = qrot_inv(g.m1.q, zf - g.m1.t) - o.n1 * target;
+    o.status = r.kind == GJK_INTERSECTION ? TOI_PENETRATING : TOI_CONVERGED;
     return o;
 }
 
