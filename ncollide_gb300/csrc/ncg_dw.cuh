@@ -22,6 +22,21 @@
 #define NCG_DEV __device__ __forceinline__
 #endif
 
+// NCG_DW_OUTLINE, defined by a translation unit before its includes: 1 keeps
+// the double-word sum, quotient and square root out of line (one shared copy
+// each: the GJK-type loops are bound by instruction fetch), 2 also the
+// product.  Unset, everything is inlined (the EPA stages are latency-bound).
+#if defined(NCG_DW_OUTLINE) && NCG_DW_OUTLINE >= 1
+#define NCG_DW_BIG static __device__ __noinline__
+#else
+#define NCG_DW_BIG NCG_DEV
+#endif
+#if defined(NCG_DW_OUTLINE) && NCG_DW_OUTLINE >= 2
+#define NCG_DW_MUL static __device__ __noinline__
+#else
+#define NCG_DW_MUL NCG_DEV
+#endif
+
 namespace ncg {
 
 struct dw {
@@ -59,7 +74,7 @@ NCG_DEV dw two_prod(float a, float b) {
     float p = a * b;
     return dw(p, __fmaf_rn(a, b, -p));
 }
-NCG_DEV dw operator+(dw x, dw y) {
+NCG_DW_BIG dw operator+(dw x, dw y) {
     dw s = two_sum(x.h, y.h);
     dw t = two_sum(x.l, y.l);
     float c = s.l + t.h;
@@ -69,7 +84,7 @@ NCG_DEV dw operator+(dw x, dw y) {
 }
 NCG_DEV dw operator-(dw x) { return dw(-x.h, -x.l); }
 NCG_DEV dw operator-(dw x, dw y) { return x + (-y); }
-NCG_DEV dw operator*(dw x, dw y) {
+NCG_DW_MUL dw operator*(dw x, dw y) {
     dw c = two_prod(x.h, y.h);
     float tl0 = x.l * y.l;
     float tl1 = __fmaf_rn(x.h, y.l, tl0);
@@ -82,7 +97,7 @@ NCG_DEV dw mul_fp(dw x, float y) {
     float cl3 = __fmaf_rn(x.l, y, c.l);
     return fast_two_sum(c.h, cl3);
 }
-NCG_DEV dw operator/(dw x, dw y) {
+NCG_DW_BIG dw operator/(dw x, dw y) {
     float th = __fdiv_rn(x.h, y.h);
     dw r = mul_fp(y, th);
     float ph = x.h - r.h;
@@ -91,7 +106,7 @@ NCG_DEV dw operator/(dw x, dw y) {
     float tl = __fdiv_rn(d, y.h);
     return fast_two_sum(th, tl);
 }
-NCG_DEV dw sqrt(dw x) {
+NCG_DW_BIG dw sqrt(dw x) {
     if (!(x.h > 0.0f)) return x.h == 0.0f ? dw(0.0f) : dw(__int_as_float(0x7fc00000));
     float s = __fsqrt_rn(x.h);
     dw p = two_prod(s, s);

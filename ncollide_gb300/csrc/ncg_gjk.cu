@@ -1,0 +1,233 @@
+// ncg_gjk.cu — the GJK stage of a batched query: classification and the
+// counting sort by cost bucket, then GJK one thread per pair (analytic list,
+// and the ConvexHull list by default) or one warp per pair (ConvexHull list).
+// Pairs whose contact needs EPA leave their final simplex in the EPA queue.
+//
+// The double-word sum, quotient and square root are kept out of line in this
+// translation unit: the GJK loop is bound by instruction fetch (its warps sit
+// in different sub-solver branches), and one shared copy of each operation
+// roughly halves its time.  The EPA stages (ncg_kernels.cu) keep them inline.
+#define NCG_DW_OUTLINE 1
+
+#include <cuda_runtime.h>
+
+#include "ncg_pipeline.cuh"
+
+#ifndef NCG_GJK_THREAD_MIN_BLOCKS
+#define NCG_GJK_THREAD_MIN_BLOCKS 4
+#endif
+
+namespace ncg {
+namespace {
+
+// First search direction of each *_with_params wrapper.  An all-zero
+// init_dir entry means None (no unit vector is zero): the default is used.
+NCG_DEV vec3<float> initial_dir(const QueryParams& qp, const ncg_batch& b, uint32_t i, const PairGeom& g) {
+    vec3<float> d;
+    float n;
+    vec3<float> given{0.0f, 0.0f, 0.0f};
+    bool has = false;
+    if (qp.use_init_dir && b.init_dir) {
+        const float* p = b.init_dir + 3 * (size_t)i;
+        given = {p[0], p[1], p[2]};
+        has = !(given.x == 0.0f && given.y == 0.0f && given.z == 0.0f);
+    }
+    if (qp.query == Q_CONTACT || qp.query == Q_PROXIMITY) {
+        if (has) return given;
+        if (try_normalize(g.m2.t - g.m1.t, qp.tol.init_eps, d, n)) return d;
+        return {1.0f, 0.0f, 0.0f};
+    }
+    vec3<float> d0 = has ? given : g.m1.t - g.m2.t;
+    if (try_normalize(d0, qp.tol.init_eps, d, n)) return d;
+    return {1.0f, 0.0f, 0.0f};
+}
+
+// Runs one pair through GJK; writes its outputs or its EPA work item.
+// All lanes of a warp call this with the same pair when Scan is WarpScan.
+// epa_queue: the EPA stage the pair starts in (0 = thread stage, 1 = warp tier A).
+// Writes an EPA work item (GJK's final simplex) and queues it for `queue`.
+NCG_DEV void enqueue_epa(const Scratch& s, uint32_t i, int queue, const Simplex& sx, uint32_t iters, uint32_t status,
+                         int mode, bool flip) {
+    unsigned long long slot = atomicAdd(&s.ctr->n_items, 1ull);
+    unsigned long long pos = atomicAdd(&s.ctr->epa_count[queue], 1ull);
+    s.queue[queue][pos] = (uint32_t)slot;
+    EpaItem& it = s.items[slot];
+    it.pair = i;
+    it.gjk_iters = iters;
+    it.status = status;
+    it.dim = (uint8_t)sx.dim;
+    it.mode = (uint8_t)mode;
+    it.flip = flip ? 1 : 0;
+    for (int k = 0; k <= sx.dim; ++k) {
+        const CSO& c = sx.v[k];
+        float* w = it.v[k];
+        w[0] = c.p.x; w[1] = c.p.y; w[2] = c.p.z;
+        w[3] = c.o1.x; w[4] = c.o1.y; w[5] = c.o1.z;
+        w[6] = c.o2.x; w[7] = c.o2.y; w[8] = c.o2.z;
+    }
+}
+
+// Runs one pair through GJK; writes its outputs or its EPA work item.
+// All lanes of a warp call this with the same pair when Scan is WarpScan.
+// epa_queue: the EPA stage the pair starts in (0 = thread stage, 1 = warp tier A).
+// Both GJK routes (the pair itself, or the point projection of a ball's centre
+// on a ConvexHull) share one inlined GJK loop to keep the kernel's code small.
+template <class Scan>
+NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, uint32_t i,
+                      const Scan& scan, bool writer, unsigned long long& iter_acc, int epa_queue) {
+    PairGeom g;
+    load_shape(b, b.g1[i], g.g1);
+    load_shape(b, b.g2[i], g.g2);
+    g.m1 = load_pose(b.m1 + i);
+    g.m2 = load_pose(b.m2 + i);
+    int mode = 0;  // 0: GJK on the pair; 1: point projection of a ball's centre on a hull
+    bool flip = false;
+    const real pred = from_host(qp.param);
+    vec3<float> d;
+    real max_dist;
+    bool exact;
+    if (qp.query == Q_CONTACT && qp.dispatch == NCG_DISPATCH_QUERY) {
+        const bool b1 = g.g1.kind == NCG_BALL, b2 = g.g2.kind == NCG_BALL;
+        const bool p1 = g.g1.kind == NCG_CUBOID || g.g1.kind == NCG_CONVEX_HULL;
+        const bool p2 = g.g2.kind == NCG_CUBOID || g.g2.kind == NCG_CONVEX_HULL;
+        if (b1 && b2) {
+            QContact q = contact_ball_ball(g.m1.t, g.g1.p0, g.m2.t, g.g2.p0, pred);
+            if (writer) write_qcontact(o, i, q, 0, 0);
+            return;
+        }
+        if ((b1 && p2) || (p1 && b2)) {
+            flip = !b1;
+            const Pose& pb = flip ? g.m2 : g.m1;
+            const Shape& sb = flip ? g.g2 : g.g1;
+            const Pose& pp = flip ? g.m1 : g.m2;
+            const Shape& sp = flip ? g.g1 : g.g2;
+            if (sp.kind == NCG_CUBOID) {
+                bool inside;
+                vec3<float> pr;
+                int fk, fi;
+                aabb_project_with_feature(pp, mk(sp.p0, sp.p1, sp.p2), pb.t, inside, pr, fk, fi);
+                QContact q = ball_polyhedron_assemble(pb.t, sb.p0, inside, to_r(pr), fk, fi, true, pred, flip);
+                if (writer) write_qcontact(o, i, q, 0, 0);
+                return;
+            }
+            // point_projection_on_support_map: GJK on the translated hull
+            mode = 1;
+        }
+    }
+    PairGeom gg = g;
+    if (mode == 1) {
+        gg = projection_geom(flip ? g.m1 : g.m2, flip ? g.g1 : g.g2, flip ? g.m2.t : g.m1.t);
+        float dn;
+        if (!try_normalize(-gg.m1.t, FLT_EPSILON, d, dn)) d = mk(1.0f, 0.0f, 0.0f);
+        max_dist = dw_max();
+        exact = true;
+    } else {
+        d = initial_dir(qp, b, i, g);
+        max_dist = qp.query == Q_DISTANCE ? dw_max() : pred;
+        exact = qp.query != Q_PROXIMITY;
+    }
+    Simplex sx;
+    sx.reset(cso_support(gg, d, scan));
+    uint32_t iters = 0, status = 0;
+    GjkOut r = gjk(gg, max_dist, exact, sx, qp.tol, scan, iters, status, qp.gjk_max_iter);
+    iter_acc += iters;
+    if (qp.query == Q_CONTACT && r.kind == GJK_INTERSECTION) {
+        if (writer) enqueue_epa(s, i, epa_queue, sx, iters, status, mode, flip);
+        return;
+    }
+    if (mode == 1) {
+        const Pose& pb = flip ? g.m2 : g.m1;
+        const Shape& sb = flip ? g.g2 : g.g1;
+        bool inside = r.kind != GJK_CLOSEST_POINTS;  // the iteration cap: unreachable!() in gjk.rs:57
+        vec3<real> w2 = inside ? to_r(pb.t) : r.p1 + to_r(pb.t);
+        QContact q = ball_polyhedron_assemble(pb.t, sb.p0, inside, w2, F_UNKNOWN, 0, false, pred, flip);
+        if (writer) write_qcontact(o, i, q, status, pack_iters(iters, 0));
+        return;
+    }
+    if (writer) write_outputs(qp, o, i, r, d, status, pack_iters(iters, 0));
+}
+
+// Validates every pair, writes the outputs of bad ones and counts the buckets.
+__global__ void k_classify(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int key = -1;
+    if (i < b.n_pairs) {
+        Shape a, c;
+        bool ok = load_shape(b, b.g1[i], a) && load_shape(b, b.g2[i], c);
+        if (!ok) write_bad(qp, o, (uint32_t)i);
+        else key = pair_bucket(a, c);
+        s.bucket[i] = key < 0 ? NO_BUCKET : (uint8_t)key;
+    }
+    (void)bucket_slot(s.ctr->bucket_n, key < 0 ? 0 : key, key >= 0);
+}
+
+// Scatters the pairs into `sorted`, bucket by bucket.
+__global__ void k_bucket(ncg_batch b, Scratch s) {
+    scatter_by_bucket(b.n_pairs, s.bucket, s.ctr->bucket_n, s.ctr->bucket_fill, s.sorted, &s.ctr->n_analytic,
+                      &s.ctr->n_hull);
+}
+
+// One thread per pair over a pair list (list 0: analytic pairs, list 1:
+// ConvexHull pairs, whose points the thread scans itself); EPA starts in the
+// thread stage.
+__global__ void __launch_bounds__(128, NCG_GJK_THREAD_MIN_BLOCKS) k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list) {
+    const unsigned long long n = *(volatile unsigned long long*)(list == 0 ? &s.ctr->n_analytic : &s.ctr->n_hull);
+    const uint32_t* ids = list == 0 ? s.sorted : s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
+    ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
+    unsigned long long acc = 0;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long start = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned long long rounds = (n + stride - 1) / stride;
+    for (unsigned long long r = 0; r < rounds; ++r) {
+        unsigned long long k = start + r * stride;
+        if (k < n) gjk_pair(b, qp, o, s, ids[k], scan, true, acc, 0);
+    }
+    warp_add(&s.ctr->gjk_iters, acc);
+}
+
+__global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->n_hull;
+    const uint32_t* ids = s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
+    WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long acc = 0;
+    for (;;) {
+        unsigned long long k = 0;
+        if (lane == 0) k = atomicAdd(&s.ctr->hull_next, 1ull);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= n) break;
+        unsigned long long a = 0;
+        gjk_pair(b, qp, o, s, ids[k], scan, lane == 0, a, Q_WARP);
+        if (lane == 0) acc += a;
+    }
+    warp_add(&s.ctr->gjk_iters, acc);
+}
+
+}  // namespace
+
+void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, cudaStream_t st) {
+    const unsigned n = (unsigned)b.n_pairs;
+    k_classify<<<(n + 255) / 256, 256, 0, st>>>(b, qp, o, s);
+    k_bucket<<<(n + 255) / 256, 256, 0, st>>>(b, s);
+}
+
+void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
+                       int list, cudaStream_t st) {
+    k_gjk_thread<<<grid, 128, 0, st>>>(b, qp, o, s, list);
+}
+
+void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
+                     cudaStream_t st) {
+    k_gjk_warp<<<grid, 128, 0, st>>>(b, qp, o, s);
+}
+
+void gjk_occupancy(int* occ_thread, int* occ_warp) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ_thread, k_gjk_thread, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ_warp, k_gjk_warp, 128, 0);
+}
+
+cudaError_t gjk_set_carveout(int pct) {
+    return cudaFuncSetAttribute(k_gjk_thread, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+}
+
+}  // namespace ncg

@@ -1,27 +1,27 @@
-// ncg_kernels.cu — batched GJK/EPA kernels for sm_103a and the C ABI of include/ncg.h.
+// ncg_kernels.cu — the EPA stages of a batched contact query, the host side
+// of every query and the C ABI of include/ncg.h.
 //
 // One batch call runs, on one stream and without host synchronisation:
-//   1. classify     1 thread/pair: validates the pair, routes it to the
-//                   analytic list (no ConvexHull) or the hull list.
-//   2. gjk_thread   1 thread/pair over the analytic list (persistent grid).
-//   3. gjk_warp     1 warp/pair over the hull list (dynamic queue); the hull
-//                   arg-max is warp-parallel with coalesced 128-bit loads.
-//   4. epa_thread   contact only, intersecting pairs: one thread per pair,
-//                   polytope of up to 48 vertices in the thread's local memory
-//                   (the median pair needs 13 iterations).
-//   5. epa tier A   pairs that outgrew epa_thread (and the EPA of hull pairs
-//                   when their GJK ran one warp per pair): one warp per pair,
-//                   up to 128 vertices in shared memory.
-//   6. epa tier B   pairs that outgrew tier A: up to 1280 vertices in a
-//                   global-memory slab per warp, as many warps per SM as
-//                   registers allow (the tail pairs run hundreds of
-//                   latency-bound iterations each, so concurrency wins over
-//                   shared-memory latency).
-//   7. epa tier C   pairs that outgrew tier B: a global-memory slab per warp
-//                   (up to 10240 vertices).
+//   1. classify, bucket   (ncg_gjk.cu) 1 thread/pair: validates the pair and
+//                         counting-sorts it by cost bucket (shape kinds, hull
+//                         sizes).
+//   2. gjk_thread         (ncg_gjk.cu) 1 thread/pair over the analytic list,
+//                         then over the ConvexHull list (or 1 warp/pair over
+//                         the ConvexHull list with NCG_TUNE_HULL_GJK_WARP).
+//   3. epa_thread         contact only, intersecting pairs: 1 thread/pair,
+//                         polytope of up to 64 vertices in local memory.
+//   4. epa warp stage     pairs that outgrew the thread stage: 1 warp/pair,
+//                         up to 1280 vertices in a global-memory slab per
+//                         warp, 12 warps per SM; pairs of two curved shapes
+//                         (the longest polytopes) first.
+//   5. epa wide stage     pairs that outgrew the warp stage: up to 10240
+//                         vertices, one slab per SM.
 // A pair that outgrows a stage is re-run by the next one from GJK's simplex.
 // Pairs are independent; the GJK stage writes its outputs directly or appends
-// the final simplex to the EPA queue.
+// the final simplex to the EPA queue.  The no-allocation entry point runs the
+// same GJK stage, then EPA with 128 and 1280 vertices in shared memory and a
+// static global slab.
+
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -38,6 +38,7 @@
 #include "ncg_toi.h"
 #include "ncg_epa.cuh"
 #include "ncg_query.cuh"
+#include "ncg_pipeline.cuh"
 #include "ncg_sort.cuh"
 
 using namespace ncg;
@@ -45,73 +46,6 @@ using namespace ncg;
 namespace {
 
 thread_local std::string g_last_error;
-
-enum QueryKind { Q_CONTACT = 0, Q_DISTANCE = 1, Q_PROXIMITY = 2, Q_CLOSEST = 3 };
-
-struct Outputs {
-    ncg_contact* contact;
-    uint8_t* tag;
-    float* dir;
-    float* value;
-    float* points;
-    uint32_t* status;
-    uint32_t* iters;
-};
-
-struct QueryParams {
-    int query;
-    int dispatch;  // ncg_dispatch (contact only)
-    int use_init_dir;
-    int gjk_max_iter;
-    int epa_max_iter;
-    dw_host param;  // prediction / margin
-    Tol tol;
-};
-
-// EPA work item: the pair and GJK's final simplex (dim + 1 CSO points).
-// `mode` 0: contact_support_map_support_map; 1: point projection of a ball's
-// centre on a ConvexHull (query::contact dispatch), `flip` when the ball is
-// the second shape.
-struct __align__(16) EpaItem {
-    uint32_t pair;
-    uint32_t gjk_iters;
-    uint32_t status;
-    uint8_t dim, mode, flip, pad;
-    float v[4][9];
-};
-
-// EPA queues: 0 the thread stage; 1 and 2 the first warp stage (1: pairs of two
-// curved shapes, whose polytopes grow longest, drained first; 2: the rest);
-// 3 and 4 the later warp stages.
-constexpr int N_EPA_QUEUES = 5;
-constexpr int Q_WARP_LONG = 1, Q_WARP = 2;
-
-struct DevCounters {
-    unsigned long long n_analytic, n_hull;
-    unsigned long long hull_next;
-    unsigned long long n_items;       // EPA work items written
-    unsigned long long epa_count[N_EPA_QUEUES];  // items per queue
-    unsigned long long epa_next[N_EPA_QUEUES];
-    unsigned long long gjk_iters, epa_iters;
-    uint32_t bucket_n[NB], bucket_fill[NB];
-    uint32_t mlp_err;  // bit 0: a learned warm-start tensor-core wait timed out
-};
-constexpr size_t CTR_SLOT = 512;
-static_assert(sizeof(DevCounters) <= CTR_SLOT, "counters must fit their slot");
-
-struct Scratch {
-    // Shape kinds of a pair's two shapes (validated by k_classify).
-    NCG_DEV uint32_t bucket_kind1(const ncg_batch& b, uint32_t i) const { return __ldg(&b.shapes[b.g1[i]].kind); }
-    NCG_DEV uint32_t bucket_kind2(const ncg_batch& b, uint32_t i) const { return __ldg(&b.shapes[b.g2[i]].kind); }
-    uint8_t* bucket;  // per pair: its cost bucket, NO_BUCKET for bad input
-    uint32_t* sorted;  // pair indices by bucket: analytic pairs, then hull pairs
-    uint32_t* queue[N_EPA_QUEUES];  // item indices per EPA stage
-    EpaItem* items;
-    DevCounters* ctr;
-    char* slabs[2];  // global EPA stores of the warp stages that use them, one per block
-    size_t slab_bytes[2];
-    int n_slabs[2];
-};
 
 // EPA store capacities: vertices, live face slots (about twice the vertices),
 // silhouette edges, flood-fill stack.  Store 0 is the per-thread store, 1-4
@@ -124,9 +58,6 @@ template <int T> struct EpaTier;
 #endif
 #ifndef NCG_EPA_THREAD_MIN_BLOCKS
 #define NCG_EPA_THREAD_MIN_BLOCKS 4
-#endif
-#ifndef NCG_GJK_THREAD_MIN_BLOCKS
-#define NCG_GJK_THREAD_MIN_BLOCKS 4
 #endif
 template <> struct EpaTier<0> {
     static constexpr int VC = NCG_EPA_THREAD_VC, FC = 2 * VC + 16, SC = VC < 64 ? 32 : VC / 2, TC = 2 * VC;
@@ -144,282 +75,6 @@ static_assert(EpaTier<3>::FC < 65536 && EpaTier<3>::VC < 65536, "16-bit face and
 constexpr int WARP_STAGE_MAX_PER_SM = NCG_WARP_STAGE_PER_SM;
 template <int T> size_t tier_bytes() {
     return EpaStore::bytes(EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC);
-}
-
-NCG_DEV uint32_t pack_iters(uint32_t g, uint32_t e) { return (g > 0xffffu ? 0xffffu : g) | ((e > 0xffffu ? 0xffffu : e) << 16); }
-
-// Results leave the device as the high word of each double-word.
-NCG_DEV void wr3(float* p, vec3<real> v) {
-    p[0] = v.x.h;
-    p[1] = v.y.h;
-    p[2] = v.z.h;
-}
-
-// Writes the outputs of a finished pair (every query except an EPA-bound contact).
-NCG_DEV void write_outputs(const QueryParams& qp, const Outputs& o, uint32_t i, const GjkOut& r,
-                           vec3<float> init_dir, uint32_t status, uint32_t iters) {
-    switch (qp.query) {
-    case Q_CONTACT: {
-        ncg_contact c;
-        memset(&c, 0, sizeof(c));
-        uint8_t tag = 0;
-        if (r.kind == GJK_CLOSEST_POINTS) {
-            tag = 1;
-            wr3(c.world1, r.p1);
-            wr3(c.world2, r.p2);
-            wr3(c.normal, r.dir);
-            c.depth = (-dot(r.dir, r.p2 - r.p1)).h;
-        }
-        o.contact[i] = c;
-        o.tag[i] = tag;
-        if (o.dir) wr3(o.dir + 3 * (size_t)i, r.dir);
-        break;
-    }
-    case Q_DISTANCE:
-        o.value[i] = r.kind == GJK_CLOSEST_POINTS ? vnorm(r.p2 - r.p1).h : 0.0f;
-        break;
-    case Q_PROXIMITY: {
-        uint8_t t = r.kind == GJK_INTERSECTION ? NCG_INTERSECTING
-                    : r.kind == GJK_PROXIMITY  ? NCG_WITHIN_MARGIN
-                                               : NCG_DISJOINT;
-        o.tag[i] = t;
-        if (o.dir) {
-            float* d = o.dir + 3 * (size_t)i;
-            if (r.kind == GJK_INTERSECTION) { d[0] = init_dir.x; d[1] = init_dir.y; d[2] = init_dir.z; }
-            else wr3(d, r.dir);
-        }
-        break;
-    }
-    default: {
-        uint8_t t = r.kind == GJK_CLOSEST_POINTS ? NCG_CP_WITHIN_MARGIN
-                    : r.kind == GJK_NO_INTERSECTION ? NCG_CP_DISJOINT
-                                                    : NCG_CP_INTERSECTING;
-        o.tag[i] = t;
-        if (o.points) {
-            float* p = o.points + 6 * (size_t)i;
-            if (t == NCG_CP_WITHIN_MARGIN) { wr3(p, r.p1); wr3(p + 3, r.p2); }
-            else { for (int k = 0; k < 6; ++k) p[k] = 0.0f; }
-        }
-        break;
-    }
-    }
-    o.status[i] = status;
-    if (o.iters) o.iters[i] = iters;
-}
-
-// Writes a contact of the query::contact routes (explicit depth; the normal as
-// the returned direction, zeros when there is no contact).
-NCG_DEV void write_qcontact(const Outputs& o, uint32_t i, const QContact& q, uint32_t status, uint32_t iters) {
-    ncg_contact c;
-    memset(&c, 0, sizeof(c));
-    if (q.tag) {
-        wr3(c.world1, q.p1);
-        wr3(c.world2, q.p2);
-        wr3(c.normal, q.n);
-        c.depth = q.depth.h;
-    }
-    o.contact[i] = c;
-    o.tag[i] = (uint8_t)q.tag;
-    if (o.dir) wr3(o.dir + 3 * (size_t)i, q.n);
-    o.status[i] = status | q.status;
-    if (o.iters) o.iters[i] = iters;
-}
-
-// A pair with an invalid shape index or hull slice: no contact, distance 0,
-// Disjoint, and NCG_STATUS_BAD_INPUT (the reference would index out of bounds).
-NCG_DEV void write_bad(const QueryParams& qp, const Outputs& o, uint32_t i) {
-    GjkOut r;
-    r.kind = GJK_NO_INTERSECTION;
-    r.p1 = r.p2 = r.dir = zero3<real>();
-    write_outputs(qp, o, i, r, zero3<float>(), NCG_STATUS_BAD_INPUT, 0);
-}
-
-// First search direction of each *_with_params wrapper.  An all-zero
-// init_dir entry means None (no unit vector is zero): the default is used.
-NCG_DEV vec3<float> initial_dir(const QueryParams& qp, const ncg_batch& b, uint32_t i, const PairGeom& g) {
-    vec3<float> d;
-    float n;
-    vec3<float> given{0.0f, 0.0f, 0.0f};
-    bool has = false;
-    if (qp.use_init_dir && b.init_dir) {
-        const float* p = b.init_dir + 3 * (size_t)i;
-        given = {p[0], p[1], p[2]};
-        has = !(given.x == 0.0f && given.y == 0.0f && given.z == 0.0f);
-    }
-    if (qp.query == Q_CONTACT || qp.query == Q_PROXIMITY) {
-        if (has) return given;
-        if (try_normalize(g.m2.t - g.m1.t, qp.tol.init_eps, d, n)) return d;
-        return {1.0f, 0.0f, 0.0f};
-    }
-    vec3<float> d0 = has ? given : g.m1.t - g.m2.t;
-    if (try_normalize(d0, qp.tol.init_eps, d, n)) return d;
-    return {1.0f, 0.0f, 0.0f};
-}
-
-// Runs one pair through GJK; writes its outputs or its EPA work item.
-// All lanes of a warp call this with the same pair when Scan is WarpScan.
-// epa_queue: the EPA stage the pair starts in (0 = thread stage, 1 = warp tier A).
-// Writes an EPA work item (GJK's final simplex) and queues it for `queue`.
-NCG_DEV void enqueue_epa(const Scratch& s, uint32_t i, int queue, const Simplex& sx, uint32_t iters, uint32_t status,
-                         int mode, bool flip) {
-    unsigned long long slot = atomicAdd(&s.ctr->n_items, 1ull);
-    unsigned long long pos = atomicAdd(&s.ctr->epa_count[queue], 1ull);
-    s.queue[queue][pos] = (uint32_t)slot;
-    EpaItem& it = s.items[slot];
-    it.pair = i;
-    it.gjk_iters = iters;
-    it.status = status;
-    it.dim = (uint8_t)sx.dim;
-    it.mode = (uint8_t)mode;
-    it.flip = flip ? 1 : 0;
-    for (int k = 0; k <= sx.dim; ++k) {
-        const CSO& c = sx.v[k];
-        float* w = it.v[k];
-        w[0] = c.p.x; w[1] = c.p.y; w[2] = c.p.z;
-        w[3] = c.o1.x; w[4] = c.o1.y; w[5] = c.o1.z;
-        w[6] = c.o2.x; w[7] = c.o2.y; w[8] = c.o2.z;
-    }
-}
-
-// Runs one pair through GJK; writes its outputs or its EPA work item.
-// All lanes of a warp call this with the same pair when Scan is WarpScan.
-// epa_queue: the EPA stage the pair starts in (0 = thread stage, 1 = warp tier A).
-// Both GJK routes (the pair itself, or the point projection of a ball's centre
-// on a ConvexHull) share one inlined GJK loop to keep the kernel's code small.
-template <class Scan>
-NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, uint32_t i,
-                      const Scan& scan, bool writer, unsigned long long& iter_acc, int epa_queue) {
-    PairGeom g;
-    load_shape(b, b.g1[i], g.g1);
-    load_shape(b, b.g2[i], g.g2);
-    g.m1 = load_pose(b.m1 + i);
-    g.m2 = load_pose(b.m2 + i);
-    int mode = 0;  // 0: GJK on the pair; 1: point projection of a ball's centre on a hull
-    bool flip = false;
-    const real pred = from_host(qp.param);
-    vec3<float> d;
-    real max_dist;
-    bool exact;
-    if (qp.query == Q_CONTACT && qp.dispatch == NCG_DISPATCH_QUERY) {
-        const bool b1 = g.g1.kind == NCG_BALL, b2 = g.g2.kind == NCG_BALL;
-        const bool p1 = g.g1.kind == NCG_CUBOID || g.g1.kind == NCG_CONVEX_HULL;
-        const bool p2 = g.g2.kind == NCG_CUBOID || g.g2.kind == NCG_CONVEX_HULL;
-        if (b1 && b2) {
-            QContact q = contact_ball_ball(g.m1.t, g.g1.p0, g.m2.t, g.g2.p0, pred);
-            if (writer) write_qcontact(o, i, q, 0, 0);
-            return;
-        }
-        if ((b1 && p2) || (p1 && b2)) {
-            flip = !b1;
-            const Pose& pb = flip ? g.m2 : g.m1;
-            const Shape& sb = flip ? g.g2 : g.g1;
-            const Pose& pp = flip ? g.m1 : g.m2;
-            const Shape& sp = flip ? g.g1 : g.g2;
-            if (sp.kind == NCG_CUBOID) {
-                bool inside;
-                vec3<float> pr;
-                int fk, fi;
-                aabb_project_with_feature(pp, mk(sp.p0, sp.p1, sp.p2), pb.t, inside, pr, fk, fi);
-                QContact q = ball_polyhedron_assemble(pb.t, sb.p0, inside, to_r(pr), fk, fi, true, pred, flip);
-                if (writer) write_qcontact(o, i, q, 0, 0);
-                return;
-            }
-            // point_projection_on_support_map: GJK on the translated hull
-            mode = 1;
-        }
-    }
-    PairGeom gg = g;
-    if (mode == 1) {
-        gg = projection_geom(flip ? g.m1 : g.m2, flip ? g.g1 : g.g2, flip ? g.m2.t : g.m1.t);
-        float dn;
-        if (!try_normalize(-gg.m1.t, FLT_EPSILON, d, dn)) d = mk(1.0f, 0.0f, 0.0f);
-        max_dist = dw_max();
-        exact = true;
-    } else {
-        d = initial_dir(qp, b, i, g);
-        max_dist = qp.query == Q_DISTANCE ? dw_max() : pred;
-        exact = qp.query != Q_PROXIMITY;
-    }
-    Simplex sx;
-    sx.reset(cso_support(gg, d, scan));
-    uint32_t iters = 0, status = 0;
-    GjkOut r = gjk(gg, max_dist, exact, sx, qp.tol, scan, iters, status, qp.gjk_max_iter);
-    iter_acc += iters;
-    if (qp.query == Q_CONTACT && r.kind == GJK_INTERSECTION) {
-        if (writer) enqueue_epa(s, i, epa_queue, sx, iters, status, mode, flip);
-        return;
-    }
-    if (mode == 1) {
-        const Pose& pb = flip ? g.m2 : g.m1;
-        const Shape& sb = flip ? g.g2 : g.g1;
-        bool inside = r.kind != GJK_CLOSEST_POINTS;  // the iteration cap: unreachable!() in gjk.rs:57
-        vec3<real> w2 = inside ? to_r(pb.t) : r.p1 + to_r(pb.t);
-        QContact q = ball_polyhedron_assemble(pb.t, sb.p0, inside, w2, F_UNKNOWN, 0, false, pred, flip);
-        if (writer) write_qcontact(o, i, q, status, pack_iters(iters, 0));
-        return;
-    }
-    if (writer) write_outputs(qp, o, i, r, d, status, pack_iters(iters, 0));
-}
-
-// Validates every pair, writes the outputs of bad ones and counts the buckets.
-__global__ void k_classify(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int key = -1;
-    if (i < b.n_pairs) {
-        Shape a, c;
-        bool ok = load_shape(b, b.g1[i], a) && load_shape(b, b.g2[i], c);
-        if (!ok) write_bad(qp, o, (uint32_t)i);
-        else key = pair_bucket(a, c);
-        s.bucket[i] = key < 0 ? NO_BUCKET : (uint8_t)key;
-    }
-    (void)bucket_slot(s.ctr->bucket_n, key < 0 ? 0 : key, key >= 0);
-}
-
-// Scatters the pairs into `sorted`, bucket by bucket.
-__global__ void k_bucket(ncg_batch b, Scratch s) {
-    scatter_by_bucket(b.n_pairs, s.bucket, s.ctr->bucket_n, s.ctr->bucket_fill, s.sorted, &s.ctr->n_analytic,
-                      &s.ctr->n_hull);
-}
-
-NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31u) == 0 && v) atomicAdd(dst, v);
-}
-
-// One thread per pair over a pair list (list 0: analytic pairs, list 1:
-// ConvexHull pairs, whose points the thread scans itself); EPA starts in the
-// thread stage.
-__global__ void __launch_bounds__(128, NCG_GJK_THREAD_MIN_BLOCKS) k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list) {
-    const unsigned long long n = *(volatile unsigned long long*)(list == 0 ? &s.ctr->n_analytic : &s.ctr->n_hull);
-    const uint32_t* ids = list == 0 ? s.sorted : s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
-    ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
-    unsigned long long acc = 0;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    const unsigned long long start = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned long long rounds = (n + stride - 1) / stride;
-    for (unsigned long long r = 0; r < rounds; ++r) {
-        unsigned long long k = start + r * stride;
-        if (k < n) gjk_pair(b, qp, o, s, ids[k], scan, true, acc, 0);
-    }
-    warp_add(&s.ctr->gjk_iters, acc);
-}
-
-__global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
-    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->n_hull;
-    const uint32_t* ids = s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
-    WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
-    const unsigned lane = threadIdx.x & 31u;
-    unsigned long long acc = 0;
-    for (;;) {
-        unsigned long long k = 0;
-        if (lane == 0) k = atomicAdd(&s.ctr->hull_next, 1ull);
-        k = __shfl_sync(0xffffffffu, k, 0);
-        if (k >= n) break;
-        unsigned long long a = 0;
-        gjk_pair(b, qp, o, s, ids[k], scan, lane == 0, a, Q_WARP);
-        if (lane == 0) acc += a;
-    }
-    warp_add(&s.ctr->gjk_iters, acc);
 }
 
 // Writes a contact finished by EPA.
@@ -747,8 +402,7 @@ struct Limits {
 Limits launch_limits() {
     Limits l;
     cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<2>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_thread, k_gjk_thread, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_warp, k_gjk_warp, 128, 0);
+    gjk_occupancy(&l.occ_thread, &l.occ_warp);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_ethread, k_epa_thread, 128, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_global, k_epa, 32, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_smem[0], k_epa, 32, tier_bytes<1>());
@@ -764,8 +418,7 @@ Limits launch_limits() {
 // (their local-memory and hull traffic wants the largest L1).
 bool set_carveout(int pct) {
     bool ok = true;
-    ok &= cuda_ok(cudaFuncSetAttribute(k_gjk_thread, cudaFuncAttributePreferredSharedMemoryCarveout, pct),
-                  "carveout(k_gjk_thread)");
+    ok &= cuda_ok(gjk_set_carveout(pct), "carveout(k_gjk_thread)");
     ok &= cuda_ok(cudaFuncSetAttribute(k_epa_thread, cudaFuncAttributePreferredSharedMemoryCarveout, pct),
                   "carveout(k_epa_thread)");
     return ok;
@@ -799,7 +452,6 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
         cudaEventRecord(c->marks[c->n_marks++], st);
     };
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset counters")) return NCG_ECUDA;
-    unsigned n = (unsigned)b->n_pairs;
     if (c->warm == NCG_WARM_MLP && (query == Q_CONTACT || query == Q_PROXIMITY)) {
         // the network's start direction replaces the default one (contact and
         // proximity start from normalize(t2 - t1) in the reference)
@@ -813,14 +465,13 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
         launches += 2;
     }
     mark(-1);
-    k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
-    k_bucket<<<(n + 255) / 256, 256, 0, st>>>(bb, s);
+    gjk_launch_sort(bb, qp, o, s, st);
     mark(0);
     const int gjk_grid = c->num_sms * (c->gjk_blocks > 0 ? c->gjk_blocks : c->occ_thread);
-    k_gjk_thread<<<gjk_grid, 128, 0, st>>>(bb, qp, o, s, 0);
+    gjk_launch_thread(gjk_grid, bb, qp, o, s, 0, st);
     mark(1);
-    if (c->hull_gjk_warp) k_gjk_warp<<<c->num_sms * c->occ_warp, 128, 0, st>>>(bb, qp, o, s);
-    else k_gjk_thread<<<gjk_grid, 128, 0, st>>>(bb, qp, o, s, 1);
+    if (c->hull_gjk_warp) gjk_launch_warp(c->num_sms * c->occ_warp, bb, qp, o, s, st);
+    else gjk_launch_thread(gjk_grid, bb, qp, o, s, 1, st);
     mark(2);
     launches += 4;
     if (query == Q_CONTACT) {
@@ -1360,11 +1011,9 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
 
     // The array keeps the previous call's contents: reset the counters and queues' heads.
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset noalloc counters")) return NCG_ECUDA;
-    unsigned n = (unsigned)b->n_pairs;
-    k_classify<<<(n + 255) / 256, 256, 0, st>>>(bb, qp, o, s);
-    k_bucket<<<(n + 255) / 256, 256, 0, st>>>(bb, s);
-    k_gjk_thread<<<d.num_sms * d.lim.occ_thread, 128, 0, st>>>(bb, qp, o, s, 0);
-    k_gjk_thread<<<d.num_sms * d.lim.occ_thread, 128, 0, st>>>(bb, qp, o, s, 1);
+    gjk_launch_sort(bb, qp, o, s, st);
+    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 0, st);
+    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 1, st);
     k_epa_thread<<<d.num_sms * d.lim.occ_ethread, 128, 0, st>>>(bb, qp, o, s);
     // warp stages in shared memory (128, then 1280 vertices), then the one global slab
     k_epa<<<d.num_sms * d.lim.occ_smem[0], 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>(Q_WARP_LONG, Q_WARP, 3, -1));

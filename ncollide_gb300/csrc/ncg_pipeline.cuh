@@ -1,0 +1,191 @@
+// ncg_pipeline.cuh — types and output writers shared by the GJK stage
+// (ncg_gjk.cu) and the EPA stages and host code (ncg_kernels.cu) of one
+// batched query, and the GJK stage's host-side launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "ncg_core.cuh"
+#include "ncg_query.cuh"
+#include "ncg_sort.cuh"
+
+namespace ncg {
+
+enum QueryKind { Q_CONTACT = 0, Q_DISTANCE = 1, Q_PROXIMITY = 2, Q_CLOSEST = 3 };
+
+struct Outputs {
+    ncg_contact* contact;
+    uint8_t* tag;
+    float* dir;
+    float* value;
+    float* points;
+    uint32_t* status;
+    uint32_t* iters;
+};
+
+struct QueryParams {
+    int query;
+    int dispatch;  // ncg_dispatch (contact only)
+    int use_init_dir;
+    int gjk_max_iter;
+    int epa_max_iter;
+    dw_host param;  // prediction / margin
+    Tol tol;
+};
+
+// EPA work item: the pair and GJK's final simplex (dim + 1 CSO points).
+// `mode` 0: contact_support_map_support_map; 1: point projection of a ball's
+// centre on a ConvexHull (query::contact dispatch), `flip` when the ball is
+// the second shape.
+struct __align__(16) EpaItem {
+    uint32_t pair;
+    uint32_t gjk_iters;
+    uint32_t status;
+    uint8_t dim, mode, flip, pad;
+    float v[4][9];
+};
+
+// EPA queues: 0 the thread stage; 1 and 2 the first warp stage (1: pairs of two
+// curved shapes, whose polytopes grow longest, drained first; 2: the rest);
+// 3 and 4 the later warp stages.
+constexpr int N_EPA_QUEUES = 5;
+constexpr int Q_WARP_LONG = 1, Q_WARP = 2;
+
+struct DevCounters {
+    unsigned long long n_analytic, n_hull;
+    unsigned long long hull_next;
+    unsigned long long n_items;       // EPA work items written
+    unsigned long long epa_count[N_EPA_QUEUES];  // items per queue
+    unsigned long long epa_next[N_EPA_QUEUES];
+    unsigned long long gjk_iters, epa_iters;
+    uint32_t bucket_n[NB], bucket_fill[NB];
+    uint32_t mlp_err;  // bit 0: a learned warm-start tensor-core wait timed out
+};
+constexpr size_t CTR_SLOT = 512;
+static_assert(sizeof(DevCounters) <= CTR_SLOT, "counters must fit their slot");
+
+struct Scratch {
+    // Shape kinds of a pair's two shapes (validated by k_classify).
+    NCG_DEV uint32_t bucket_kind1(const ncg_batch& b, uint32_t i) const { return __ldg(&b.shapes[b.g1[i]].kind); }
+    NCG_DEV uint32_t bucket_kind2(const ncg_batch& b, uint32_t i) const { return __ldg(&b.shapes[b.g2[i]].kind); }
+    uint8_t* bucket;  // per pair: its cost bucket, NO_BUCKET for bad input
+    uint32_t* sorted;  // pair indices by bucket: analytic pairs, then hull pairs
+    uint32_t* queue[N_EPA_QUEUES];  // item indices per EPA stage
+    EpaItem* items;
+    DevCounters* ctr;
+    char* slabs[2];  // global EPA stores of the warp stages that use them, one per block
+    size_t slab_bytes[2];
+    int n_slabs[2];
+};
+
+NCG_DEV uint32_t pack_iters(uint32_t g, uint32_t e) { return (g > 0xffffu ? 0xffffu : g) | ((e > 0xffffu ? 0xffffu : e) << 16); }
+
+// Results leave the device as the high word of each double-word.
+NCG_DEV void wr3(float* p, vec3<real> v) {
+    p[0] = v.x.h;
+    p[1] = v.y.h;
+    p[2] = v.z.h;
+}
+
+// Writes the outputs of a finished pair (every query except an EPA-bound contact).
+NCG_DEV void write_outputs(const QueryParams& qp, const Outputs& o, uint32_t i, const GjkOut& r,
+                           vec3<float> init_dir, uint32_t status, uint32_t iters) {
+    switch (qp.query) {
+    case Q_CONTACT: {
+        ncg_contact c;
+        memset(&c, 0, sizeof(c));
+        uint8_t tag = 0;
+        if (r.kind == GJK_CLOSEST_POINTS) {
+            tag = 1;
+            wr3(c.world1, r.p1);
+            wr3(c.world2, r.p2);
+            wr3(c.normal, r.dir);
+            c.depth = (-dot(r.dir, r.p2 - r.p1)).h;
+        }
+        o.contact[i] = c;
+        o.tag[i] = tag;
+        if (o.dir) wr3(o.dir + 3 * (size_t)i, r.dir);
+        break;
+    }
+    case Q_DISTANCE:
+        o.value[i] = r.kind == GJK_CLOSEST_POINTS ? vnorm(r.p2 - r.p1).h : 0.0f;
+        break;
+    case Q_PROXIMITY: {
+        uint8_t t = r.kind == GJK_INTERSECTION ? NCG_INTERSECTING
+                    : r.kind == GJK_PROXIMITY  ? NCG_WITHIN_MARGIN
+                                               : NCG_DISJOINT;
+        o.tag[i] = t;
+        if (o.dir) {
+            float* d = o.dir + 3 * (size_t)i;
+            if (r.kind == GJK_INTERSECTION) { d[0] = init_dir.x; d[1] = init_dir.y; d[2] = init_dir.z; }
+            else wr3(d, r.dir);
+        }
+        break;
+    }
+    default: {
+        uint8_t t = r.kind == GJK_CLOSEST_POINTS ? NCG_CP_WITHIN_MARGIN
+                    : r.kind == GJK_NO_INTERSECTION ? NCG_CP_DISJOINT
+                                                    : NCG_CP_INTERSECTING;
+        o.tag[i] = t;
+        if (o.points) {
+            float* p = o.points + 6 * (size_t)i;
+            if (t == NCG_CP_WITHIN_MARGIN) { wr3(p, r.p1); wr3(p + 3, r.p2); }
+            else { for (int k = 0; k < 6; ++k) p[k] = 0.0f; }
+        }
+        break;
+    }
+    }
+    o.status[i] = status;
+    if (o.iters) o.iters[i] = iters;
+}
+
+// Writes a contact of the query::contact routes (explicit depth; the normal as
+// the returned direction, zeros when there is no contact).
+NCG_DEV void write_qcontact(const Outputs& o, uint32_t i, const QContact& q, uint32_t status, uint32_t iters) {
+    ncg_contact c;
+    memset(&c, 0, sizeof(c));
+    if (q.tag) {
+        wr3(c.world1, q.p1);
+        wr3(c.world2, q.p2);
+        wr3(c.normal, q.n);
+        c.depth = q.depth.h;
+    }
+    o.contact[i] = c;
+    o.tag[i] = (uint8_t)q.tag;
+    if (o.dir) wr3(o.dir + 3 * (size_t)i, q.n);
+    o.status[i] = status | q.status;
+    if (o.iters) o.iters[i] = iters;
+}
+
+// A pair with an invalid shape index or hull slice: no contact, distance 0,
+// Disjoint, and NCG_STATUS_BAD_INPUT (the reference would index out of bounds).
+NCG_DEV void write_bad(const QueryParams& qp, const Outputs& o, uint32_t i) {
+    GjkOut r;
+    r.kind = GJK_NO_INTERSECTION;
+    r.p1 = r.p2 = r.dir = zero3<real>();
+    write_outputs(qp, o, i, r, zero3<float>(), NCG_STATUS_BAD_INPUT, 0);
+}
+
+NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31u) == 0 && v) atomicAdd(dst, v);
+}
+
+// ---- GJK stage (ncg_gjk.cu) -------------------------------------------------
+// Validates the pairs, writes the outputs of bad ones and counting-sorts the
+// rest into s.sorted (k_classify, k_bucket): two launches over n pairs.
+void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, cudaStream_t st);
+// One thread per pair over list 0 (analytic pairs) or 1 (ConvexHull pairs).
+void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
+                       int list, cudaStream_t st);
+// One warp per pair over the ConvexHull list.
+void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
+                     cudaStream_t st);
+// Resident 128-thread blocks per SM of the thread and warp GJK kernels.
+void gjk_occupancy(int* occ_thread, int* occ_warp);
+// Shared-memory carveout preference of the thread GJK kernel.
+cudaError_t gjk_set_carveout(int pct);
+
+}  // namespace ncg

@@ -1,6 +1,10 @@
 // ncg_toi.cu — batched linear time of impact: query::time_of_impact for the
 // support-map shapes of this library (time_of_impact.rs:63-90), one thread per
-// pair.  The arithmetic is in ncg_toi.cuh.
+// pair.  The arithmetic is in ncg_toi.cuh.  As in the GJK stage, the
+// double-word sum, quotient and square root are kept out of line (the loop is
+// bound by instruction fetch).
+#define NCG_DW_OUTLINE 1
+
 #include <cuda_runtime.h>
 
 #include <cfloat>
