@@ -558,6 +558,56 @@ def time_of_impact_report(args, local, tolerance, dispatch):
                 [float(np.percentile(rel32, 50)), float(np.percentile(rel32, 99))] if rel32.size else None}
 
 
+def ray_cast_report(args, local, tolerance):
+    """RayCast::toi_and_normal_with_ray (GJK ray cast) for 2^20 rays
+    (ray_casts, seed 9; solid): GPU throughput with inputs resident, the CPU
+    reference path (oracle, f32) on a 65,536-ray sample with every host core,
+    and agreement with f64."""
+    import torch
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import workloads as W
+    from oracle import oracle as O
+    n = args.ray_count
+    b, rays = W.ray_casts(n, seed=9)
+    dev = f"cuda:{local}"
+    db = Q.DeviceBatch.from_host(b, device=dev)
+    tr = torch.from_numpy(rays).to(dev)
+    ctx = Q.Context(local, tolerance=tolerance)
+    for _ in range(3):
+        o = Q.ray_cast_batch(ctx, db, tr, with_iters=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        o = Q.ray_cast_batch(ctx, db, tr, with_iters=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    hit = o["has_hit"].cpu().numpy()
+    toi = o["toi"].cpu().numpy()
+    iters = o["iters"].cpu().numpy()
+    ctx.close()
+    sample = min(65536, n)
+    idx = np.arange(sample)
+    sb = b.subset(idx)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    r32 = O.ray_cast(sb, rays[idx], O.F32, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    r64 = O.ray_cast(sb, rays[idx], O.F64, threads=threads)
+    m = (hit[idx] == 1) & (r64["hit"] == 1)
+    rel = np.abs(toi[idx][m] - r64["toi"][m]) / np.maximum(np.abs(r64["toi"][m]), 1e-30)
+    return {"workload": f"ray_casts {n} rays, seed 9, solid, max_toi inf", "rays_per_s": n / (ms / 1e3),
+            "ms_per_step": ms, "hit_fraction": float(hit.mean()),
+            "ray_cast_iters_per_ray": float(iters.astype(np.float64).mean()),
+            "cpu_reference_path_rays_per_s": sample / cpu_s, "cpu_cores": threads,
+            "cpu_sample": f"first {sample} rays, f32 reference path (oracle)",
+            "hit_mismatch_vs_f64": int((hit[idx] != r64["hit"]).sum()),
+            "hit_mismatch_f32_reference_vs_f64": int((r32["hit"] != r64["hit"]).sum()),
+            "toi_rel_err_vs_f64_p50_p99": [float(np.percentile(rel, 50)), float(np.percentile(rel, 99))] if rel.size else None}
+
+
 def cpu_baseline(batch, threads, query):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -620,8 +670,9 @@ def main():
     ap.add_argument("--no-mlp", action="store_true")
     ap.add_argument("--stress-pairs", type=int, default=1 << 20)
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the precision-stress, cuboid and time-of-impact reports")
+                    help="skip the precision-stress, cuboid, time-of-impact and ray-cast reports")
     ap.add_argument("--toi-pairs", type=int, default=1 << 20, help="sweeps of the time-of-impact report")
+    ap.add_argument("--ray-count", type=int, default=1 << 20, help="rays of the ray-cast report")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profiling: stop after the timed device steps (no second dispatch, no e2e, no report)")
     args = ap.parse_args()
@@ -802,11 +853,12 @@ def main():
         out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
         acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs), qo)
 
-    stress = cuboids = toi_rep = None
+    stress = cuboids = toi_rep = ray_rep = None
     if not args.no_extras:
         stress = precision_stress(args, local, args.tolerance)
         cuboids = cuboid_small(args, local, args.tolerance)
         toi_rep = time_of_impact_report(args, local, args.tolerance, args.dispatch)
+        ray_rep = ray_cast_report(args, local, args.tolerance)
     learned = mlp_params = None
     if not args.no_mlp:
         mlp_params, learned = learned_warm_start(args, local, args.tolerance, args.dispatch, db, batch)
@@ -825,7 +877,7 @@ def main():
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc, "warm_start_coherent": coherent,
             "warm_start_learned": learned,
-            "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep,
+            "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep, "ray_cast": ray_rep,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
             "epa": {"pairs": stats["n_epa"], "warp_stage_pairs": stats["n_epa_overflow"],

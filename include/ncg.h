@@ -16,6 +16,7 @@
  *   closest    src/query/closest_points/closest_points_support_map_support_map.rs:9-67
  *   toi        src/query/time_of_impact/time_of_impact.rs:63-90,
  *              src/query/time_of_impact/time_of_impact_support_map_support_map.rs:10-127
+ *   ray cast   src/query/ray/ray_support_map.rs:14-110, src/query/algorithms/gjk.rs:180-194
  * The per-pair arithmetic is gjk::closest_points (src/query/algorithms/gjk.rs:76-177)
  * with VoronoiSimplex (voronoi_simplex3.rs) and EPA (epa3.rs:219-454).
  */
@@ -303,6 +304,19 @@ int ncg_time_of_impact_batch(ncg_ctx* ctx, const ncg_batch* batch, const float* 
                              const float* vel2, float max_toi, float target_distance,
                              ncg_toi* out, uint8_t* has_toi, uint32_t* status,
                              uint32_t* iters, void* stream);
+
+/* RayCast::toi_and_normal_with_ray of support-map shapes for every ray
+ * (src/query/ray/ray_support_map.rs:14-56 and its RayCast impls :58-110,
+ * gjk::cast_ray src/query/algorithms/gjk.rs:180-194): ray i against
+ * shapes[g1[i]] at pose m1[i] (m2, g2 and init_dir unused).  rays: origin[3],
+ * dir[3] per ray, world frame; the toi is in units of |dir|.  Every shape kind
+ * takes the GJK ray cast (the reference's Ball and Cuboid have analytic
+ * RayCast impls of their own).  solid = 0: a ray starting inside returns its
+ * exit.  out_normal nullable (3 floats per ray, world frame).  Returns
+ * NCG_EINVAL when max_toi is negative or NaN. */
+int ncg_ray_cast_batch(ncg_ctx* ctx, const ncg_batch* batch, const float* rays, float max_toi,
+                       int solid, float* out_toi, float* out_normal, uint8_t* has_hit,
+                       uint32_t* status, uint32_t* iters, void* stream);
 
 /* ---- the same on host memory (synchronous; copies in and out) -------------- */
 int ncg_contact_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float prediction,

@@ -793,6 +793,41 @@ int ncg_time_of_impact_batch(ncg_ctx* c, const ncg_batch* b, const float* vel1, 
     return NCG_OK;
 }
 
+int ncg_ray_cast_batch(ncg_ctx* c, const ncg_batch* b, const float* rays, float max_toi, int solid, float* out_toi,
+                       float* out_normal, uint8_t* has_hit, uint32_t* status, uint32_t* iters, void* stream) {
+    if (!(max_toi >= 0.0f)) {
+        g_last_error = "max_toi must be >= 0";
+        return NCG_EINVAL;
+    }
+    if (!c || !b) { g_last_error = "null context or batch"; return NCG_EINVAL; }
+    if (b->n_pairs == 0) return NCG_OK;
+    if (b->n_pairs > 0xffffffffull) { g_last_error = "more than 2^32-1 rays"; return NCG_EINVAL; }
+    if (!b->shapes || !b->m1 || !b->g1 || !rays || !out_toi || !has_hit || !status) {
+        g_last_error = "null required pointer";
+        return NCG_EINVAL;
+    }
+    if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    if (!ensure_scratch(c, b->n_pairs)) return NCG_ENOMEM;
+    const Scratch s = carve_scratch(c);
+    const Tol tol = make_tol(c->tol_mode);
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset counters")) return NCG_ECUDA;
+    uint32_t launches = 0;
+    int rc = ray_launch(*b, tol, rays, max_toi, solid, out_toi, out_normal, has_hit, status, iters,
+                        ToiScratch{s.bucket, s.sorted, s.items, reinterpret_cast<char*>(s.items) + 512,
+                                   &s.ctr->gjk_iters},
+                        c->num_sms, st, &launches);
+    if (rc != NCG_OK) return rc;
+    if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st),
+                 "copy counters"))
+        return NCG_ECUDA;
+    c->launches = launches;
+    c->graph_launches = launches;
+    c->last = ncg_stats{};
+    c->last.n_pairs = b->n_pairs;
+    return NCG_OK;
+}
+
 }  // extern "C"
 
 // ------------------------------------------------------------------ host-memory entry points

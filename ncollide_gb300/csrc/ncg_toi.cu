@@ -164,6 +164,79 @@ k_toi_refine(ncg_batch b, Tol tol, ToiArgs a, const ToiCounters* ctr, const Refi
     if ((threadIdx.x & 31u) == 0 && acc) atomicAdd(iter_sum, acc);
 }
 
+struct RayArgs {
+    const float* rays;  // origin[3], dir[3] per ray (world)
+    dw_host max_toi;
+    int solid;
+    int max_iter;
+    float* toi;
+    float* normal;  // nullable
+    uint8_t* hit;
+    uint32_t* status;
+    uint32_t* iters;  // nullable
+};
+
+NCG_DEV void write_ray(const RayArgs& a, uint64_t i, const RayResult& r, uint32_t status, uint32_t iters) {
+    a.toi[i] = r.hit ? float(r.toi) : 0.0f;
+    if (a.normal) {
+        float* n = a.normal + 3 * i;
+        n[0] = r.normal.x;
+        n[1] = r.normal.y;
+        n[2] = r.normal.z;
+    }
+    a.hit[i] = r.hit ? 1 : 0;
+    a.status[i] = status;
+    if (a.iters) a.iters[i] = iters;
+}
+
+// Validates every ray's shape, writes the outputs of bad ones and counts the
+// buckets (the shape's kind, or its hull size).
+__global__ void k_ray_classify(ncg_batch b, RayArgs a, uint8_t* bucket, ToiCounters* ctr) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int key = -1;
+    if (i < b.n_pairs) {
+        Shape s1;
+        if (load_shape(b, b.g1[i], s1)) {
+            const Shape ball{NCG_BALL, 0, 0, 0.0f, 0.0f, 0.0f};
+            key = pair_bucket(ball, s1);
+        } else {
+            RayResult r;
+            r.hit = false;
+            r.normal = zero3<float>();
+            write_ray(a, i, r, NCG_STATUS_BAD_INPUT, 0);
+        }
+        bucket[i] = key < 0 ? NO_BUCKET : (uint8_t)key;
+    }
+    (void)bucket_slot(ctr->bucket_n, key < 0 ? 0 : key, key >= 0);
+}
+
+// One thread per ray over the sorted rays (ConvexHull shapes first).
+__global__ void __launch_bounds__(128, NCG_TOI_MIN_BLOCKS)
+k_ray(ncg_batch b, Tol tol, RayArgs a, const uint32_t* sorted, const ToiCounters* ctr, unsigned long long* iter_sum) {
+    const ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
+    const unsigned long long na = *(volatile const unsigned long long*)&ctr->n_analytic;
+    const unsigned long long nh = *(volatile const unsigned long long*)&ctr->n_hull;
+    const unsigned long long n = na + nh;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    unsigned long long acc = 0;
+    for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const uint32_t i = sorted[k < nh ? na + k : k - nh];
+        Shape s1;
+        load_shape(b, b.g1[i], s1);
+        const Pose m = load_pose(b.m1 + i);
+        const float* r6 = a.rays + 6 * (size_t)i;
+        const vec3<float> ro{__ldg(r6), __ldg(r6 + 1), __ldg(r6 + 2)};
+        const vec3<float> rd{__ldg(r6 + 3), __ldg(r6 + 4), __ldg(r6 + 5)};
+        uint32_t status = 0, iters = 0;
+        const RayResult r = ray_cast_support_map(m, s1, ro, rd, from_host(a.max_toi), a.solid != 0, tol, scan, iters,
+                                                 status, a.max_iter);
+        write_ray(a, i, r, status, iters);
+        acc += iters;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31u) == 0 && acc) atomicAdd(iter_sum, acc);
+}
+
 }  // namespace
 
 int toi_launch(const ncg_batch& b, const Tol& tol, int dispatch, const float* vel1, const float* vel2,
@@ -202,6 +275,40 @@ int toi_launch(const ncg_batch& b, const Tol& tol, int dispatch, const float* ve
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_last_error(std::string("TOI kernel launch: ") + cudaGetErrorString(e));
+        return NCG_ECUDA;
+    }
+    return NCG_OK;
+}
+
+int ray_launch(const ncg_batch& b, const Tol& tol, const float* rays, float max_toi, int solid, float* out_toi,
+               float* out_normal, uint8_t* hit, uint32_t* status, uint32_t* iters, const ToiScratch& scratch,
+               int num_sms, cudaStream_t st, uint32_t* launches) {
+    RayArgs a;
+    a.rays = rays;
+    a.max_toi = max_toi >= FLT_MAX ? dw_host{FLT_MAX, 0.0f} : dw_split((double)max_toi);
+    a.solid = solid;
+    a.max_iter = 10000;
+    a.toi = out_toi;
+    a.normal = out_normal;
+    a.hit = hit;
+    a.status = status;
+    a.iters = iters;
+    ToiCounters* ctr = static_cast<ToiCounters*>(scratch.ctr);
+    cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(ToiCounters), st);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("memset ray counters: ") + cudaGetErrorString(e));
+        return NCG_ECUDA;
+    }
+    const unsigned blocks = (unsigned)((b.n_pairs + 255) / 256);
+    k_ray_classify<<<blocks, 256, 0, st>>>(b, a, scratch.bucket, ctr);
+    k_toi_bucket<<<blocks, 256, 0, st>>>(b, scratch.bucket, scratch.sorted, ctr);
+    const uint64_t need = (b.n_pairs + 127) / 128;
+    const uint64_t cap = (uint64_t)num_sms * NCG_TOI_MIN_BLOCKS;
+    k_ray<<<(unsigned)(need < cap ? need : cap), 128, 0, st>>>(b, tol, a, scratch.sorted, ctr, scratch.iter_sum);
+    *launches += 3;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_last_error(std::string("ray-cast kernel launch: ") + cudaGetErrorString(e));
         return NCG_ECUDA;
     }
     return NCG_OK;

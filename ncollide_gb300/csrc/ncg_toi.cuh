@@ -14,6 +14,8 @@
 //   src/query/time_of_impact/time_of_impact_support_map_support_map.rs:10-127
 //   src/query/time_of_impact/time_of_impact_ball_ball.rs:9-62, src/query/ray/ray_ball.rs:77-121
 //   src/query/time_of_impact/time_of_impact.rs:63-90 (Ball-Ball dispatch)
+//   src/query/ray/ray_support_map.rs:14-56 and the RayCast impls :58-110,
+//   src/query/algorithms/gjk.rs:180-194 (cast_ray)  ray casts on support maps
 #pragma once
 
 #include "ncg_core.cuh"
@@ -80,14 +82,15 @@ struct RayHit {
     vec3<real> normal;
 };
 
-// minkowski_ray_cast of the ray (origin 0, ray_dir, max_toi = the largest
-// float) against m1 * g1 - m2 * g2.  `iters` counts loop entries.  The loop is
+// minkowski_ray_cast of the ray (origin0, ray_dir) against m1 * g1 - m2 * g2
+// (None past max_toi).  `iters` counts loop entries.  The loop is
 // rotated so that the support mapping and the simplex sub-solve each have a
 // single call site (the first pass takes the reference's initial support
 // point and simplex reset): inlined twice they overflow the instruction cache.
 template <class Scan>
-NCG_DEV RayHit minkowski_ray_cast(const PairGeom& g, float radius, bool dilated, vec3<real> ray_dir, Simplex& sx,
-                                  const Tol& tol, const Scan& scan, uint32_t& iters, uint32_t& status, int max_iter) {
+NCG_DEV RayHit minkowski_ray_cast(const PairGeom& g, float radius, bool dilated, vec3<float> origin0,
+                                  vec3<real> ray_dir, real max_toi, Simplex& sx, const Tol& tol, const Scan& scan,
+                                  uint32_t& iters, uint32_t& status, int max_iter) {
     RayHit out;
     out.hit = false;
     out.toi = real(0.0f);
@@ -96,7 +99,7 @@ NCG_DEV RayHit minkowski_ray_cast(const PairGeom& g, float radius, bool dilated,
     const real ray_length = vnorm(ray_dir);
     if (ray_length <= eps) return out;
     real ltoi = real(0.0f);
-    vec3<float> origin = zero3<float>();
+    vec3<float> origin = origin0;
     const vec3<real> rdir = ray_dir / ray_length;
     vec3<real> dir = -rdir;
     vec3<real> ldir = dir;
@@ -123,7 +126,7 @@ NCG_DEV RayHit minkowski_ray_cast(const PairGeom& g, float radius, bool dilated,
                     // a new lower bound: the ray origin moves
                     ldir = dir;
                     ltoi = ltoi + t;
-                    if (ltoi / ray_length > dw_max()) return out;
+                    if (ltoi / ray_length > max_toi) return out;
                     const vec3<float> shift = to_f(rdir * t);
                     origin = origin + shift;
                     max_bound = dw_max();
@@ -184,7 +187,8 @@ NCG_DEV ToiResult toi_support_map(const PairGeom& g, vec3<float> vel1, vec3<floa
     const vec3<float> dvel = vel2 - vel1;
     const bool dilated = target != 0.0f;
     Simplex sx;
-    RayHit rc = minkowski_ray_cast(g, target, dilated, to_r(dvel), sx, tol, scan, iters, status, max_iter);
+    RayHit rc = minkowski_ray_cast(g, target, dilated, zero3<float>(), to_r(dvel), dw_max(), sx, tol, scan, iters,
+                                   status, max_iter);
     if (!rc.hit) return o;
     // directional_distance: the witness points are the simplex's unless the toi is zero
     vec3<real> w1 = zero3<real>(), w2 = zero3<real>();
@@ -300,6 +304,67 @@ NCG_DEV ToiResult toi_ball_ball(const Pose& m1, vec3<float> vel1, float r1, cons
     o.w2 = qrot_inv(m2.q, to_f(w2));
     o.n1 = qrot_inv(m1.q, to_f(n1));
     o.n2 = qrot_inv(m2.q, to_f(n2));
+    return o;
+}
+
+// RayCast::toi_and_normal_with_ray of a support-map shape: the ray in the
+// shape's local frame, gjk::cast_ray against (identity, g) - (identity,
+// ConstantOrigin); with solid false and the origin inside, a second cast
+// backwards from beyond the shape (the support distance along the ray +
+// 0.001).  The normal is rotated back into the world frame.
+struct RayResult {
+    bool hit;
+    real toi;
+    vec3<float> normal;
+};
+
+template <class Scan>
+NCG_DEV RayResult ray_cast_support_map(const Pose& m, const Shape& s, vec3<float> ro, vec3<float> rd, real max_toi,
+                                       bool solid, const Tol& tol, const Scan& scan, uint32_t& iters,
+                                       uint32_t& status, int max_iter) {
+    RayResult o;
+    o.hit = false;
+    o.toi = real(0.0f);
+    o.normal = zero3<float>();
+    PairGeom g;
+    g.m1 = Pose{make_float4(0.0f, 0.0f, 0.0f, 1.0f), zero3<float>()};
+    g.g1 = s;
+    g.m2 = g.m1;
+    g.g2 = Shape{KIND_CONSTANT_ORIGIN, 0, 0, 0.0f, 0.0f, 0.0f};
+    const vec3<float> lo = qrot_inv(m.q, ro - m.t);
+    const vec3<float> ld = qrot_inv(m.q, rd);
+    Simplex sx;
+    // at most two casts; the second starts beyond the shape, looking back
+    vec3<float> origin = lo, dir = ld;
+    real cast_max = max_toi;
+    float shift = 0.0f;
+    for (int pass = 0; pass < 2; ++pass) {
+        RayHit rc = minkowski_ray_cast(g, 0.0f, false, origin, to_r(dir), cast_max, sx, tol, scan, iters, status,
+                                       max_iter);
+        if (!rc.hit) return o;
+        if (pass == 1) {
+            const real toi = real(shift) - rc.toi;
+            if (!(toi <= max_toi)) return o;
+            o.hit = true;
+            o.toi = toi;
+            o.normal = qrot(m.q, to_f(rc.normal));
+            return o;
+        }
+        if (solid || !(rc.toi == real(0.0f))) {
+            o.hit = true;
+            o.toi = rc.toi;
+            o.normal = qrot(m.q, to_f(rc.normal));
+            return o;
+        }
+        // the ray starts inside the shape
+        const vec3<float> ndir = ld / vnorm(ld);
+        const vec3<float> supp = support_point(g.m1, s, ndir, scan);
+        const float eps = 0.001f;
+        shift = dot(supp - lo, ndir) + eps;
+        origin = lo + ndir * shift;
+        dir = -ld;
+        cast_max = real(shift + eps);
+    }
     return o;
 }
 

@@ -1,5 +1,5 @@
 // ncg_toi.h — internal interface between the C ABI (ncg_kernels.cu) and the
-// time-of-impact kernel (ncg_toi.cu).
+// time-of-impact and ray-cast kernels (ncg_toi.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,5 +28,11 @@ struct ToiScratch {
 int toi_launch(const ncg_batch& b, const Tol& tol, int dispatch, const float* vel1, const float* vel2,
                float max_toi, float target_distance, ncg_toi* out, uint8_t* has_toi, uint32_t* status,
                uint32_t* iters, const ToiScratch& scratch, int num_sms, cudaStream_t st, uint32_t* launches);
+
+// Launches the ray-cast kernels over every ray of the batch (ray i against
+// shapes[g1[i]] at m1[i]; m2, g2 unused; arguments validated by the caller).
+int ray_launch(const ncg_batch& b, const Tol& tol, const float* rays, float max_toi, int solid, float* out_toi,
+               float* out_normal, uint8_t* hit, uint32_t* status, uint32_t* iters, const ToiScratch& scratch,
+               int num_sms, cudaStream_t st, uint32_t* launches);
 
 }  // namespace ncg

@@ -279,6 +279,29 @@ def time_of_impact_batch(ctx: Context, db: DeviceBatch, vel1, vel2, max_toi=floa
             "status": status, "iters": iters, "_keep": (vel1, vel2)}
 
 
+def ray_cast_batch(ctx: Context, db: DeviceBatch, rays, max_toi=float("inf"), solid=True, with_normal=True,
+                   with_iters=False, stream=None):
+    """RayCast::toi_and_normal_with_ray (GJK ray cast) for every ray: ray i
+    against shape g1[i] at pose m1[i]; rays [N,6] float32 device tensor
+    (origin, dir; world frame).  Returns has_hit, toi, normal (world), status
+    and, with with_iters, the ray-cast iterations."""
+    n, dev = db.n_pairs, db.m1.device
+    rays = rays.to(dev, torch.float32).contiguous()
+    if n and tuple(rays.shape) != (n, 6):
+        raise ValueError("rays must be [n, 6]")
+    out = {"has_hit": _empty(n, (), torch.uint8, dev), "toi": _empty(n, (), torch.float32, dev),
+           "normal": _empty(n, (3,), torch.float32, dev) if with_normal else None,
+           "status": _empty(n, (), torch.int32, dev),
+           "iters": _empty(n, (), torch.int32, dev) if with_iters else None}
+    cb = db.c_struct()
+    N.check(ctx._L.ncg_ray_cast_batch(ctx.handle, ctypes.byref(cb), _ptr(rays), ctypes.c_float(max_toi),
+                                      int(bool(solid)), _ptr(out["toi"]), _ptr(out["normal"]), _ptr(out["has_hit"]),
+                                      _ptr(out["status"]), _ptr(out["iters"]), _stream(stream)),
+            "ncg_ray_cast_batch")
+    out["_keep"] = rays
+    return out
+
+
 def _host_struct(b: PairBatch, keep):
     arrs = {"shapes": np.ascontiguousarray(b.shapes), "hull": np.ascontiguousarray(b.hull_points, np.float32),
             "m1": np.ascontiguousarray(b.m1, np.float32), "g1": np.ascontiguousarray(b.g1, np.uint32),

@@ -240,3 +240,32 @@ def toi_sweeps(n=1 << 20, seed=7, kinds=MIXED_KINDS, hull_n=(8, 1024), dmax=3.0,
     vel1 = (aim * speed).astype(np.float32)
     vel2 = (random_unit_vectors(rng, n) * speed * 0.1).astype(np.float32)
     return b, vel1, vel2
+
+
+def ray_casts(n=1 << 20, seed=9, kinds=(BALL, CUBOID, CAPSULE, CONE, CYLINDER, CONVEX_HULL), hull_n=(8, 1024),
+              inside=0.1, cone_deg=20.0):
+    """Rays against single shapes: shape i at a random pose, the ray starting
+    at 1.5 to 4 circumradii from its centre (a fraction `inside` of the rays
+    start at the centre) and aimed at the centre within a cone of half-angle
+    cone_deg; |dir| in [0.5, 2].  Returns (batch, rays [n,6]); the batch's m2/g2
+    repeat m1/g1 and are unused."""
+    rng = np.random.default_rng(seed)
+    shapes, pts = random_shapes(rng, n, kinds=kinds, hull_n=hull_n)
+    radii = _circumradius(shapes, pts)
+    m1 = np.zeros((n, 8), np.float32)
+    m1[:, :4] = random_unit_quaternions(rng, n)
+    m1[:, 4:7] = rng.uniform(-1.0, 1.0, (n, 3))
+    g1 = np.arange(n, dtype=np.uint32)
+    u = random_unit_vectors(rng, n)
+    dist = rng.uniform(1.5, 4.0, (n, 1)) * radii[:, None]
+    dist[rng.uniform(0.0, 1.0, n) < inside] = 0.0
+    origin = m1[:, 4:7].astype(np.float64) + u * dist
+    jitter = random_unit_vectors(rng, n)
+    jitter -= (jitter * u).sum(1, keepdims=True) * u
+    jitter /= np.maximum(np.linalg.norm(jitter, axis=1, keepdims=True), 1e-30)
+    ang = np.radians(cone_deg) * np.sqrt(rng.uniform(0.0, 1.0, (n, 1)))
+    aim = -u * np.cos(ang) + jitter * np.sin(ang)
+    rays = np.concatenate([origin, aim * rng.uniform(0.5, 2.0, (n, 1))], 1).astype(np.float32)
+    b = PairBatch(shapes, np.ascontiguousarray(pts), m1, g1, m1.copy(), g1.copy(), scale=radii,
+                  meta={"workload": "ray_casts", "n": n, "seed": seed})
+    return b, rays

@@ -12,6 +12,8 @@
 //   src/query/time_of_impact/time_of_impact_support_map_support_map.rs:10-127
 //   src/query/time_of_impact/time_of_impact_ball_ball.rs:9-62, query/ray/ray_ball.rs:77-121
 //   src/query/time_of_impact/time_of_impact.rs:63-90 (Ball-Ball dispatch)
+//   src/query/ray/ray_support_map.rs:14-56 and the RayCast impls :58-110,
+//   src/query/algorithms/gjk.rs:180-194 (cast_ray)  ray casts on support maps
 #pragma once
 
 #include "ncg_oracle.hpp"
@@ -78,18 +80,18 @@ template <class S> struct RayCastOut {
     V3<S> normal;
 };
 
-// minkowski_ray_cast (gjk.rs:226-345) of the ray (origin 0, ray_dir) against
+// minkowski_ray_cast (gjk.rs:226-345) of the ray (ray_origin, ray_dir) against
 // m1 * g1 - m2 * g2.  The ray origin and the simplex points move in N (the
 // CSO point arithmetic); the bounds, the ray parameter and the direction in S.
 template <class N, class S>
 RayCastOut<S> minkowski_ray_cast(const Iso<N>& m1, const Shape<N>& g1, N radius, bool dilated, const Iso<N>& m2,
-                                 const Shape<N>& g2, V3<S> ray_dir, S max_toi, VoronoiSimplex<N, S>& simplex,
-                                 const Tol<S>& tol, Counters* cnt) {
+                                 const Shape<N>& g2, V3<N> ray_origin, V3<S> ray_dir, S max_toi,
+                                 VoronoiSimplex<N, S>& simplex, const Tol<S>& tol, Counters* cnt) {
     RayCastOut<S> out;
     const S ray_length = norm(ray_dir);
     if (ray_length <= tol.eps) return out;  // relative_eq!(ray_length, 0) (a norm is >= 0)
     S ltoi = S(0);
-    V3<N> origin = zero3<N>();
+    V3<N> origin = ray_origin;
     const V3<S> rdir = ray_dir / ray_length;
     V3<S> dir = -rdir;
     V3<S> ldir = dir;
@@ -163,7 +165,7 @@ TOIOut<S> toi_support_map(const Iso<N>& m1, V3<N> vel1, const Shape<N>& g1, cons
     const V3<N> dvel = vel2 - vel1;
     const bool dilated = target_distance != N(0);
     VoronoiSimplex<N, S> simplex;
-    RayCastOut<S> rc = minkowski_ray_cast(m1, g1, target_distance, dilated, m2, g2, cvt<S>(dvel),
+    RayCastOut<S> rc = minkowski_ray_cast(m1, g1, target_distance, dilated, m2, g2, zero3<N>(), cvt<S>(dvel),
                                           std::numeric_limits<S>::max(), simplex, tol, cnt);
     if (!rc.hit) return o;
     // directional_distance (gjk.rs:196-224): witnesses unless the toi is zero
@@ -263,6 +265,54 @@ TOIOut<S> toi_ball_ball(const Iso<N>& m1, V3<N> vel1, N r1, const Iso<N>& m2, V3
     o.w2 = cvt<S>(inverse_transform_vector(m2, cvt<N>(w2)));
     o.n1 = cvt<S>(inverse_transform_vector(m1, cvt<N>(n1)));
     o.n2 = cvt<S>(inverse_transform_vector(m2, cvt<N>(n2)));
+    return o;
+}
+
+template <class S> struct RayOut {
+    bool hit = false;
+    S toi = S(0);
+    V3<S> normal;  // world frame
+};
+
+// RayCast::toi_and_normal_with_ray of a support-map shape (the impls of
+// ray_support_map.rs:58-110): the ray in the shape's local frame,
+// ray_intersection_with_support_map_with_params (:14-56) = gjk::cast_ray
+// (gjk.rs:180-194), i.e. the ray cast against (identity, g) - (identity,
+// ConstantOrigin); with solid = false and the origin inside the shape, a
+// second cast backwards from beyond the shape (shift = the support distance
+// along the ray + 0.001).  The normal is rotated back into the world frame.
+// The ray parameters are in S, the ray origin and the shift in N.
+template <class N, class S>
+RayOut<S> ray_cast_support_map(const Iso<N>& m, const Shape<N>& g, V3<N> ray_origin, V3<N> ray_dir, S max_toi,
+                               bool solid, const Tol<S>& tol, Counters* cnt) {
+    RayOut<S> o;
+    const Iso<N> id{Quat<N>{N(0), N(0), N(0), N(1)}, zero3<N>()};
+    Shape<N> origin{};
+    origin.kind = CONSTANT_ORIGIN;
+    const V3<N> lo = inverse_transform_vector(m, ray_origin - m.t);
+    const V3<N> ld = inverse_transform_vector(m, ray_dir);
+    VoronoiSimplex<N, S> simplex;
+    RayCastOut<S> rc = minkowski_ray_cast(id, g, N(0), false, id, origin, lo, cvt<S>(ld), max_toi, simplex, tol, cnt);
+    if (!rc.hit) return o;
+    S toi = rc.toi;
+    V3<S> normal = rc.normal;
+    if (!solid && toi == S(0)) {
+        // the ray starts inside the shape
+        const V3<N> ndir = ld / norm(ld);
+        const V3<N> supp = support_point(id, g, ndir, cnt);
+        const N eps = N(0.001);
+        const N shift = dot(supp - lo, ndir) + eps;
+        const V3<N> no = lo + ndir * shift;
+        RayCastOut<S> rc2 =
+            minkowski_ray_cast(id, g, N(0), false, id, origin, no, cvt<S>(-ld), S(shift + eps), simplex, tol, cnt);
+        if (!rc2.hit) return o;
+        toi = S(shift) - rc2.toi;
+        if (!(toi <= max_toi)) return o;
+        normal = rc2.normal;
+    }
+    o.hit = true;
+    o.toi = toi;
+    o.normal = cvt<S>(rotate(m.q, cvt<N>(normal)));
     return o;
 }
 

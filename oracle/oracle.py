@@ -51,6 +51,8 @@ def lib():
         L.ncgo_toi.argtypes = [i32, i32, f64, f64, f64, i32, vp, u32, vp, u64, u64, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                vp]
         L.ncgo_toi.restype = i32
+        L.ncgo_ray_cast.argtypes = [i32, f64, i32, f64, i32, vp, u32, vp, u64, u64, vp, vp, vp, vp, vp, vp, vp]
+        L.ncgo_ray_cast.restype = i32
         L.ncgo_simplex_kat.restype = i32
         _lib = L
     return _lib
@@ -192,3 +194,28 @@ def toi(batch, vel1, vel2, policy=F32, dispatch=0, max_toi=float("inf"), target_
     return {"toi": out[:, 0], "witness1": out[:, 1:4], "witness2": out[:, 4:7], "normal1": out[:, 7:10],
             "normal2": out[:, 10:13], "status": out[:, 13].astype(np.int32), "some": tag, "gjk_status": status,
             "iters": counters[:, 0]}
+
+
+
+def ray_cast(batch, rays, policy=F32, max_toi=float("inf"), solid=True, eps=0.0, threads=None):
+    """Ray casts on support maps (RayCast::toi_and_normal_with_ray via the GJK
+    ray cast): ray i against shapes[g1[i]] at pose m1[i]; rays [N,6] = origin,
+    dir (world).  Returns a dict with hit, toi, normal (world), status, iters."""
+    L = lib()
+    n = batch.n_pairs
+    threads = threads if threads is not None else (os.cpu_count() or 1)
+    out = np.zeros((n, 16), np.float64)
+    tag = np.zeros(n, np.uint8)
+    status = np.zeros(n, np.uint32)
+    counters = np.zeros((n, 8), np.uint32)
+    shapes = np.ascontiguousarray(batch.shapes)
+    pts = np.ascontiguousarray(batch.hull_points, np.float32)
+    m1 = np.ascontiguousarray(batch.m1, np.float32)
+    g1 = np.ascontiguousarray(batch.g1, np.uint32)
+    ry = np.ascontiguousarray(rays, np.float32).reshape(n, 6)
+    mt = float(np.finfo(np.float32).max) if not np.isfinite(max_toi) else float(max_toi)
+    rc = L.ncgo_ray_cast(policy, mt, int(bool(solid)), float(eps), int(threads), _p(shapes), len(shapes), _p(pts),
+                         pts.shape[0], n, _p(m1), _p(g1), _p(ry), _p(out), _p(tag), _p(status), _p(counters))
+    if rc != 0:
+        raise ValueError(f"oracle rejected the call (rc={rc})")
+    return {"hit": tag, "toi": out[:, 0], "normal": out[:, 1:4], "status": status, "iters": counters[:, 0]}

@@ -260,9 +260,87 @@ int toi_run(const InF32& in, const float* vel1, const float* vel2, uint64_t n, i
     return 0;
 }
 
+template <class N, class S>
+void ray_range(const InF32& in, const float* rays, S max_toi, bool solid, const Tol<S>& tol, uint64_t lo, uint64_t hi,
+               const Outs& o) {
+    for (uint64_t i = lo; i < hi; ++i) {
+        Counters cnt;
+        Shape<N> s1;
+        RayOut<S> r;
+        if (!load_shape<N>(in, in.g1[i], &s1)) {
+            cnt.status |= ST_BAD_INPUT;
+        } else {
+            const Iso<N> m = pose1<N>(in, i);
+            const float* ry = rays + 6 * i;
+            r = ray_cast_support_map<N, S>(m, s1, V3<N>{N(ry[0]), N(ry[1]), N(ry[2])},
+                                           V3<N>{N(ry[3]), N(ry[4]), N(ry[5])}, max_toi, solid, tol, &cnt);
+        }
+        if (o.out16) {
+            double* w = o.out16 + 16 * i;
+            for (int k = 0; k < 16; ++k) w[k] = 0.0;
+            if (r.hit) {
+                w[0] = double(r.toi);
+                w[1] = double(r.normal.x);
+                w[2] = double(r.normal.y);
+                w[3] = double(r.normal.z);
+            }
+        }
+        if (o.tag) o.tag[i] = r.hit ? 1 : 0;
+        if (o.status) o.status[i] = cnt.status;
+        if (o.counters8) {
+            uint32_t* c = o.counters8 + 8 * i;
+            for (int k = 0; k < 8; ++k) c[k] = 0;
+            c[0] = cnt.gjk_iters;
+            c[2] = cnt.support_calls;
+            c[3] = cnt.hull_points_scanned;
+        }
+    }
+}
+
+template <class N, class S>
+int ray_run(const InF32& in, const float* rays, uint64_t n, double max_toi, int solid, double eps, int nt,
+            const Outs& o) {
+    double e = eps > 0 ? eps : (double)std::numeric_limits<N>::epsilon();
+    Tol<S> tol = eps < 0 ? make_tol_precise<S>(0.0) : make_tol<S>(e, 0.0);
+    S mt = max_toi >= (double)std::numeric_limits<float>::max() ? std::numeric_limits<S>::max() : S(max_toi);
+    if (nt <= 1 || n < 64) {
+        ray_range<N, S>(in, rays, mt, solid != 0, tol, 0, n, o);
+        return 0;
+    }
+    std::vector<std::thread> th;
+    uint64_t chunk = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t) {
+        uint64_t lo = t * chunk, hi = std::min<uint64_t>(n, lo + chunk);
+        if (lo >= hi) break;
+        th.emplace_back([&, lo, hi] { ray_range<N, S>(in, rays, mt, solid != 0, tol, lo, hi, o); });
+    }
+    for (auto& x : th) x.join();
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Ray casts on support maps (RayCast::toi_and_normal_with_ray through
+// ray_intersection_with_support_map_with_params): ray i hits the shape
+// shapes[g1[i]] at pose m1[i]; rays: origin[3], dir[3] per ray (world).
+// out16: toi, normal[3] (world); tag 1 = hit.  counters8[0] = ray-cast
+// iterations (both casts when solid = 0 and the origin is inside).
+int ncgo_ray_cast(int policy, double max_toi, int solid, double eps, int n_threads, const ncg_shape* shapes,
+                  uint32_t n_shapes, const float* hull_points, uint64_t n_hull_points, uint64_t n_rays,
+                  const ncg_pose* m1, const uint32_t* g1, const float* rays, double* out16, uint8_t* tag,
+                  uint32_t* status, uint32_t* counters8) {
+    if (!(max_toi >= 0.0)) return NCG_EINVAL;
+    InF32 in{shapes, n_shapes, hull_points, n_hull_points, m1, g1, nullptr, nullptr, nullptr};
+    Outs o{out16, tag, status, counters8};
+    switch (policy) {
+    case POLICY_F32: return ray_run<float, float>(in, rays, n_rays, max_toi, solid, eps, n_threads, o);
+    case POLICY_F64: return ray_run<double, double>(in, rays, n_rays, max_toi, solid, eps, n_threads, o);
+    case POLICY_MIXED: return ray_run<float, dw>(in, rays, n_rays, max_toi, solid, eps, n_threads, o);
+    default: return NCG_EINVAL;
+    }
+}
 
 // Linear time of impact (time_of_impact_support_map_support_map; with
 // dispatch 1 Ball-Ball pairs take time_of_impact_ball_ball as

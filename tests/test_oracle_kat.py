@@ -164,3 +164,45 @@ def test_time_of_impact_still_objects():
     for pol in (O.F32, O.MIXED):
         r = O.toi(b, v1, np.zeros_like(v1), pol, dispatch=1)
         assert [bool(x) for x in r["some"]] == [cs["some"] for cs in k["cases"]]
+
+
+def _ray_batch(shape_list):
+    from ncollide_gb300 import shapes as S
+    shp = np.zeros(len(shape_list), S.SHAPE_DTYPE)
+    for i, (kind, prm) in enumerate(shape_list):
+        shp[i]["kind"] = kind
+        shp[i]["p"] = list(prm) + [0.0] * (4 - len(prm))
+    m = np.zeros((len(shape_list), 8), np.float32)
+    m[:, 3] = 1.0
+    g = np.arange(len(shape_list), dtype=np.uint32)
+    return S.PairBatch(shp, np.zeros((1, 4), np.float32), m, g, m, g)
+
+
+def test_solid_ray_cast_example():
+    k = GOLD["solid_ray_cast3d"]
+    b = _ray_batch([(1, k["half_extents"])])
+    for cs in k["cases"]:
+        rays = np.array([cs["origin"] + cs["dir"]], np.float32)
+        for pol in (O.F32, O.F64, O.MIXED):
+            r = O.ray_cast(b, rays, pol, solid=cs["solid"])
+            if cs["toi"] is None:
+                assert r["hit"][0] == 0
+            else:
+                assert r["hit"][0] == 1 and abs(r["toi"][0] - cs["toi"]) <= 1e-6 * max(1.0, cs["toi"])
+                if cs["toi"] > 0:  # exit through the +y face
+                    assert np.allclose(r["normal"][0], [0.0, 1.0, 0.0], atol=1e-6)
+
+
+def test_ray_cast_support_maps_analytic_answers():
+    # unit cuboid, unit ball, capsule (half height 1, radius 0.5) along y
+    b = _ray_batch([(1, (1, 1, 1)), (0, (1,)), (2, (1, 0.5)), (1, (1, 1, 1))])
+    rays = np.array([[-5, 0, 0, 1, 0, 0], [-5, 0, 0, 2, 0, 0], [0, -5, 0, 0, 1, 0], [-5, 0, 0, 0, 0, 0]], np.float32)
+    for pol in (O.F64, O.MIXED):
+        r = O.ray_cast(b, rays, pol)
+        assert list(r["hit"]) == [1, 1, 1, 0]
+        assert np.allclose(r["toi"][:3], [4.0, 2.0, 3.5], atol=1e-6)
+        assert np.allclose(r["normal"][0], [-1, 0, 0], atol=1e-6)
+        assert np.allclose(r["normal"][1], [-1, 0, 0], atol=1e-6)
+        assert np.allclose(r["normal"][2], [0, -1, 0], atol=1e-6)
+        r = O.ray_cast(b, rays, pol, max_toi=3.0)
+        assert list(r["hit"]) == [0, 1, 0, 0]
