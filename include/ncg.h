@@ -17,6 +17,7 @@
  *   toi        src/query/time_of_impact/time_of_impact.rs:63-90,
  *              src/query/time_of_impact/time_of_impact_support_map_support_map.rs:10-127
  *   ray cast   src/query/ray/ray_support_map.rs:14-110, src/query/algorithms/gjk.rs:180-194
+ *   aabb       src/bounding_volume/aabb_*.rs; broad phase src/pipeline/broad_phase/dbvt_broad_phase.rs
  * The per-pair arithmetic is gjk::closest_points (src/query/algorithms/gjk.rs:76-177)
  * with VoronoiSimplex (voronoi_simplex3.rs) and EPA (epa3.rs:219-454).
  */
@@ -317,6 +318,36 @@ int ncg_time_of_impact_batch(ncg_ctx* ctx, const ncg_batch* batch, const float* 
 int ncg_ray_cast_batch(ncg_ctx* ctx, const ncg_batch* batch, const float* rays, float max_toi,
                        int solid, float* out_toi, float* out_normal, uint8_t* has_hit,
                        uint32_t* status, uint32_t* iters, void* stream);
+
+/* ---- bounding volumes and the broad phase ----------------------------------
+ * ncg_aabb_batch: HasBoundingVolume<AABB>::bounding_volume of shapes[g1[i]] at
+ * m1[i] for every entry (src/bounding_volume/aabb_ball.rs, aabb_cuboid.rs,
+ * aabb_support_map.rs, aabb_convex.rs, aabb_utils.rs:8-74); out_aabbs: mins[3],
+ * maxs[3] per entry (device); a bad shape gets NaN bounds and
+ * NCG_STATUS_BAD_INPUT.  m2, g2, init_dir unused.
+ *
+ * ncg_broad_phase: DBVTBroadPhase (src/pipeline/broad_phase/dbvt_broad_phase.rs)
+ * over proxies 0 .. n-1.  ncg_bp_update(boxes) = deferred_set_bounding_volume
+ * for every proxy (:322-347: a stored box that does not contain the new one is
+ * replaced by new.loosened(margin)) followed by update (:174-258).  The pair
+ * set is every intersecting pair of stored boxes; started / stopped are the
+ * pairs that entered / left it (interference_started / _stopped).  Pairs are
+ * (lower id, higher id) uint32 pairs sorted lexicographically, in device
+ * memory owned by the broad phase and valid until its next update.  The proxy
+ * count may grow between updates, not shrink: a proxy with a NaN bound has no
+ * pairs (remove).  Every pair is allowed (no is_interference_allowed filter).
+ * ncg_bp_update synchronises the stream. */
+typedef struct ncg_broad_phase ncg_broad_phase;
+int ncg_aabb_batch(ncg_ctx* ctx, const ncg_batch* batch, float* out_aabbs, uint32_t* status,
+                   void* stream);
+int ncg_bp_create(ncg_ctx* ctx, float margin, ncg_broad_phase** out);
+int ncg_bp_update(ncg_broad_phase* bp, const float* aabbs, uint32_t n_proxies, void* stream);
+int ncg_bp_results(ncg_broad_phase* bp, uint64_t* n_pairs, uint64_t* n_started, uint64_t* n_stopped,
+                   const uint32_t** pairs, const uint32_t** started, const uint32_t** stopped);
+/* Copies the last update's pairs / started / stopped (2 uint32 each) into
+ * caller buffers (device or host; NULL skips one), asynchronously on stream. */
+int ncg_bp_copy(ncg_broad_phase* bp, uint32_t* pairs, uint32_t* started, uint32_t* stopped, void* stream);
+int ncg_bp_destroy(ncg_broad_phase* bp);
 
 /* ---- the same on host memory (synchronous; copies in and out) -------------- */
 int ncg_contact_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float prediction,

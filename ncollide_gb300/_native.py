@@ -34,7 +34,8 @@ EXPORTED = [
     "ncg_ctx_set_dispatch", "ncg_ctx_set_tuning", "ncg_contact_graph_create", "ncg_graph_launch",
     "ncg_graph_destroy", "ncg_mlp_n_params", "ncg_ctx_set_mlp_params", "ncg_mlp_features", "ncg_mlp_infer",
     "ncg_mlp_grad", "ncg_mlp_adam", "ncg_time_of_impact_batch",
-    "ncg_ray_cast_batch",
+    "ncg_ray_cast_batch", "ncg_aabb_batch", "ncg_bp_create", "ncg_bp_update", "ncg_bp_results",
+    "ncg_bp_destroy", "ncg_bp_copy",
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
 TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT = range(4)
@@ -100,6 +101,13 @@ def load(build_if_missing=True):
     L.ncg_ctx_set_tuning.argtypes = [vp, i32, i32]
     L.ncg_time_of_impact_batch.argtypes = [vp, P(NcgBatch), vp, vp, f32, f32, vp, vp, vp, vp, vp]
     L.ncg_ray_cast_batch.argtypes = [vp, P(NcgBatch), vp, f32, i32, vp, vp, vp, vp, vp, vp]
+    L.ncg_aabb_batch.argtypes = [vp, P(NcgBatch), vp, vp, vp]
+    L.ncg_bp_create.argtypes = [vp, f32, P(vp)]
+    L.ncg_bp_update.argtypes = [vp, vp, ctypes.c_uint32, vp]
+    L.ncg_bp_results.argtypes = [vp, P(ctypes.c_uint64), P(ctypes.c_uint64), P(ctypes.c_uint64), P(vp), P(vp),
+                                 P(vp)]
+    L.ncg_bp_destroy.argtypes = [vp]
+    L.ncg_bp_copy.argtypes = [vp, vp, vp, vp, vp]
     L.ncg_contact_graph_create.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp, vp, P(vp)]
     L.ncg_graph_launch.argtypes = [vp, vp]
     L.ncg_graph_destroy.argtypes = [vp]

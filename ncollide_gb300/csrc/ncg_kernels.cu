@@ -36,6 +36,7 @@
 #include "ncg_core.cuh"
 #include "ncg_mlp.h"
 #include "ncg_toi.h"
+#include "ncg_bp.h"
 #include "ncg_epa.cuh"
 #include "ncg_query.cuh"
 #include "ncg_pipeline.cuh"
@@ -825,6 +826,67 @@ int ncg_ray_cast_batch(ncg_ctx* c, const ncg_batch* b, const float* rays, float 
     c->graph_launches = launches;
     c->last = ncg_stats{};
     c->last.n_pairs = b->n_pairs;
+    return NCG_OK;
+}
+
+int ncg_aabb_batch(ncg_ctx* c, const ncg_batch* b, float* out_aabbs, uint32_t* status, void* stream) {
+    if (!c || !b) { g_last_error = "null context or batch"; return NCG_EINVAL; }
+    if (b->n_pairs == 0) return NCG_OK;
+    if (!b->shapes || !b->m1 || !b->g1 || !out_aabbs) { g_last_error = "null required pointer"; return NCG_EINVAL; }
+    if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    int rc = aabb_launch(*b, out_aabbs, status, c->num_sms, (cudaStream_t)stream);
+    if (rc == NCG_OK) c->launches = 1;
+    return rc;
+}
+
+struct ncg_broad_phase {
+    ncg::BroadPhaseState* s;
+};
+
+int ncg_bp_create(ncg_ctx* c, float margin, ncg_broad_phase** out) {
+    if (!c || !out) { g_last_error = "null context or output"; return NCG_EINVAL; }
+    if (!(margin >= 0.0f)) { g_last_error = "The loosening margin must be positive."; return NCG_EINVAL; }
+    if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    ncg::BroadPhaseState* s = nullptr;
+    int rc = ncg::bp_create(margin, c->device, &s);
+    if (rc != NCG_OK) return rc;
+    *out = new ncg_broad_phase{s};
+    return NCG_OK;
+}
+
+int ncg_bp_update(ncg_broad_phase* bp, const float* aabbs, uint32_t n, void* stream) {
+    if (!bp) { g_last_error = "null broad phase"; return NCG_EINVAL; }
+    if (n > 0 && !aabbs) { g_last_error = "null boxes"; return NCG_EINVAL; }
+    if (n > (1u << 30)) { g_last_error = "more than 2^30 proxies"; return NCG_EINVAL; }
+    return ncg::bp_update(bp->s, aabbs, n, (cudaStream_t)stream);
+}
+
+int ncg_bp_results(ncg_broad_phase* bp, uint64_t* n_pairs, uint64_t* n_started, uint64_t* n_stopped,
+                   const uint32_t** pairs, const uint32_t** started, const uint32_t** stopped) {
+    if (!bp) { g_last_error = "null broad phase"; return NCG_EINVAL; }
+    ncg::bp_results(bp->s, n_pairs, n_started, n_stopped, pairs, started, stopped);
+    return NCG_OK;
+}
+
+int ncg_bp_copy(ncg_broad_phase* bp, uint32_t* pairs, uint32_t* started, uint32_t* stopped, void* stream) {
+    if (!bp) { g_last_error = "null broad phase"; return NCG_EINVAL; }
+    uint64_t n[3];
+    const uint32_t* src[3];
+    ncg::bp_results(bp->s, &n[0], &n[1], &n[2], &src[0], &src[1], &src[2]);
+    uint32_t* dst[3] = {pairs, started, stopped};
+    for (int k = 0; k < 3; ++k) {
+        if (!dst[k] || n[k] == 0) continue;
+        if (!cuda_ok(cudaMemcpyAsync(dst[k], src[k], 8 * n[k], cudaMemcpyDefault, (cudaStream_t)stream),
+                     "ncg_bp_copy"))
+            return NCG_ECUDA;
+    }
+    return NCG_OK;
+}
+
+int ncg_bp_destroy(ncg_broad_phase* bp) {
+    if (!bp) return NCG_OK;
+    ncg::bp_destroy(bp->s);
+    delete bp;
     return NCG_OK;
 }
 

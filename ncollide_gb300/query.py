@@ -302,6 +302,55 @@ def ray_cast_batch(ctx: Context, db: DeviceBatch, rays, max_toi=float("inf"), so
     return out
 
 
+def aabb_batch(ctx: Context, db: DeviceBatch, stream=None):
+    """World AABBs [N,6] (mins, maxs) of shape g1[i] at pose m1[i], and status."""
+    n, dev = db.n_pairs, db.m1.device
+    out = _empty(n, (6,), torch.float32, dev)
+    status = _empty(n, (), torch.int32, dev)
+    cb = db.c_struct()
+    N.check(ctx._L.ncg_aabb_batch(ctx.handle, ctypes.byref(cb), _ptr(out), _ptr(status), _stream(stream)),
+            "ncg_aabb_batch")
+    return out, status
+
+
+class BroadPhase:
+    """DBVTBroadPhase over proxies 0..n-1 on the device: update(boxes) stores
+    each box (loosened by `margin` when it left its stored box) and returns
+    (pairs, started, stopped) as int64 [k,2] device tensors sorted by
+    (lower id, higher id)."""
+
+    def __init__(self, ctx: Context, margin):
+        self._L = ctx._L
+        self._ctx = ctx
+        self._p = ctypes.c_void_p()
+        N.check(self._L.ncg_bp_create(ctx.handle, ctypes.c_float(margin), ctypes.byref(self._p)), "ncg_bp_create")
+        self.device = torch.device("cuda", ctx.device)
+
+    def update(self, boxes, stream=None):
+        boxes = boxes.to(self.device, torch.float32).contiguous()
+        n = boxes.shape[0]
+        N.check(self._L.ncg_bp_update(self._p, _ptr(boxes) if n else None, n, _stream(stream)), "ncg_bp_update")
+        counts = [ctypes.c_uint64() for _ in range(3)]
+        ptrs = [ctypes.c_void_p() for _ in range(3)]
+        N.check(self._L.ncg_bp_results(self._p, *[ctypes.byref(c) for c in counts], *[ctypes.byref(p) for p in ptrs]),
+                "ncg_bp_results")
+        bufs = [torch.empty((int(c.value), 2), dtype=torch.int32, device=self.device) for c in counts]
+        N.check(self._L.ncg_bp_copy(self._p, *[_ptr(b) if b.numel() else None for b in bufs], _stream(stream)),
+                "ncg_bp_copy")
+        return tuple(b.to(torch.int64) & 0xffffffff for b in bufs)
+
+    def close(self):
+        if self._p:
+            self._L.ncg_bp_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _host_struct(b: PairBatch, keep):
     arrs = {"shapes": np.ascontiguousarray(b.shapes), "hull": np.ascontiguousarray(b.hull_points, np.float32),
             "m1": np.ascontiguousarray(b.m1, np.float32), "g1": np.ascontiguousarray(b.g1, np.uint32),

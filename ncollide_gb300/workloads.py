@@ -269,3 +269,23 @@ def ray_casts(n=1 << 20, seed=9, kinds=(BALL, CUBOID, CAPSULE, CONE, CYLINDER, C
     b = PairBatch(shapes, np.ascontiguousarray(pts), m1, g1, m1.copy(), g1.copy(), scale=radii,
                   meta={"workload": "ray_casts", "n": n, "seed": seed})
     return b, rays
+
+
+def scene_objects(n=1 << 20, seed=11, kinds=(BALL, CUBOID, CAPSULE, CONE, CYLINDER, CONVEX_HULL),
+                  hull_n=(8, 256), overlaps=4.0):
+    """A scene for the broad phase: n shapes with the mixed size distribution
+    at uniform random poses in a cube sized so that an object's AABB meets
+    about `overlaps` others.  Returns a batch whose pair i is object i alone
+    (m1, g1 = its pose and shape; m2, g2 repeat them, unused)."""
+    rng = np.random.default_rng(seed)
+    shapes, pts = random_shapes(rng, n, kinds=kinds, hull_n=hull_n)
+    radii = _circumradius(shapes, pts)
+    # boxes of side ~2r: a pair overlaps when centres are within ~(r_a + r_b) per axis
+    mean_side = float(np.mean(2.0 * radii))
+    side = (n * (2.0 * mean_side) ** 3 / max(overlaps, 1e-6)) ** (1.0 / 3.0)
+    m1 = np.zeros((n, 8), np.float32)
+    m1[:, :4] = random_unit_quaternions(rng, n)
+    m1[:, 4:7] = rng.uniform(-side / 2, side / 2, (n, 3))
+    g1 = np.arange(n, dtype=np.uint32)
+    return PairBatch(shapes, np.ascontiguousarray(pts), m1, g1, m1.copy(), g1.copy(), scale=radii,
+                     meta={"workload": "scene_objects", "n": n, "seed": seed, "side": side})

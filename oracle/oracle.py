@@ -28,7 +28,8 @@ _lib = None
 
 def build(force=False):
     """Compiles the oracle with the committed Makefile (g++ only)."""
-    srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "ncg_oracle.hpp", "ncg_oracle_toi.hpp", "dw.hpp")]
+    srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "ncg_oracle.hpp", "ncg_oracle_toi.hpp",
+                                            "ncg_oracle_bp.hpp", "dw.hpp")]
     if not force and os.path.exists(LIB_PATH):
         if os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
             return LIB_PATH
@@ -53,6 +54,10 @@ def lib():
         L.ncgo_toi.restype = i32
         L.ncgo_ray_cast.argtypes = [i32, f64, i32, f64, i32, vp, u32, vp, u64, u64, vp, vp, vp, vp, vp, vp, vp]
         L.ncgo_ray_cast.restype = i32
+        L.ncgo_aabb.argtypes = [vp, u32, vp, u64, u64, vp, vp, vp, vp]
+        L.ncgo_aabb.restype = i32
+        L.ncgo_pairs.argtypes = [vp, u32, vp, u64]
+        L.ncgo_pairs.restype = ctypes.c_int64
         L.ncgo_simplex_kat.restype = i32
         _lib = L
     return _lib
@@ -219,3 +224,61 @@ def ray_cast(batch, rays, policy=F32, max_toi=float("inf"), solid=True, eps=0.0,
     if rc != 0:
         raise ValueError(f"oracle rejected the call (rc={rc})")
     return {"hit": tag, "toi": out[:, 0], "normal": out[:, 1:4], "status": status, "iters": counters[:, 0]}
+
+
+def aabbs(batch):
+    """World AABBs [N,6] (mins, maxs) of shapes[g1[i]] at m1[i], and status."""
+    L = lib()
+    n = batch.n_pairs
+    out = np.zeros((n, 6), np.float32)
+    status = np.zeros(n, np.uint32)
+    shapes = np.ascontiguousarray(batch.shapes)
+    pts = np.ascontiguousarray(batch.hull_points, np.float32)
+    m1 = np.ascontiguousarray(batch.m1, np.float32)
+    g1 = np.ascontiguousarray(batch.g1, np.uint32)
+    L.ncgo_aabb(_p(shapes), len(shapes), _p(pts), pts.shape[0], n, _p(m1), _p(g1), _p(out), _p(status))
+    return out, status
+
+
+def intersecting_pairs(boxes):
+    """Sorted uint64 keys (lo << 32 | hi) of every intersecting pair of boxes [N,6]."""
+    L = lib()
+    b = np.ascontiguousarray(boxes, np.float32).reshape(-1, 6)
+    cap = 1 << 16
+    while True:
+        out = np.zeros(cap, np.uint64)
+        k = L.ncgo_pairs(_p(b), b.shape[0], _p(out), cap)
+        if k <= cap:
+            return out[:k]
+        cap = int(k)
+
+
+class BroadPhase:
+    """The pair set and events of DBVTBroadPhase.update (dbvt_broad_phase.rs:174-258):
+    a proxy's stored box is replaced by new_box.loosened(margin) when the stored
+    box does not contain the new one (deferred_set_bounding_volume, :322-347);
+    the pairs are the intersecting pairs of the stored boxes; started / stopped
+    are the pairs that entered / left the set.  A proxy whose box has a NaN
+    bound has no pairs (removed)."""
+
+    def __init__(self, margin):
+        self.margin = np.float32(margin)
+        self.stored = np.zeros((0, 6), np.float32)
+        self.pairs = np.zeros(0, np.uint64)
+
+    def update(self, boxes):
+        b = np.asarray(boxes, np.float32).reshape(-1, 6)
+        n_old = self.stored.shape[0]
+        st = np.full((b.shape[0], 6), np.nan, np.float32)
+        st[:n_old] = self.stored[:b.shape[0]]
+        with np.errstate(invalid="ignore"):
+            contains = (st[:, :3] <= b[:, :3]).all(1) & (st[:, 3:] >= b[:, 3:]).all(1)
+        new = ~contains
+        st[new, :3] = b[new, :3] + (-self.margin)
+        st[new, 3:] = b[new, 3:] + self.margin
+        self.stored = st
+        pairs = intersecting_pairs(st)
+        started = np.setdiff1d(pairs, self.pairs)
+        stopped = np.setdiff1d(self.pairs, pairs)
+        self.pairs = pairs
+        return pairs, started, stopped

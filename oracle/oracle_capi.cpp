@@ -9,6 +9,7 @@
 #include "../include/ncg.h"
 #include "ncg_oracle.hpp"
 #include "ncg_oracle_toi.hpp"
+#include "ncg_oracle_bp.hpp"
 
 using namespace ncgo;
 
@@ -340,6 +341,43 @@ int ncgo_ray_cast(int policy, double max_toi, int solid, double eps, int n_threa
     case POLICY_MIXED: return ray_run<float, dw>(in, rays, n_rays, max_toi, solid, eps, n_threads, o);
     default: return NCG_EINVAL;
     }
+}
+
+// World AABBs of shapes[g1[i]] at m1[i] (HasBoundingVolume<AABB>::bounding_volume):
+// out6 = mins[3], maxs[3] per entry; status ST_BAD_INPUT (and NaN boxes) for a bad shape.
+int ncgo_aabb(const ncg_shape* shapes, uint32_t n_shapes, const float* hull_points, uint64_t n_hull_points,
+              uint64_t n, const ncg_pose* m1, const uint32_t* g1, float* out6, uint32_t* status) {
+    InF32 in{shapes, n_shapes, hull_points, n_hull_points, m1, g1, nullptr, nullptr, nullptr};
+    for (uint64_t i = 0; i < n; ++i) {
+        Shape<float> s;
+        float* o = out6 + 6 * i;
+        if (!load_shape<float>(in, in.g1[i], &s)) {
+            for (int k = 0; k < 6; ++k) o[k] = std::numeric_limits<float>::quiet_NaN();
+            if (status) status[i] = ST_BAD_INPUT;
+            continue;
+        }
+        const AABB b = shape_aabb(pose1<float>(in, i), s);
+        for (int d = 0; d < 3; ++d) {
+            o[d] = b.mins[d];
+            o[3 + d] = b.maxs[d];
+        }
+        if (status) status[i] = 0;
+    }
+    return 0;
+}
+
+// The sorted intersecting pairs (lo << 32 | hi) of n boxes (6 floats each);
+// writes at most cap of them and returns how many there are.
+int64_t ncgo_pairs(const float* boxes6, uint32_t n, uint64_t* out, uint64_t cap) {
+    std::vector<AABB> b(n);
+    for (uint32_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            b[i].mins[d] = boxes6[6 * i + d];
+            b[i].maxs[d] = boxes6[6 * i + 3 + d];
+        }
+    const std::vector<uint64_t> p = intersecting_pairs(b.data(), n);
+    for (uint64_t k = 0; k < p.size() && k < cap; ++k) out[k] = p[k];
+    return (int64_t)p.size();
 }
 
 // Linear time of impact (time_of_impact_support_map_support_map; with
