@@ -608,6 +608,68 @@ def ray_cast_report(args, local, tolerance):
             "toi_rel_err_vs_f64_p50_p99": [float(np.percentile(rel, 50)), float(np.percentile(rel, 99))] if rel.size else None}
 
 
+def scene_pipeline_report(args, local, tolerance, dispatch):
+    """One collision-world frame on a scene of 2^20 objects (scene_objects,
+    seed 11): AABBs, the broad phase update (tree rebuild, pairs, events),
+    the gathered narrow-phase batch and query::contact on every pair; then a
+    frame of motion.  CPU: the oracle's sort-and-sweep pair set on a 131,072
+    object sample (the reference's DBVT is Rust and cannot run here)."""
+    import torch
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import workloads as W
+    from oracle import oracle as O
+    n = args.scene_objects
+    b = W.scene_objects(n, seed=11)
+    dev = f"cuda:{local}"
+    objects = Q.DeviceBatch.from_host(b, device=dev)
+    ctx = Q.Context(local, tolerance=tolerance, dispatch=dispatch)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+
+    def frame(bp):
+        ev[0].record()
+        boxes, _ = Q.aabb_batch(ctx, objects)
+        ev[1].record()
+        pairs, started, stopped = bp.update(boxes)
+        ev[2].record()
+        db = Q.gather_pairs(ctx, objects, bp.pairs_u32)
+        ev[3].record()
+        o = Q.contact_batch(ctx, db, 0.0)
+        ev[4].record()
+        torch.cuda.synchronize()
+        return pairs.shape[0], started.shape[0], stopped.shape[0], int(o["has_contact"].sum().item())
+
+    for _ in range(2):  # warm-up (allocations)
+        bp = Q.BroadPhase(ctx, 0.05)
+        frame(bp)
+        bp.close()
+    bp = Q.BroadPhase(ctx, 0.05)
+    counts0 = frame(bp)
+    t0 = [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
+    rng = np.random.default_rng(12)
+    moved = W.advance_frame(b, rng, sigma_t=0.02, sigma_r=0.02)
+    objects = Q.DeviceBatch.from_host(moved, device=dev)
+    counts1 = frame(bp)
+    t1 = [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
+    bp.close()
+    ctx.close()
+    sample = min(131072, n)
+    sb = b.subset(np.arange(sample))
+    boxes_h, _ = O.aabbs(sb)
+    tc = time.perf_counter()
+    cpu_pairs = O.intersecting_pairs(boxes_h + np.array([-0.05] * 3 + [0.05] * 3, np.float32))
+    cpu_s = time.perf_counter() - tc
+    names = ["aabb_ms", "broad_phase_ms", "gather_ms", "contact_ms"]
+    return {"workload": f"scene_objects {n} objects (seed 11; ~1.1 box overlaps per object), margin 0.05, "
+                        f"contact prediction 0",
+            "first_frame": dict(zip(names, t0), pairs=counts0[0], started=counts0[1], contacts=counts0[3],
+                                frame_ms=sum(t0)),
+            "moved_frame": dict(zip(names, t1), pairs=counts1[0], started=counts1[1], stopped=counts1[2],
+                                contacts=counts1[3], frame_ms=sum(t1)),
+            "broad_phase_objects_per_s": n / (t1[1] / 1e3),
+            "cpu_pair_set_sample": {"objects": sample, "seconds": cpu_s, "pairs": int(cpu_pairs.size),
+                                    "method": "oracle sort-and-sweep on x, 1 core (not the reference's DBVT)"}}
+
+
 def cpu_baseline(batch, threads, query):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -670,9 +732,10 @@ def main():
     ap.add_argument("--no-mlp", action="store_true")
     ap.add_argument("--stress-pairs", type=int, default=1 << 20)
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the precision-stress, cuboid, time-of-impact and ray-cast reports")
+                    help="skip the precision-stress, cuboid, time-of-impact, ray-cast and scene reports")
     ap.add_argument("--toi-pairs", type=int, default=1 << 20, help="sweeps of the time-of-impact report")
     ap.add_argument("--ray-count", type=int, default=1 << 20, help="rays of the ray-cast report")
+    ap.add_argument("--scene-objects", type=int, default=1 << 20, help="objects of the broad-phase scene report")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profiling: stop after the timed device steps (no second dispatch, no e2e, no report)")
     args = ap.parse_args()
@@ -853,8 +916,9 @@ def main():
         out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
         acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs), qo)
 
-    stress = cuboids = toi_rep = ray_rep = None
+    stress = cuboids = toi_rep = ray_rep = scene = None
     if not args.no_extras:
+        scene = scene_pipeline_report(args, local, args.tolerance, args.dispatch)
         stress = precision_stress(args, local, args.tolerance)
         cuboids = cuboid_small(args, local, args.tolerance)
         toi_rep = time_of_impact_report(args, local, args.tolerance, args.dispatch)
@@ -877,7 +941,7 @@ def main():
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc, "warm_start_coherent": coherent,
             "warm_start_learned": learned,
-            "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep, "ray_cast": ray_rep,
+            "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep, "ray_cast": ray_rep, "scene_pipeline": scene,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
             "epa": {"pairs": stats["n_epa"], "warp_stage_pairs": stats["n_epa_overflow"],

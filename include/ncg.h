@@ -348,6 +348,11 @@ int ncg_bp_results(ncg_broad_phase* bp, uint64_t* n_pairs, uint64_t* n_started, 
  * caller buffers (device or host; NULL skips one), asynchronously on stream. */
 int ncg_bp_copy(ncg_broad_phase* bp, uint32_t* pairs, uint32_t* started, uint32_t* stopped, void* stream);
 int ncg_bp_destroy(ncg_broad_phase* bp);
+/* The narrow-phase batch of a pair list (device): m1/g1 and m2/g2 of pair k are
+ * the pose and shape id of proxies pairs[2k] and pairs[2k+1] (the collision
+ * world's step from the broad phase's pairs to the narrow phase). */
+int ncg_gather_pairs(ncg_ctx* ctx, const ncg_pose* poses, const uint32_t* shape_ids, const uint32_t* pairs,
+                     uint64_t n_pairs, ncg_pose* m1, uint32_t* g1, ncg_pose* m2, uint32_t* g2, void* stream);
 
 /* ---- the same on host memory (synchronous; copies in and out) -------------- */
 int ncg_contact_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float prediction,

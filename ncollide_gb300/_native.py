@@ -35,7 +35,7 @@ EXPORTED = [
     "ncg_graph_destroy", "ncg_mlp_n_params", "ncg_ctx_set_mlp_params", "ncg_mlp_features", "ncg_mlp_infer",
     "ncg_mlp_grad", "ncg_mlp_adam", "ncg_time_of_impact_batch",
     "ncg_ray_cast_batch", "ncg_aabb_batch", "ncg_bp_create", "ncg_bp_update", "ncg_bp_results",
-    "ncg_bp_destroy", "ncg_bp_copy",
+    "ncg_bp_destroy", "ncg_bp_copy", "ncg_gather_pairs",
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
 TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT = range(4)
@@ -108,6 +108,7 @@ def load(build_if_missing=True):
                                  P(vp)]
     L.ncg_bp_destroy.argtypes = [vp]
     L.ncg_bp_copy.argtypes = [vp, vp, vp, vp, vp]
+    L.ncg_gather_pairs.argtypes = [vp, vp, vp, vp, ctypes.c_uint64, vp, vp, vp, vp, vp]
     L.ncg_contact_graph_create.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp, vp, P(vp)]
     L.ncg_graph_launch.argtypes = [vp, vp]
     L.ncg_graph_destroy.argtypes = [vp]

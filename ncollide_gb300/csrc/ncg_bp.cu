@@ -470,9 +470,43 @@ __global__ void k_compact(const uint2* a, uint32_t na, const uint32_t* flag, con
     out[pos[i]] = a[i];
 }
 
+// Narrow-phase batch of the broad phase's pairs: pair k = (proxy a, proxy b).
+__global__ void k_gather_pairs(const ncg_pose* poses, const uint32_t* shape_ids, const uint2* pairs, uint64_t n,
+                               ncg_pose* m1, uint32_t* g1, ncg_pose* m2, uint32_t* g2) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const uint2 p = pairs[k];
+        const float4* a = reinterpret_cast<const float4*>(poses + p.x);
+        const float4* b = reinterpret_cast<const float4*>(poses + p.y);
+        float4* o1 = reinterpret_cast<float4*>(m1 + k);
+        float4* o2 = reinterpret_cast<float4*>(m2 + k);
+        o1[0] = __ldg(a);
+        o1[1] = __ldg(a + 1);
+        o2[0] = __ldg(b);
+        o2[1] = __ldg(b + 1);
+        g1[k] = __ldg(shape_ids + p.x);
+        g2[k] = __ldg(shape_ids + p.y);
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ host side
+int gather_launch(const ncg_pose* poses, const uint32_t* shape_ids, const uint32_t* pairs, uint64_t n, ncg_pose* m1,
+                  uint32_t* g1, ncg_pose* m2, uint32_t* g2, int num_sms, cudaStream_t st) {
+    if (n == 0) return NCG_OK;
+    const uint64_t need = (n + 255) / 256;
+    const uint64_t cap = (uint64_t)num_sms * 8;
+    k_gather_pairs<<<(unsigned)(need < cap ? need : cap), 256, 0, st>>>(
+        poses, shape_ids, reinterpret_cast<const uint2*>(pairs), n, m1, g1, m2, g2);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_last_error(std::string("k_gather_pairs launch: ") + cudaGetErrorString(e));
+        return NCG_ECUDA;
+    }
+    return NCG_OK;
+}
+
 int aabb_launch(const ncg_batch& b, float* out, uint32_t* status, int num_sms, cudaStream_t st) {
     const uint64_t need = (b.n_pairs + 127) / 128;
     const uint64_t cap = (uint64_t)num_sms * 16;

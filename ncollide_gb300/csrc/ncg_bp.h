@@ -14,6 +14,10 @@ struct BroadPhaseState;
 // the batch; a bad shape gets NaN bounds and NCG_STATUS_BAD_INPUT.
 int aabb_launch(const ncg_batch& b, float* out, uint32_t* status, int num_sms, cudaStream_t st);
 
+// m1/g1/m2/g2 of pair k = (pairs[2k], pairs[2k+1]) from the proxies' poses and shape ids.
+int gather_launch(const ncg_pose* poses, const uint32_t* shape_ids, const uint32_t* pairs, uint64_t n, ncg_pose* m1,
+                  uint32_t* g1, ncg_pose* m2, uint32_t* g2, int num_sms, cudaStream_t st);
+
 int bp_create(float margin, int device, BroadPhaseState** out);
 void bp_destroy(BroadPhaseState* s);
 // Stores the boxes (loosened where they left their stored box), rebuilds the

@@ -883,6 +883,18 @@ int ncg_bp_copy(ncg_broad_phase* bp, uint32_t* pairs, uint32_t* started, uint32_
     return NCG_OK;
 }
 
+int ncg_gather_pairs(ncg_ctx* c, const ncg_pose* poses, const uint32_t* shape_ids, const uint32_t* pairs,
+                     uint64_t n, ncg_pose* m1, uint32_t* g1, ncg_pose* m2, uint32_t* g2, void* stream) {
+    if (!c) { g_last_error = "null context"; return NCG_EINVAL; }
+    if (n == 0) return NCG_OK;
+    if (!poses || !shape_ids || !pairs || !m1 || !g1 || !m2 || !g2) {
+        g_last_error = "null required pointer";
+        return NCG_EINVAL;
+    }
+    if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    return ncg::gather_launch(poses, shape_ids, pairs, n, m1, g1, m2, g2, c->num_sms, (cudaStream_t)stream);
+}
+
 int ncg_bp_destroy(ncg_broad_phase* bp) {
     if (!bp) return NCG_OK;
     ncg::bp_destroy(bp->s);

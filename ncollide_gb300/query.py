@@ -337,6 +337,7 @@ class BroadPhase:
         bufs = [torch.empty((int(c.value), 2), dtype=torch.int32, device=self.device) for c in counts]
         N.check(self._L.ncg_bp_copy(self._p, *[_ptr(b) if b.numel() else None for b in bufs], _stream(stream)),
                 "ncg_bp_copy")
+        self.pairs_u32 = bufs[0]  # the pair list as stored (uint32 ids), for gather_pairs
         return tuple(b.to(torch.int64) & 0xffffffff for b in bufs)
 
     def close(self):
@@ -349,6 +350,20 @@ class BroadPhase:
             self.close()
         except Exception:
             pass
+
+
+def gather_pairs(ctx: Context, objects: DeviceBatch, pairs_u32, stream=None):
+    """The narrow-phase DeviceBatch of a pair list: objects holds one proxy per
+    entry (pose m1, shape id g1); pairs_u32 [k,2] int32 (uint32 ids)."""
+    k, dev = int(pairs_u32.shape[0]), objects.m1.device
+    pairs_u32 = pairs_u32.contiguous()
+    m1 = torch.empty((k, 8), dtype=torch.float32, device=dev)
+    m2 = torch.empty((k, 8), dtype=torch.float32, device=dev)
+    g1 = torch.empty(k, dtype=torch.int32, device=dev)
+    g2 = torch.empty(k, dtype=torch.int32, device=dev)
+    N.check(ctx._L.ncg_gather_pairs(ctx.handle, _ptr(objects.m1), _ptr(objects.g1), _ptr(pairs_u32), k, _ptr(m1),
+                                    _ptr(g1), _ptr(m2), _ptr(g2), _stream(stream)), "ncg_gather_pairs")
+    return DeviceBatch(objects.shapes, objects.hull_points, m1, g1, m2, g2, None, objects.n_shapes)
 
 
 def _host_struct(b: PairBatch, keep):

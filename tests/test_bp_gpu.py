@@ -110,3 +110,31 @@ def test_bp_frames_events(ctx_factory):
     bp.close()
     with pytest.raises(N.NcgError):
         Q.BroadPhase(ctx, -1.0)
+
+
+def test_scene_pipeline_contacts(ctx_factory):
+    """AABBs -> broad phase -> gathered pairs -> query::contact, bit-exact
+    against the oracle on the same pairs."""
+    ctx = ctx_factory(tolerance=N.TOL_PRECISE)
+    ctx.set_dispatch(N.DISPATCH_QUERY)
+    b = W.scene_objects(20000, seed=34, overlaps=8.0)
+    objects = Q.DeviceBatch.from_host(b)
+    boxes, _ = Q.aabb_batch(ctx, objects)
+    bp = Q.BroadPhase(ctx, 0.0)
+    pairs, _, _ = bp.update(boxes)
+    db = Q.gather_pairs(ctx, objects, bp.pairs_u32)
+    got = Q.contact_batch(ctx, db, 0.0, with_iters=True)
+    torch.cuda.synchronize()
+    p = pairs.cpu().numpy()
+    assert p.shape[0] > 1000
+    pb = S.PairBatch(b.shapes, b.hull_points, b.m1[p[:, 0]], p[:, 0].astype(np.uint32), b.m1[p[:, 1]],
+                     p[:, 1].astype(np.uint32))
+    assert np.array_equal(db.m1.cpu().numpy(), pb.m1) and np.array_equal(db.g2.cpu().numpy().view(np.uint32), pb.g2)
+    r = O.query(pb, O.CONTACT_QUERY, O.MIXED, eps=-1.0, epa_tol=1e-6)
+    assert np.array_equal(got["has_contact"].cpu().numpy(), r.tag)
+    assert np.array_equal(got["status"].cpu().numpy().view(np.uint32), r.status)
+    m = r.tag == 1
+    c = got["contact"].cpu().numpy()
+    want = np.concatenate([r.p1, r.p2, r.dir, r.value[:, None]], 1).astype(np.float32)
+    assert np.array_equal(c[m], want[m])
+    bp.close()
