@@ -18,6 +18,7 @@
  *              src/query/time_of_impact/time_of_impact_support_map_support_map.rs:10-127
  *   ray cast   src/query/ray/ray_support_map.rs:14-110, src/query/algorithms/gjk.rs:180-194
  *   aabb       src/bounding_volume/aabb_*.rs; broad phase src/pipeline/broad_phase/dbvt_broad_phase.rs
+ *   manifold   src/pipeline/narrow_phase/contact_generator/convex_polyhedron_convex_polyhedron_manifold_generator.rs
  * The per-pair arithmetic is gjk::closest_points (src/query/algorithms/gjk.rs:76-177)
  * with VoronoiSimplex (voronoi_simplex3.rs) and EPA (epa3.rs:219-454).
  */
@@ -106,12 +107,33 @@ enum ncg_closest_points { NCG_CP_INTERSECTING = 0, NCG_CP_WITHIN_MARGIN = 1, NCG
 #define NCG_STATUS_BAD_INPUT     (1u << 6) /* shape index out of range, bad hull slice */
 #define NCG_STATUS_UNSUPPORTED_FEATURE (1u << 7) /* query dispatch: ball centre on a ConvexHull's
                                                     surface needs the hull's face topology */
+#define NCG_STATUS_NOT_POLYHEDRA (1u << 9) /* manifold: not a Cuboid pair; the manifold is the
+                                              single GJK/EPA contact with unknown features  */
 #define NCG_STATUS_EPA_PRECISION_LIMIT (1u << 8) /* NCG_TOL_PRECISE: EPA's expansion would have
                                                     returned None (f32 noise on sliver faces); the
                                                     contact is the best face found so far */
 
 /* query::TOI<f32> (src/query/time_of_impact/time_of_impact.rs:29-42):
  * witnesses and normals in the shapes' local frames; valid when has_toi. */
+/* Contact manifolds.  FeatureId (src/shape/feature_id.rs) packed as
+ * kind << 28 | id with kind NCG_FEATURE_*; Cuboid ids as in cuboid.rs:148-277. */
+enum ncg_feature_kind { NCG_FEATURE_UNKNOWN = 0, NCG_FEATURE_VERTEX = 1, NCG_FEATURE_EDGE = 2,
+                        NCG_FEATURE_FACE = 3 };
+#define NCG_MANIFOLD_MAX 16
+typedef struct ncg_manifold_point {
+    float world1[3];
+    float world2[3];
+    float depth;
+    uint32_t feature1, feature2;
+} ncg_manifold_point;
+/* The contacts ConvexPolyhedronConvexPolyhedronManifoldGenerator::generate_contacts
+ * pushes for one pair, all with the pair's normal. */
+typedef struct ncg_manifold {
+    float normal[3];
+    uint32_t n;
+    ncg_manifold_point points[NCG_MANIFOLD_MAX];
+} ncg_manifold;
+
 typedef struct ncg_toi {
     float toi;
     float witness1[3];
@@ -318,6 +340,22 @@ int ncg_time_of_impact_batch(ncg_ctx* ctx, const ncg_batch* batch, const float* 
 int ncg_ray_cast_batch(ncg_ctx* ctx, const ncg_batch* batch, const float* rays, float max_toi,
                        int solid, float* out_toi, float* out_normal, uint8_t* has_hit,
                        uint32_t* status, uint32_t* iters, void* stream);
+
+/* ConvexPolyhedronConvexPolyhedronManifoldGenerator::generate_contacts
+ * (src/pipeline/narrow_phase/contact_generator/convex_polyhedron_convex_polyhedron_manifold_generator.rs:84-176)
+ * for every pair: contact_support_map_support_map_with_params with
+ * prediction.linear (init_dir = last_gjk_dir under NCG_WARM_INIT_DIR), then for
+ * Cuboid pairs the support faces (depth > 0) or the support features within
+ * the angular tolerances (cuboid.rs:279-405), their clipping
+ * (convex_polygonal_feature3.rs:217-339) and the contacts handed to the
+ * manifold (add_contact_to_manifold's feature checks; the manifold's
+ * persistence cache is the caller's).  contact / has_contact / out_dir receive
+ * the contact query's results (out_dir may alias batch->init_dir: the next
+ * frame's last_gjk_dir).  Pairs that are not two Cuboids get their single
+ * contact with NCG_STATUS_NOT_POLYHEDRA. */
+int ncg_manifold_batch(ncg_ctx* ctx, const ncg_batch* batch, float prediction, float angular1,
+                       float angular2, ncg_contact* contact, uint8_t* has_contact, float* out_dir,
+                       ncg_manifold* out, uint32_t* status, void* stream);
 
 /* ---- bounding volumes and the broad phase ----------------------------------
  * ncg_aabb_batch: HasBoundingVolume<AABB>::bounding_volume of shapes[g1[i]] at

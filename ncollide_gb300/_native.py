@@ -35,7 +35,7 @@ EXPORTED = [
     "ncg_graph_destroy", "ncg_mlp_n_params", "ncg_ctx_set_mlp_params", "ncg_mlp_features", "ncg_mlp_infer",
     "ncg_mlp_grad", "ncg_mlp_adam", "ncg_time_of_impact_batch",
     "ncg_ray_cast_batch", "ncg_aabb_batch", "ncg_bp_create", "ncg_bp_update", "ncg_bp_results",
-    "ncg_bp_destroy", "ncg_bp_copy", "ncg_gather_pairs",
+    "ncg_bp_destroy", "ncg_bp_copy", "ncg_gather_pairs", "ncg_manifold_batch",
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
 TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT = range(4)
@@ -43,6 +43,8 @@ DISPATCH_SUPPORT_MAP, DISPATCH_QUERY = 0, 1
 TOI_OUT_OF_ITERATIONS, TOI_CONVERGED, TOI_FAILED, TOI_PENETRATING = range(4)
 STATUS_UNSUPPORTED_FEATURE = 1 << 7
 STATUS_EPA_PRECISION_LIMIT = 1 << 8
+STATUS_NOT_POLYHEDRA = 1 << 9
+MANIFOLD_MAX = 16
 NOALLOC_MAX_PAIRS = 32768
 NOALLOC_SCRATCH_BYTES = 7827200
 STAGES = ["classify", "gjk_thread", "gjk_warp", "epa_thread", "epa_warp", "epa_wide"]
@@ -109,6 +111,7 @@ def load(build_if_missing=True):
     L.ncg_bp_destroy.argtypes = [vp]
     L.ncg_bp_copy.argtypes = [vp, vp, vp, vp, vp]
     L.ncg_gather_pairs.argtypes = [vp, vp, vp, vp, ctypes.c_uint64, vp, vp, vp, vp, vp]
+    L.ncg_manifold_batch.argtypes = [vp, P(NcgBatch), f32, f32, f32, vp, vp, vp, vp, vp, vp]
     L.ncg_contact_graph_create.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp, vp, P(vp)]
     L.ncg_graph_launch.argtypes = [vp, vp]
     L.ncg_graph_destroy.argtypes = [vp]

@@ -37,6 +37,7 @@
 #include "ncg_mlp.h"
 #include "ncg_toi.h"
 #include "ncg_bp.h"
+#include "ncg_manifold.h"
 #include "ncg_epa.cuh"
 #include "ncg_query.cuh"
 #include "ncg_pipeline.cuh"
@@ -827,6 +828,31 @@ int ncg_ray_cast_batch(ncg_ctx* c, const ncg_batch* b, const float* rays, float 
     c->last = ncg_stats{};
     c->last.n_pairs = b->n_pairs;
     return NCG_OK;
+}
+
+int ncg_manifold_batch(ncg_ctx* c, const ncg_batch* b, float prediction, float angular1, float angular2,
+                       ncg_contact* contact, uint8_t* has_contact, float* out_dir, ncg_manifold* out, uint32_t* status,
+                       void* stream) {
+    if (!(prediction >= 0.0f) || !(angular1 >= 0.0f) || !(angular2 >= 0.0f)) {
+        g_last_error = "the contact prediction must be >= 0";
+        return NCG_EINVAL;
+    }
+    if (c && b && b->n_pairs == 0) return NCG_OK;
+    if (!contact || !has_contact || !out || !status) { g_last_error = "null output"; return NCG_EINVAL; }
+    if (!c) { g_last_error = "null context"; return NCG_EINVAL; }
+    // the generator calls contact_support_map_support_map_with_params for every pair
+    const int dispatch = c->dispatch;
+    c->dispatch = NCG_DISPATCH_SUPPORT_MAP;
+    Outputs o{contact, has_contact, out_dir, nullptr, nullptr, status, nullptr};
+    const cudaStream_t st = (cudaStream_t)stream;
+    int rc = run_query(c, b, Q_CONTACT, prediction, o, st);
+    c->dispatch = dispatch;
+    if (rc != NCG_OK) return rc;
+    const ncg::ManifoldParams mp{prediction, std::cos(angular1), std::sin(angular1), std::cos(angular2),
+                                 std::sin(angular2)};
+    rc = ncg::manifold_launch(*b, contact, has_contact, mp, out, status, c->num_sms, st);
+    if (rc == NCG_OK) c->launches += 1;
+    return rc;
 }
 
 int ncg_aabb_batch(ncg_ctx* c, const ncg_batch* b, float* out_aabbs, uint32_t* status, void* stream) {

@@ -289,3 +289,42 @@ def scene_objects(n=1 << 20, seed=11, kinds=(BALL, CUBOID, CAPSULE, CONE, CYLIND
     g1 = np.arange(n, dtype=np.uint32)
     return PairBatch(shapes, np.ascontiguousarray(pts), m1, g1, m1.copy(), g1.copy(), scale=radii,
                      meta={"workload": "scene_objects", "n": n, "seed": seed, "side": side})
+
+
+def cuboid_stacks(n=1 << 18, seed=13, tilt_deg=5.0, gap=0.05):
+    """Cuboid pairs resting on each other (the manifold generator's face-face
+    case): B above A along A's y axis with a random yaw, a tilt up to tilt_deg
+    and a vertical gap or penetration in [-gap, gap]; A at a random pose."""
+    rng = np.random.default_rng(seed)
+    shapes = np.zeros(2 * n, SHAPE_DTYPE)
+    shapes["kind"] = CUBOID
+    shapes["p"][:, :3] = rng.uniform(0.1, 1.0, (2 * n, 3))
+    ha, hb = shapes["p"][0::2, :3].astype(np.float64), shapes["p"][1::2, :3].astype(np.float64)
+    qa = random_unit_quaternions(rng, n).astype(np.float64)
+    yaw = rng.uniform(-np.pi, np.pi, n)
+    q_yaw = np.stack([np.zeros(n), np.sin(yaw / 2), np.zeros(n), np.cos(yaw / 2)], 1)
+    ax = random_unit_vectors(rng, n)
+    tilt = np.radians(tilt_deg) * rng.uniform(0.0, 1.0, n)
+    q_tilt = np.concatenate([ax * np.sin(tilt / 2)[:, None], np.cos(tilt / 2)[:, None]], 1)
+    qb_rel = _quat_mul(q_tilt, q_yaw)
+    qb = _quat_mul(qa, qb_rel)
+    qb /= np.linalg.norm(qb, axis=1, keepdims=True)
+    up = _rotate(qa, np.tile([0.0, 1.0, 0.0], (n, 1)))
+    slide = rng.uniform(-0.5, 0.5, (n, 2)) * np.minimum(ha[:, [0, 2]], hb[:, [0, 2]])
+    side = _rotate(qa, np.stack([slide[:, 0], np.zeros(n), slide[:, 1]], 1))
+    ta = rng.uniform(-1.0, 1.0, (n, 3))
+    tb = ta + up * (ha[:, 1:2] + hb[:, 1:2] + rng.uniform(-gap, gap, (n, 1))) + side
+    m1 = np.zeros((n, 8), np.float32)
+    m2 = np.zeros((n, 8), np.float32)
+    m1[:, :4], m1[:, 4:7] = qa, ta
+    m2[:, :4], m2[:, 4:7] = qb, tb
+    g1 = np.arange(0, 2 * n, 2, dtype=np.uint32)
+    radii = np.linalg.norm(shapes["p"][:, :3], axis=1)
+    return PairBatch(shapes, np.zeros((1, 4), np.float32), m1, g1, m2, g1 + 1, scale=radii[0::2] + radii[1::2],
+                     meta={"workload": "cuboid_stacks", "n": n, "seed": seed})
+
+
+def _rotate(q, v):
+    qv = q[:, :3]
+    t = 2.0 * np.cross(qv, v)
+    return v + q[:, 3:4] * t + np.cross(qv, t)

@@ -29,7 +29,7 @@ _lib = None
 def build(force=False):
     """Compiles the oracle with the committed Makefile (g++ only)."""
     srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "ncg_oracle.hpp", "ncg_oracle_toi.hpp",
-                                            "ncg_oracle_bp.hpp", "dw.hpp")]
+                                            "ncg_oracle_bp.hpp", "ncg_oracle_manifold.hpp", "dw.hpp")]
     if not force and os.path.exists(LIB_PATH):
         if os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
             return LIB_PATH
@@ -58,6 +58,9 @@ def lib():
         L.ncgo_aabb.restype = i32
         L.ncgo_pairs.argtypes = [vp, u32, vp, u64]
         L.ncgo_pairs.restype = ctypes.c_int64
+        L.ncgo_manifold.argtypes = [vp, u32, u64, vp, vp, vp, vp, vp, vp, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_float, vp, vp]
+        L.ncgo_manifold.restype = i32
         L.ncgo_simplex_kat.restype = i32
         _lib = L
     return _lib
@@ -282,3 +285,29 @@ class BroadPhase:
         stopped = np.setdiff1d(self.pairs, pairs)
         self.pairs = pairs
         return pairs, started, stopped
+
+
+MANIFOLD_MAX = 16
+MANIFOLD_DTYPE = np.dtype([("normal", np.float32, 3), ("n", np.uint32),
+                           ("points", np.dtype([("world1", np.float32, 3), ("world2", np.float32, 3),
+                                                ("depth", np.float32), ("feature1", np.uint32),
+                                                ("feature2", np.uint32)]), MANIFOLD_MAX)])
+
+
+def manifold(batch, contact9, has, linear=0.0, angular1=0.0, angular2=0.0):
+    """Manifolds (MANIFOLD_DTYPE [N]) and status from each pair's contact query
+    result: contact9 [N,9] = world1, world2, normal (float32), has [N]."""
+    L = lib()
+    n = batch.n_pairs
+    out = np.zeros(n, MANIFOLD_DTYPE)
+    status = np.zeros(n, np.uint32)
+    shapes = np.ascontiguousarray(batch.shapes)
+    m1 = np.ascontiguousarray(batch.m1, np.float32)
+    m2 = np.ascontiguousarray(batch.m2, np.float32)
+    g1 = np.ascontiguousarray(batch.g1, np.uint32)
+    g2 = np.ascontiguousarray(batch.g2, np.uint32)
+    c = np.ascontiguousarray(contact9, np.float32).reshape(n, 9)
+    h = np.ascontiguousarray(has, np.uint8)
+    L.ncgo_manifold(_p(shapes), len(shapes), n, _p(m1), _p(g1), _p(m2), _p(g2), _p(c), _p(h), float(linear),
+                    float(angular1), float(angular2), _p(out), _p(status))
+    return out, status

@@ -10,6 +10,7 @@
 #include "ncg_oracle.hpp"
 #include "ncg_oracle_toi.hpp"
 #include "ncg_oracle_bp.hpp"
+#include "ncg_oracle_manifold.hpp"
 
 using namespace ncgo;
 
@@ -378,6 +379,53 @@ int64_t ncgo_pairs(const float* boxes6, uint32_t n, uint64_t* out, uint64_t cap)
     const std::vector<uint64_t> p = intersecting_pairs(b.data(), n);
     for (uint64_t k = 0; k < p.size() && k < cap; ++k) out[k] = p[k];
     return (int64_t)p.size();
+}
+
+// The manifold step of ConvexPolyhedronConvexPolyhedronManifoldGenerator from
+// each pair's contact query result: contact9 = world1, world2, normal (f32),
+// has = the query returned ClosestPoints.  out: ncg_manifold per pair.
+int ncgo_manifold(const ncg_shape* shapes, uint32_t n_shapes, uint64_t n, const ncg_pose* m1, const uint32_t* g1,
+                  const ncg_pose* m2, const uint32_t* g2, const float* contact9, const uint8_t* has, float linear,
+                  float angular1, float angular2, ncg_manifold* out, uint32_t* status) {
+    InF32 in{shapes, n_shapes, nullptr, 0, m1, g1, m2, g2, nullptr};
+    const float cang1 = std::cos(angular1), sang1 = std::sin(angular1);
+    const float cang2 = std::cos(angular2), sang2 = std::sin(angular2);
+    for (uint64_t i = 0; i < n; ++i) {
+        ncg_manifold& o = out[i];
+        std::memset(&o, 0, sizeof(o));
+        status[i] = 0;
+        const float* c = contact9 + 9 * i;
+        const V3<float> w1{c[0], c[1], c[2]}, w2{c[3], c[4], c[5]}, nn{c[6], c[7], c[8]};
+        if (!has[i]) continue;
+        o.normal[0] = nn.x;
+        o.normal[1] = nn.y;
+        o.normal[2] = nn.z;
+        const bool cub = g1[i] < n_shapes && g2[i] < n_shapes && shapes[g1[i]].kind == NCG_CUBOID &&
+                         shapes[g2[i]].kind == NCG_CUBOID;
+        ManifoldPoint pts[MANIFOLD_MAX];
+        int k;
+        if (cub) {
+            const ncg_shape& s1 = shapes[g1[i]];
+            const ncg_shape& s2 = shapes[g2[i]];
+            k = cuboid_manifold(pose1<float>(in, i), V3<float>{s1.p[0], s1.p[1], s1.p[2]}, pose2<float>(in, i),
+                                V3<float>{s2.p[0], s2.p[1], s2.p[2]}, w1, w2, nn, linear, cang1, sang1, cang2, sang2,
+                                pts);
+        } else {
+            pts[0] = ManifoldPoint{w1, w2, depth_wo(w1, w2, nn), 0u, 0u};
+            k = 1;
+            status[i] = NCG_STATUS_NOT_POLYHEDRA;
+        }
+        o.n = (uint32_t)k;
+        for (int j = 0; j < k; ++j) {
+            ncg_manifold_point& p = o.points[j];
+            p.world1[0] = pts[j].w1.x; p.world1[1] = pts[j].w1.y; p.world1[2] = pts[j].w1.z;
+            p.world2[0] = pts[j].w2.x; p.world2[1] = pts[j].w2.y; p.world2[2] = pts[j].w2.z;
+            p.depth = pts[j].depth;
+            p.feature1 = pts[j].f1;
+            p.feature2 = pts[j].f2;
+        }
+    }
+    return 0;
 }
 
 // Linear time of impact (time_of_impact_support_map_support_map; with

@@ -206,3 +206,42 @@ def test_ray_cast_support_maps_analytic_answers():
         assert np.allclose(r["normal"][2], [0, -1, 0], atol=1e-6)
         r = O.ray_cast(b, rays, pol, max_toi=3.0)
         assert list(r["hit"]) == [0, 1, 0, 0]
+
+
+def _cuboid_pairs(pairs):
+    from ncollide_gb300 import shapes as S
+    shp = np.zeros(2 * len(pairs), S.SHAPE_DTYPE)
+    m1 = np.zeros((len(pairs), 8), np.float32)
+    m2 = np.zeros((len(pairs), 8), np.float32)
+    for i, (t1, h1, t2, h2) in enumerate(pairs):
+        shp[2 * i]["kind"] = shp[2 * i + 1]["kind"] = 1
+        shp[2 * i]["p"] = list(h1) + [0.0]
+        shp[2 * i + 1]["p"] = list(h2) + [0.0]
+        m1[i, 3] = m2[i, 3] = 1.0
+        m1[i, 4:7] = t1
+        m2[i, 4:7] = t2
+    g = np.arange(0, 2 * len(pairs), 2, dtype=np.uint32)
+    return S.PairBatch(shp, np.zeros((1, 4), np.float32), m1, g, m2, g + 1)
+
+
+def test_cuboid_manifold_analytic():
+    """Face-face manifolds of stacked unit cubes (analytic answers: the corners
+    of the overlap rectangle at the penetration depth)."""
+    b = _cuboid_pairs([((0, 0, 0), (1, 1, 1), (0, 1.9, 0), (1, 1, 1)),
+                       ((0, 0, 0), (1, 1, 1), (0.5, 1.9, 0.3), (1, 1, 1)),
+                       ((0, 0, 0), (1, 1, 1), (0, 2.05, 0), (1, 1, 1))])
+    r = O.query(b, O.CONTACT, O.F32, param=0.1)
+    c9 = np.concatenate([r.p1, r.p2, r.dir], 1).astype(np.float32)
+    man, st = O.manifold(b, c9, r.tag, linear=0.1, angular1=0.1, angular2=0.1)
+    assert not st.any()
+    corners = lambda m: {(round(float(p["world1"][0]), 5), round(float(p["world1"][2]), 5))
+                         for p in m["points"][:m["n"]]}
+    assert man[0]["n"] == 8 and corners(man[0]) == {(1, 1), (1, -1), (-1, 1), (-1, -1)}
+    assert man[1]["n"] == 4 and corners(man[1]) == {(1, 1), (1, -0.7), (-0.5, 1), (-0.5, -0.7)}
+    for m, d in ((man[0], 0.1), (man[1], 0.1), (man[2], -0.05)):
+        pts = m["points"][:m["n"]]
+        assert np.allclose(pts["depth"], d, atol=1e-6)
+        assert np.allclose(pts["world1"][:, 1], 1.0) and np.allclose(m["normal"], [0, 1, 0], atol=1e-7)
+    # features: cube 1's +y face is Face(1), cube 2's -y face Face(4)
+    assert {int(p["feature2"]) for p in man[0]["points"][:4]} == {(3 << 28) | 4}
+    assert {int(p["feature1"]) for p in man[0]["points"][4:8]} == {(3 << 28) | 1}
