@@ -670,6 +670,48 @@ def scene_pipeline_report(args, local, tolerance, dispatch):
                                     "method": "oracle sort-and-sweep on x, 1 core (not the reference's DBVT)"}}
 
 
+def manifold_report(args, local, tolerance):
+    """Contact manifolds of 2^20 resting Cuboid pairs (cuboid_stacks, seed 13;
+    prediction 0.1, angular tolerances 0.05): the contact query plus the
+    manifold step on the GPU, inputs resident; the f32 reference path (oracle:
+    contact and manifold) on a 65,536-pair sample with every host core."""
+    import torch
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import workloads as W
+    from oracle import oracle as O
+    n = args.manifold_pairs
+    b = W.cuboid_stacks(n, seed=13)
+    db = Q.DeviceBatch.from_host(b, device=f"cuda:{local}")
+    ctx = Q.Context(local, tolerance=tolerance)
+    for _ in range(3):
+        o = Q.manifold_batch(ctx, db, 0.1, 0.05, 0.05)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        o = Q.manifold_batch(ctx, db, 0.1, 0.05, 0.05)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    man = o["manifold"].cpu().numpy().view(O.MANIFOLD_DTYPE).reshape(-1)
+    ctx.close()
+    sample = min(65536, n)
+    sb = b.subset(np.arange(sample))
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    r = O.query(sb, O.CONTACT, O.F32, param=0.1, threads=threads)
+    c9 = np.concatenate([r.p1, r.p2, r.dir], 1).astype(np.float32)
+    O.manifold(sb, c9, r.tag, linear=0.1, angular1=0.05, angular2=0.05, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": f"cuboid_stacks {n} pairs, seed 13, prediction 0.1, angular 0.05",
+            "pairs_per_s": n / (ms / 1e3), "ms_per_step": ms,
+            "contacts_per_pair": float(man["n"].mean()),
+            "manifold_size_histogram": np.bincount(man["n"], minlength=9)[:9].tolist(),
+            "cpu_reference_path_pairs_per_s": sample / cpu_s, "cpu_cores": threads,
+            "cpu_sample": f"first {sample} pairs, f32 reference path (oracle contact and manifold step)"}
+
+
 def cpu_baseline(batch, threads, query):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -732,10 +774,11 @@ def main():
     ap.add_argument("--no-mlp", action="store_true")
     ap.add_argument("--stress-pairs", type=int, default=1 << 20)
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the precision-stress, cuboid, time-of-impact, ray-cast and scene reports")
+                    help="skip the precision-stress, cuboid, time-of-impact, ray-cast, scene and manifold reports")
     ap.add_argument("--toi-pairs", type=int, default=1 << 20, help="sweeps of the time-of-impact report")
     ap.add_argument("--ray-count", type=int, default=1 << 20, help="rays of the ray-cast report")
     ap.add_argument("--scene-objects", type=int, default=1 << 20, help="objects of the broad-phase scene report")
+    ap.add_argument("--manifold-pairs", type=int, default=1 << 20, help="pairs of the manifold report")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profiling: stop after the timed device steps (no second dispatch, no e2e, no report)")
     args = ap.parse_args()
@@ -916,9 +959,10 @@ def main():
         out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
         acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs), qo)
 
-    stress = cuboids = toi_rep = ray_rep = scene = None
+    stress = cuboids = toi_rep = ray_rep = scene = manifolds = None
     if not args.no_extras:
         scene = scene_pipeline_report(args, local, args.tolerance, args.dispatch)
+        manifolds = manifold_report(args, local, args.tolerance)
         stress = precision_stress(args, local, args.tolerance)
         cuboids = cuboid_small(args, local, args.tolerance)
         toi_rep = time_of_impact_report(args, local, args.tolerance, args.dispatch)
@@ -941,7 +985,7 @@ def main():
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc, "warm_start_coherent": coherent,
             "warm_start_learned": learned,
-            "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep, "ray_cast": ray_rep, "scene_pipeline": scene,
+            "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep, "ray_cast": ray_rep, "scene_pipeline": scene, "manifolds": manifolds,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
             "epa": {"pairs": stats["n_epa"], "warp_stage_pairs": stats["n_epa_overflow"],

@@ -383,14 +383,16 @@ int64_t ncgo_pairs(const float* boxes6, uint32_t n, uint64_t* out, uint64_t cap)
 
 // The manifold step of ConvexPolyhedronConvexPolyhedronManifoldGenerator from
 // each pair's contact query result: contact9 = world1, world2, normal (f32),
-// has = the query returned ClosestPoints.  out: ncg_manifold per pair.
+// has = the query returned ClosestPoints.  out: ncg_manifold per pair; one
+// static chunk of pairs per thread.
 int ncgo_manifold(const ncg_shape* shapes, uint32_t n_shapes, uint64_t n, const ncg_pose* m1, const uint32_t* g1,
                   const ncg_pose* m2, const uint32_t* g2, const float* contact9, const uint8_t* has, float linear,
-                  float angular1, float angular2, ncg_manifold* out, uint32_t* status) {
+                  float angular1, float angular2, ncg_manifold* out, uint32_t* status, int n_threads) {
     InF32 in{shapes, n_shapes, nullptr, 0, m1, g1, m2, g2, nullptr};
     const float cang1 = std::cos(angular1), sang1 = std::sin(angular1);
     const float cang2 = std::cos(angular2), sang2 = std::sin(angular2);
-    for (uint64_t i = 0; i < n; ++i) {
+    auto range = [&](uint64_t lo, uint64_t hi) {
+    for (uint64_t i = lo; i < hi; ++i) {
         ncg_manifold& o = out[i];
         std::memset(&o, 0, sizeof(o));
         status[i] = 0;
@@ -425,6 +427,19 @@ int ncgo_manifold(const ncg_shape* shapes, uint32_t n_shapes, uint64_t n, const 
             p.feature2 = pts[j].f2;
         }
     }
+    };
+    if (n_threads <= 1 || n < 1024) {
+        range(0, n);
+        return 0;
+    }
+    std::vector<std::thread> th;
+    const uint64_t chunk = (n + n_threads - 1) / n_threads;
+    for (int t = 0; t < n_threads; ++t) {
+        const uint64_t lo = t * chunk, hi = std::min<uint64_t>(n, lo + chunk);
+        if (lo >= hi) break;
+        th.emplace_back(range, lo, hi);
+    }
+    for (auto& x : th) x.join();
     return 0;
 }
 
