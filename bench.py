@@ -781,6 +781,8 @@ def main():
     ap.add_argument("--manifold-pairs", type=int, default=1 << 20, help="pairs of the manifold report")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profiling: stop after the timed device steps (no second dispatch, no e2e, no report)")
+    ap.add_argument("--only", choices=["toi", "ray", "scene", "manifold", "stress", "cuboid"],
+                    help="run one secondary report alone and print it (not a bench line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -795,6 +797,15 @@ def main():
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if args.only:
+        report = {"toi": lambda: time_of_impact_report(args, local, args.tolerance, args.dispatch),
+                  "ray": lambda: ray_cast_report(args, local, args.tolerance),
+                  "scene": lambda: scene_pipeline_report(args, local, args.tolerance, args.dispatch),
+                  "manifold": lambda: manifold_report(args, local, args.tolerance),
+                  "stress": lambda: precision_stress(args, local, args.tolerance),
+                  "cuboid": lambda: cuboid_small(args, local, args.tolerance)}[args.only]()
+        print(json.dumps({"report": args.only, **report}), flush=True)
+        return 0
     dist = None
     if world > 1:
         import torch.distributed as dist
