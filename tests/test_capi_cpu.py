@@ -39,6 +39,8 @@ def test_struct_layouts_match_header():
     assert S.CONTACT_DTYPE.itemsize == 40
     assert ctypes.sizeof(N.NcgBatch) == 80
     assert ctypes.sizeof(N.NcgStats) == 48
+    from oracle import oracle as O
+    assert O.MANIFOLD_DTYPE.itemsize == 16 + 36 * N.MANIFOLD_MAX  # ncg_manifold
 
 
 def test_invalid_arguments_rejected_without_gpu():
@@ -47,6 +49,19 @@ def test_invalid_arguments_rejected_without_gpu():
     assert L.ncg_contact_batch(None, None, 0.0, None, None, None, None, None, None) == N.NCG_EINVAL
     assert L.ncg_proximity_batch(None, None, ctypes.c_float(-1.0), None, None, None, None, None) == N.NCG_EINVAL
     assert L.ncg_ctx_set_tolerance(None, 0) == N.NCG_EINVAL
+    f = ctypes.c_float
+    # the reference's asserts become NCG_EINVAL: negative or NaN max_toi / target / margin / prediction
+    assert L.ncg_time_of_impact_batch(None, None, None, None, f(-1.0), f(0.0), None, None, None, None,
+                                      None) == N.NCG_EINVAL
+    assert L.ncg_time_of_impact_batch(None, None, None, None, f(1.0), f(float("nan")), None, None, None, None,
+                                      None) == N.NCG_EINVAL
+    assert L.ncg_ray_cast_batch(None, None, None, f(-1.0), 1, None, None, None, None, None, None) == N.NCG_EINVAL
+    assert L.ncg_manifold_batch(None, None, f(-0.1), f(0.0), f(0.0), None, None, None, None, None,
+                                None) == N.NCG_EINVAL
+    assert L.ncg_bp_create(None, f(0.1), None) == N.NCG_EINVAL
+    assert L.ncg_bp_update(None, None, 0, None) == N.NCG_EINVAL
+    assert L.ncg_aabb_batch(None, None, None, None, None) == N.NCG_EINVAL
+    assert L.ncg_gather_pairs(None, None, None, None, 1, None, None, None, None, None) == N.NCG_EINVAL
 
 
 def test_ctx_create_reports_missing_gpu():
