@@ -44,6 +44,10 @@
 
 #include "ncg_core.cuh"
 
+#ifndef NCG_EPA_HEAP_ARITY
+#define NCG_EPA_HEAP_ARITY 2
+#endif
+
 namespace ncg {
 
 enum EpaExit : int {
@@ -204,7 +208,11 @@ struct EpaStore {
         return s == 0.0f || fabsf(s) <= tol.affine_eps_f;
     }
 
-    // ---- binary heap on (neg_dist, earlier push) — one thread only.
+    // ---- d-ary heap on (neg_dist, earlier push) — one thread only.  With a
+    // strict total order the pop sequence does not depend on the arity
+    // (NCG_EPA_HEAP_ARITY; 4- and 8-ary heaps measured no faster than binary:
+    // the heap is not what bounds an EPA iteration).
+    static constexpr int HA = NCG_EPA_HEAP_ARITY;
     NCG_DEV static bool before(float4 a, float4 b) {
         real ka(a.x, a.y), kb(b.x, b.y);
         if (ka > kb) return true;
@@ -213,7 +221,7 @@ struct EpaStore {
     }
     NCG_DEV void sift_up(int pos, float4 e) {
         while (pos > 0) {
-            int parent = (pos - 1) >> 1;
+            int parent = (pos - 1) / HA;
             float4 p = heap[parent];
             if (!before(e, p)) break;
             heap[pos] = p;
@@ -223,12 +231,16 @@ struct EpaStore {
     }
     NCG_DEV void sift_down(int pos, int size, float4 e) {
         for (;;) {
-            int c = 2 * pos + 1;
-            if (c >= size) break;
-            float4 ce = heap[c];
-            if (c + 1 < size) {
-                float4 c2 = heap[c + 1];
-                if (before(c2, ce)) { ce = c2; c = c + 1; }
+            const int c0 = HA * pos + 1;
+            if (c0 >= size) break;
+            int c = c0;
+            float4 ce = heap[c0];
+#pragma unroll
+            for (int k = 1; k < HA; ++k) {
+                if (c0 + k < size) {
+                    float4 ck = heap[c0 + k];
+                    if (before(ck, ce)) { ce = ck; c = c0 + k; }
+                }
             }
             if (!before(ce, e)) break;
             heap[pos] = ce;
@@ -244,7 +256,7 @@ struct EpaStore {
             if (live(__float_as_uint(e.w))) heap[j++] = e;
         }
         size = j;
-        for (int i = size / 2 - 1; i >= 0; --i) sift_down(i, size, heap[i]);
+        for (int i = (size - 2) / HA; i >= 0; --i) sift_down(i, size, heap[i]);
     }
     // Returns false when the heap is full even after purging.
     NCG_DEV bool push(int& size, uint32_t& seq, uint32_t ref, real key) {
