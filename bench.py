@@ -712,6 +712,52 @@ def manifold_report(args, local, tolerance):
             "cpu_sample": f"first {sample} pairs, f32 reference path (oracle contact and manifold step)"}
 
 
+def other_queries_report(args, local, tolerance, db, batch):
+    """distance, proximity (margin 0.1) and closest points (prediction 0.1) on
+    the headline workload (inputs resident), with the f32 reference path on a
+    65,536-pair sample (every host core) and the agreement with f64."""
+    import torch
+    from ncollide_gb300 import query as Q
+    from oracle import oracle as O
+    ctx = Q.Context(local, tolerance=tolerance)
+    runs = {"distance": (lambda: Q.distance_batch(ctx, db), O.DISTANCE, 0.0),
+            "proximity_margin_0.1": (lambda: Q.proximity_batch(ctx, db, 0.1), O.PROXIMITY, 0.1),
+            "closest_points_prediction_0.1": (lambda: Q.closest_points_batch(ctx, db, 0.1), O.CLOSEST, 0.1)}
+    sample = min(65536, batch.n_pairs)
+    sb = batch.subset(np.arange(sample))
+    threads = os.cpu_count() or 1
+    out = {}
+    for name, (fn, q, param) in runs.items():
+        for _ in range(3):
+            o = fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            o = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        t0 = time.perf_counter()
+        O.query(sb, q, O.F32, param=param, threads=threads)
+        cpu_s = time.perf_counter() - t0
+        rec = {"pairs_per_s": batch.n_pairs / (ms / 1e3), "ms_per_step": ms,
+               "cpu_reference_path_pairs_per_s": sample / cpu_s}
+        r64 = O.query(sb, q, O.F64, param=param, threads=threads)
+        if q == O.DISTANCE:
+            d = o["distance"].cpu().numpy()[:sample].astype(np.float64)
+            err = np.abs(d - r64.value) / np.maximum(np.abs(r64.value), sb.scale)
+            rec["distance_rel_err_vs_f64_p50_p99_max"] = [float(np.percentile(err, 50)), float(np.percentile(err, 99)),
+                                                          float(err.max())]
+        else:
+            t = (o["proximity"] if q == O.PROXIMITY else o["tag"]).cpu().numpy()[:sample]
+            rec["class_mismatch_vs_f64"] = int((t != r64.tag).sum())
+        out[name] = rec
+    ctx.close()
+    out["cpu_sample"] = f"first {sample} pairs, f32 reference path (oracle) on {threads} threads"
+    return out
+
+
 def cpu_baseline(batch, threads, query):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -970,8 +1016,9 @@ def main():
         out_h = {"has_contact": out["has_contact"].cpu().numpy(), "contact": out["contact"].cpu().numpy()}
         acc = accuracy_report(batch, out_h, min(args.accuracy_sample, batch.n_pairs), qo)
 
-    stress = cuboids = toi_rep = ray_rep = scene = manifolds = None
+    stress = cuboids = toi_rep = ray_rep = scene = manifolds = queries = None
     if not args.no_extras:
+        queries = other_queries_report(args, local, args.tolerance, db, batch)
         scene = scene_pipeline_report(args, local, args.tolerance, args.dispatch)
         manifolds = manifold_report(args, local, args.tolerance)
         stress = precision_stress(args, local, args.tolerance)
@@ -996,7 +1043,7 @@ def main():
             "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "accuracy_vs_f64": acc, "warm_start_coherent": coherent,
             "warm_start_learned": learned,
-            "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep, "ray_cast": ray_rep, "scene_pipeline": scene, "manifolds": manifolds,
+            "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep, "ray_cast": ray_rep, "scene_pipeline": scene, "manifolds": manifolds, "other_queries": queries,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
             "epa": {"pairs": stats["n_epa"], "warp_stage_pairs": stats["n_epa_overflow"],
