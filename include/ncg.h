@@ -206,7 +206,8 @@ int ncg_ctx_set_warm_start(ncg_ctx* ctx, int warm_start);
 int ncg_ctx_set_dispatch(ncg_ctx* ctx, int dispatch);
 /* Launch tuning (no reference counterpart).  Keys:
  *   NCG_TUNE_HULL_GJK_WARP   0: GJK of ConvexHull pairs one thread per pair
- *                            (default), 1: one warp per pair
+ *                            (default), 1: one warp per pair, v in 2..14: one
+ *                            warp per pair for pairs scanning >= 2^v hull points
  *   NCG_TUNE_GJK_BLOCKS      blocks of 128 threads per SM for the thread-per-pair
  *                            GJK kernel; 0 = as many as fit (default)
  *   NCG_TUNE_EPA_BLOCKS      the same for the thread-per-pair EPA kernel

@@ -167,12 +167,23 @@ __global__ void k_bucket(ncg_batch b, Scratch s) {
                       &s.ctr->n_hull);
 }
 
+// Hull pairs in the first `warp_buckets` ConvexHull buckets (the largest
+// hulls) run one warp per pair; the rest of the hull list one thread per pair.
+NCG_DEV unsigned long long hull_warp_count(const Scratch& s, int warp_buckets) {
+    unsigned long long n = 0;
+    for (int k = 0; k < warp_buckets && k < NB_HULL; ++k) n += *(volatile uint32_t*)&s.ctr->bucket_n[NB_ANALYTIC + k];
+    return n;
+}
+
 // One thread per pair over a pair list (list 0: analytic pairs, list 1:
-// ConvexHull pairs, whose points the thread scans itself); EPA starts in the
-// thread stage.
-__global__ void __launch_bounds__(128, NCG_GJK_THREAD_MIN_BLOCKS) k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list) {
-    const unsigned long long n = *(volatile unsigned long long*)(list == 0 ? &s.ctr->n_analytic : &s.ctr->n_hull);
-    const uint32_t* ids = list == 0 ? s.sorted : s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
+// ConvexHull pairs after the warp kernel's, whose points the thread scans
+// itself); EPA starts in the thread stage.
+__global__ void __launch_bounds__(128, NCG_GJK_THREAD_MIN_BLOCKS)
+k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int warp_buckets) {
+    const unsigned long long na = *(volatile unsigned long long*)&s.ctr->n_analytic;
+    const unsigned long long nw = list == 0 ? 0ull : hull_warp_count(s, warp_buckets);
+    const unsigned long long n = list == 0 ? na : *(volatile unsigned long long*)&s.ctr->n_hull - nw;
+    const uint32_t* ids = list == 0 ? s.sorted : s.sorted + na + nw;
     ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     unsigned long long acc = 0;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
@@ -185,8 +196,8 @@ __global__ void __launch_bounds__(128, NCG_GJK_THREAD_MIN_BLOCKS) k_gjk_thread(n
     warp_add(&s.ctr->gjk_iters, acc);
 }
 
-__global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
-    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->n_hull;
+__global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int warp_buckets) {
+    const unsigned long long n = hull_warp_count(s, warp_buckets);
     const uint32_t* ids = s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
     WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     const unsigned lane = threadIdx.x & 31u;
@@ -212,13 +223,13 @@ void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o
 }
 
 void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                       int list, cudaStream_t st) {
-    k_gjk_thread<<<grid, 128, 0, st>>>(b, qp, o, s, list);
+                       int list, int warp_buckets, cudaStream_t st) {
+    k_gjk_thread<<<grid, 128, 0, st>>>(b, qp, o, s, list, warp_buckets);
 }
 
 void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                     cudaStream_t st) {
-    k_gjk_warp<<<grid, 128, 0, st>>>(b, qp, o, s);
+                     int warp_buckets, cudaStream_t st) {
+    k_gjk_warp<<<grid, 128, 0, st>>>(b, qp, o, s, warp_buckets);
 }
 
 void gjk_occupancy(int* occ_thread, int* occ_warp) {

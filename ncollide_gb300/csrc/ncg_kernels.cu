@@ -24,6 +24,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -470,12 +471,16 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     gjk_launch_sort(bb, qp, o, s, st);
     mark(0);
     const int gjk_grid = c->num_sms * (c->gjk_blocks > 0 ? c->gjk_blocks : c->occ_thread);
-    gjk_launch_thread(gjk_grid, bb, qp, o, s, 0, st);
+    gjk_launch_thread(gjk_grid, bb, qp, o, s, 0, 0, st);
     mark(1);
-    if (c->hull_gjk_warp) gjk_launch_warp(c->num_sms * c->occ_warp, bb, qp, o, s, st);
-    else gjk_launch_thread(gjk_grid, bb, qp, o, s, 1, st);
+    // hull pairs of the first warp_buckets buckets (largest hulls) one warp per pair
+    const int warp_buckets = c->hull_gjk_warp == 0   ? 0
+                             : c->hull_gjk_warp == 1 ? NB_HULL
+                                                     : std::max(0, std::min(NB_HULL, 3 + NB_HULL - c->hull_gjk_warp));
+    if (warp_buckets > 0) gjk_launch_warp(c->num_sms * c->occ_warp, bb, qp, o, s, warp_buckets, st);
+    if (warp_buckets < NB_HULL) gjk_launch_thread(gjk_grid, bb, qp, o, s, 1, warp_buckets, st);
     mark(2);
-    launches += 4;
+    launches += 3 + (warp_buckets > 0 ? 1 : 0) + (warp_buckets < NB_HULL ? 1 : 0);
     if (query == Q_CONTACT) {
         k_epa_thread<<<c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread), 128, 0, st>>>(
             bb, qp, o, s);
@@ -575,7 +580,7 @@ int ncg_ctx_set_tuning(ncg_ctx* c, int key, int value) {
     if (!c) return NCG_EINVAL;
     switch (key) {
     case NCG_TUNE_HULL_GJK_WARP:
-        if (value != 0 && value != 1) return NCG_EINVAL;
+        if (value < 0 || value > 3 + NB_HULL - 1) return NCG_EINVAL;
         c->hull_gjk_warp = value;
         return NCG_OK;
     case NCG_TUNE_GJK_BLOCKS:
@@ -1147,8 +1152,8 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     // The array keeps the previous call's contents: reset the counters and queues' heads.
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset noalloc counters")) return NCG_ECUDA;
     gjk_launch_sort(bb, qp, o, s, st);
-    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 0, st);
-    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 1, st);
+    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 0, 0, st);
+    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 1, 0, st);
     k_epa_thread<<<d.num_sms * d.lim.occ_ethread, 128, 0, st>>>(bb, qp, o, s);
     // warp stages in shared memory (128, then 1280 vertices), then the one global slab
     k_epa<<<d.num_sms * d.lim.occ_smem[0], 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>(Q_WARP_LONG, Q_WARP, 3, -1));

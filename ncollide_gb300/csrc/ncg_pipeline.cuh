@@ -177,12 +177,14 @@ NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
 // Validates the pairs, writes the outputs of bad ones and counting-sorts the
 // rest into s.sorted (k_classify, k_bucket): two launches over n pairs.
 void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, cudaStream_t st);
-// One thread per pair over list 0 (analytic pairs) or 1 (ConvexHull pairs).
+// One thread per pair over list 0 (analytic pairs) or 1 (the ConvexHull
+// pairs after the first `warp_buckets` hull buckets).
 void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                       int list, cudaStream_t st);
-// One warp per pair over the ConvexHull list.
+                       int list, int warp_buckets, cudaStream_t st);
+// One warp per pair over the ConvexHull pairs of the first `warp_buckets`
+// hull buckets (the largest hulls).
 void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                     cudaStream_t st);
+                     int warp_buckets, cudaStream_t st);
 // Resident 128-thread blocks per SM of the thread and warp GJK kernels.
 void gjk_occupancy(int* occ_thread, int* occ_warp);
 // Shared-memory carveout preference of the thread GJK kernel.

@@ -273,3 +273,16 @@ def test_repeated_calls_are_deterministic(ctx_factory):
     b = Q.contact_batch(ctx, db, 0.0)
     torch.cuda.synchronize()
     assert torch.equal(a["contact"], b["contact"]) and torch.equal(a["has_contact"], b["has_contact"])
+
+
+@pytest.mark.parametrize("hull_warp", [1, 9])
+@pytest.mark.parametrize("query,param", [(O.CONTACT_QUERY, 0.0), (O.DISTANCE, 0.0)])
+def test_hull_gjk_warp_modes_bit_exact(ctx_factory, hull_warp, query, param):
+    """ConvexHull GJK one warp per pair (all hull pairs, or those scanning >= 2^9
+    points) gives the same results as one thread per pair."""
+    ctx = ctx_factory(tolerance=N.TOL_PRECISE)
+    ctx.set_tuning(N.TUNE_HULL_GJK_WARP, hull_warp)
+    try:
+        check_query(ctx, W.mixed_convex(8192, seed=19), query, param, N.TOL_PRECISE)
+    finally:
+        ctx.set_tuning(N.TUNE_HULL_GJK_WARP, 0)
