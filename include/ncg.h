@@ -157,6 +157,7 @@ enum ncg_toi_status {
 #define NCG_ECUDA      (-2)  /* a CUDA call failed; ncg_last_error() has the text     */
 #define NCG_ENOMEM     (-3)
 #define NCG_ENOTBUILT  (-4)
+#define NCG_EINTERNAL  (-5)  /* a self-check failed (e.g. results depended on tuning) */
 
 /* Tolerance sets.  NCG_TOL_REFERENCE uses the reference's own f32 constants
  * (eps = f32::EPSILON: gjk eps_tol = 10 eps, eps_rel = sqrt(eps_tol), EPA
@@ -193,7 +194,9 @@ typedef struct ncg_stats {
     uint64_t epa_iters;      /* sum over pairs                                */
     uint32_t kernels_launched;
     uint32_t flags;          /* bit 0: a learned warm-start tensor-core wait
-                                timed out (directions fell back to default) */
+                                timed out (directions fell back to default);
+                                bit 1: a hull-stage bulk-copy wait timed out
+                                (those pairs read global memory instead) */
 } ncg_stats;
 
 /* ---- context --------------------------------------------------------------- */
@@ -214,14 +217,48 @@ int ncg_ctx_set_dispatch(ncg_ctx* ctx, int dispatch);
  *   NCG_TUNE_L1_CARVEOUT     shared-memory carveout (percent) preferred by the
  *                            kernels that use no shared memory; -1 = driver
  *                            default, 0 = largest L1 (default)
+ *   NCG_TUNE_HULL_STAGE_MIN  warp-per-pair hull GJK: a pair whose ConvexHull
+ *                            shapes hold at least this many points has them
+ *                            copied into shared memory by the bulk-copy (TMA)
+ *                            engine before its first support scan; 0 = never
+ *                            (default), at most 2048
+ *   NCG_TUNE_HULL_STAGE_CAP  points of that shared-memory stage per warp
+ *                            (multiple of 32, 32..2048; default 1024); a hull
+ *                            that does not fit is scanned from global memory
  * Results do not depend on any of these. */
 enum ncg_tune {
     NCG_TUNE_HULL_GJK_WARP = 0,
     NCG_TUNE_GJK_BLOCKS = 1,
     NCG_TUNE_EPA_BLOCKS = 2,
-    NCG_TUNE_L1_CARVEOUT = 3
+    NCG_TUNE_L1_CARVEOUT = 3,
+    NCG_TUNE_HULL_STAGE_MIN = 4,
+    NCG_TUNE_HULL_STAGE_CAP = 5
 };
+#define NCG_N_TUNE 6
 int ncg_ctx_set_tuning(ncg_ctx* ctx, int key, int value);
+
+/* Autotuner (no reference counterpart; the reference has no launch tuning).
+ * Times `query` (ncg_query_kind; param = prediction or margin) on the given
+ * device-resident batch for candidate values of every NCG_TUNE_* key, by
+ * coordinate descent from the context's current values (at most two passes;
+ * a value is kept when it is at least 1% faster), and leaves the fastest
+ * values set in the context.  Each candidate runs once untimed, then `reps`
+ * times (1..64) between CUDA events on `stream`; its time is the fastest of
+ * those.  The outputs of every candidate are checked against the first
+ * candidate's (a digest of every output byte): results must not depend on
+ * tuning, and a difference returns NCG_EINTERNAL.  Writes the chosen values
+ * (indexed by key, NCG_N_TUNE of them) to out_values and the chosen
+ * configuration's time to *out_ms (either may be NULL).  Allocates its own
+ * output buffers; synchronises `stream`. */
+enum ncg_query_kind {
+    NCG_QUERY_CONTACT = 0,
+    NCG_QUERY_DISTANCE = 1,
+    NCG_QUERY_PROXIMITY = 2,
+    NCG_QUERY_CLOSEST_POINTS = 3
+};
+int ncg_autotune(ncg_ctx* ctx, const ncg_batch* batch, int query, float param, int reps, int* out_values,
+                 float* out_ms, void* stream);
+int ncg_ctx_get_tuning(ncg_ctx* ctx, int key, int* value);
 int ncg_sync(ncg_ctx* ctx, void* stream);
 int ncg_get_stats(ncg_ctx* ctx, ncg_stats* out);
 

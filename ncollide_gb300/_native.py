@@ -13,7 +13,7 @@ from . import build as _build
 
 LIB_PATH = _build.LIB_PATH
 
-NCG_OK, NCG_EINVAL, NCG_ECUDA, NCG_ENOMEM = 0, -1, -2, -3
+NCG_OK, NCG_EINVAL, NCG_ECUDA, NCG_ENOMEM, NCG_ENOTBUILT, NCG_EINTERNAL = 0, -1, -2, -3, -4, -5
 TOL_REFERENCE, TOL_PRECISE = 0, 1
 WARM_NONE, WARM_INIT_DIR, WARM_MLP = 0, 1, 2
 
@@ -35,10 +35,13 @@ EXPORTED = [
     "ncg_graph_destroy", "ncg_mlp_n_params", "ncg_ctx_set_mlp_params", "ncg_mlp_features", "ncg_mlp_infer",
     "ncg_mlp_grad", "ncg_mlp_adam", "ncg_time_of_impact_batch",
     "ncg_ray_cast_batch", "ncg_aabb_batch", "ncg_bp_create", "ncg_bp_update", "ncg_bp_results",
-    "ncg_bp_destroy", "ncg_bp_copy", "ncg_gather_pairs", "ncg_manifold_batch",
+    "ncg_bp_destroy", "ncg_bp_copy", "ncg_gather_pairs", "ncg_manifold_batch", "ncg_autotune",
+    "ncg_ctx_get_tuning",
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
-TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT = range(4)
+TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT, TUNE_HULL_STAGE_MIN, TUNE_HULL_STAGE_CAP = range(6)
+N_TUNE = 6
+QUERY_CONTACT, QUERY_DISTANCE, QUERY_PROXIMITY, QUERY_CLOSEST_POINTS = range(4)
 DISPATCH_SUPPORT_MAP, DISPATCH_QUERY = 0, 1
 TOI_OUT_OF_ITERATIONS, TOI_CONVERGED, TOI_FAILED, TOI_PENETRATING = range(4)
 STATUS_UNSUPPORTED_FEATURE = 1 << 7
@@ -101,6 +104,8 @@ def load(build_if_missing=True):
     L.ncg_get_stage_ms.argtypes = [vp, vp, i32]
     L.ncg_contact_batch_noalloc.argtypes = [P(NcgBatch), f32, i32, vp, vp, vp, vp, vp]
     L.ncg_ctx_set_tuning.argtypes = [vp, i32, i32]
+    L.ncg_ctx_get_tuning.argtypes = [vp, i32, P(i32)]
+    L.ncg_autotune.argtypes = [vp, P(NcgBatch), i32, f32, i32, vp, P(f32), vp]
     L.ncg_time_of_impact_batch.argtypes = [vp, P(NcgBatch), vp, vp, f32, f32, vp, vp, vp, vp, vp]
     L.ncg_ray_cast_batch.argtypes = [vp, P(NcgBatch), vp, f32, i32, vp, vp, vp, vp, vp, vp]
     L.ncg_aabb_batch.argtypes = [vp, P(NcgBatch), vp, vp, vp]

@@ -164,6 +164,53 @@ struct WarpScan {
     }
 };
 
+// WarpScan for a pair whose ConvexHull points (one or two slices of the flat
+// point buffer) sit in the warp's shared-memory stage, copied there by the
+// bulk-copy engine: up to two staged slices, identified by their first point
+// and count; every other shape is scanned from global memory.  The points
+// and the order of comparisons are those of WarpScan, so the arg-max is the
+// same whichever memory the points come from.
+struct StagedWarpScan {
+    const float4* pts;
+    uint32_t sbase;                // shared-memory address of the warp's stage
+    uint32_t off[2], n[2], at[2];  // staged slice: first point, count (0: none), index in the stage
+    NCG_DEV uint32_t argmax(const Shape& s, vec3<float> d) const {
+        const int k = (n[0] != 0 && s.off == off[0] && s.n == n[0])   ? 0
+                      : (n[1] != 0 && s.off == off[1] && s.n == n[1]) ? 1
+                                                                       : -1;
+        if (k < 0) return WarpScan{pts}.argmax(s, d);
+        const unsigned lane = threadIdx.x & 31u;
+        const uint32_t base = sbase + 16u * at[k];
+        float best = -INFINITY;
+        uint32_t bi = 0xffffffffu;
+        for (uint32_t i = lane; i < s.n; i += 32) {
+            float4 v;
+            // volatile: the stage is written by the async proxy; these reads
+            // stay after the barrier wait that made it visible
+            asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                         : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                         : "r"(base + 16u * i));
+            float x = dot(vec3<float>{v.x, v.y, v.z}, d);
+            x = (x != x) ? -INFINITY : x;
+            if (bi == 0xffffffffu || x > best) {
+                best = x;
+                bi = i;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            bool take = ob > best || (ob == best && oi < bi);
+            if (take) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        return bi;
+    }
+};
+
 // Local support functions.
 template <class Scan> NCG_DEV vec3<float> local_support(const Shape& s, vec3<float> d, const Scan& scan) {
     switch (s.kind) {

@@ -312,14 +312,30 @@ struct EpaResult {
     uint32_t status;
 };
 
-// EPA::closest_points.  With WarpExec all 32 lanes of a warp call it with
-// identical arguments and every lane returns the same result; with ThreadExec
-// one thread runs it alone.
-template <class E, class Scan>
-NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& tol, const Scan& scan, EpaStore& st,
-                          int max_iter) {
-    const int lane = E::lane();
+// The state EPA keeps from one expansion step to the next (the store holds
+// the polytope): counts of vertices, fresh and free face slots, heap size and
+// push sequence, the best face so far and its support distance, and the result.
+struct EpaState {
+    int nv, nfresh, nfree, hsize, niter;
+    uint32_t seq;
+    int b0, b1, b2;
+    vec3<float> bn;
+    real max_dist;
     EpaResult res;
+};
+
+// EPA::closest_points (epa3.rs:219-430) in two parts: epa_begin builds the
+// initial polytope from GJK's simplex (epa3.rs:219-321); epa_step runs one
+// iteration of the expansion loop (epa3.rs:323-428).  Each returns true when
+// EPA has finished, with the result in S.res.  With WarpExec all 32 lanes of a
+// warp call them with identical arguments and every lane gets the same state;
+// with ThreadExec one thread runs them alone, so a thread can interleave
+// several pairs' steps with others' (the thread stage's per-thread scheduler).
+template <class E, class Scan>
+NCG_DEV bool epa_begin(const PairGeom& g, int dim, const CSO* sv, const Tol& tol, const Scan& scan, EpaStore& st,
+                       EpaState& S) {
+    const int lane = E::lane();
+    EpaResult& res = S.res;
     res.exit = EPA_NONE;
     res.p1 = res.p2 = res.n = zero3<real>();
     res.iters = 0;
@@ -327,9 +343,9 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
     if (dim == 0) {
         res.n = mk(real(0.0f), real(1.0f), real(0.0f));
         res.exit = EPA_OK_DIM0;
-        return res;
+        return true;
     }
-    const real eps_tol = from_host(tol.eps_tol), epa_tol = from_host(tol.epa_eps_tol);
+    const real eps_tol = from_host(tol.eps_tol);
     const float eps = tol.eps.h;
     int nv = dim + 1, nfresh = 0, nfree = 0, hsize = 0;
     uint32_t seq = 0;
@@ -374,7 +390,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         hsize = E::bcast(hsize);
         seq = E::bcast(seq);
         nfresh = 4;
-        if (fail) { res.status |= NCG_STATUS_EPA_FAILED; return res; }
+        if (fail) { res.status |= NCG_STATUS_EPA_FAILED; return true; }
     } else {
         if (dim == 1) {
             vec3<real> dpt = to_r(st.vf(1)) - to_r(st.vf(0));
@@ -402,17 +418,40 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
     }
     if (hsize == 0) {  // the reference panics on heap.peek().unwrap()
         res.status |= NCG_STATUS_EPA_NO_FACE;
-        return res;
+        return true;
     }
     // best face (its points and normal are kept: its slot may be recycled)
     int bslot = rslot(__float_as_uint(st.heap[0].w));
-    int b0, b1, b2;
-    st.pts(bslot, b0, b1, b2);
-    vec3<float> bn = st.normalf(bslot);
-    real max_dist = dw_max();
-    int niter = 0;
+    st.pts(bslot, S.b0, S.b1, S.b2);
+    S.bn = st.normalf(bslot);
+    S.max_dist = dw_max();
+    S.niter = 0;
+    S.nv = nv;
+    S.nfresh = nfresh;
+    S.nfree = nfree;
+    S.hsize = hsize;
+    S.seq = seq;
+    return false;
+}
 
-    for (;;) {
+template <class E, class Scan>
+NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaStore& st, EpaState& S, int max_iter) {
+    const int lane = E::lane();
+    EpaResult& res = S.res;
+    const real eps_tol = from_host(tol.eps_tol), epa_tol = from_host(tol.epa_eps_tol);
+    const float eps = tol.eps.h;
+    int& nv = S.nv;
+    int& nfresh = S.nfresh;
+    int& nfree = S.nfree;
+    int& hsize = S.hsize;
+    uint32_t& seq = S.seq;
+    int& b0 = S.b0;
+    int& b1 = S.b1;
+    int& b2 = S.b2;
+    vec3<float>& bn = S.bn;
+    real& max_dist = S.max_dist;
+    int& niter = S.niter;
+    {
         // ---- pop the closest live face (lane 0)
         int fid = -1;
         real key(0.0f);
@@ -427,7 +466,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
             st.face_points(b0, b1, b2, res.p1, res.p2);
             res.n = to_r(bn);
             res.exit = EPA_OK_HEAP_EMPTY;
-            return res;
+            return true;
         }
         res.iters++;
         int f0, f1, f2;
@@ -435,7 +474,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         vec3<float> fnf = st.normalf(fid);
         vec3<real> fnrm = to_r(fnf);
         CSO c = cso_support(g, fnf, scan);
-        if (nv >= st.VC) { res.exit = EPA_OVERFLOW; return res; }
+        if (nv >= st.VC) { res.exit = EPA_OVERFLOW; return true; }
         const int sup = nv++;
         if (lane == 0) st.put_vertex(sup, c);
         real cand = dot(to_r(c.p), fnrm);
@@ -450,7 +489,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
             st.face_points(b0, b1, b2, res.p1, res.p2);
             res.n = to_r(bn);
             res.exit = EPA_OK_CONVERGED;
-            return res;
+            return true;
         }
 
         // ---- silhouette flood fill (lane 0), recursion order kept with a stack
@@ -495,17 +534,17 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         ovf = E::bcast(ovf);
         nfree = E::bcast(nfree);
         E::sync();
-        if (ovf) { res.exit = EPA_OVERFLOW; return res; }
+        if (ovf) { res.exit = EPA_OVERFLOW; return true; }
         if (nsil == 0) {
             if (tol.best_on_failure) {
                 st.face_points(b0, b1, b2, res.p1, res.p2);
                 res.n = to_r(bn);
                 res.exit = EPA_OK_PRECISION;
                 res.status |= NCG_STATUS_EPA_PRECISION_LIMIT;
-                return res;
+                return true;
             }
             res.status |= NCG_STATUS_EPA_FAILED;
-            return res;
+            return true;
         }
 
         // ---- which silhouette edges still border a live face (after the whole fill)
@@ -539,17 +578,17 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
         nfree = E::bcast(nfree);
         nfresh = E::bcast(nfresh);
         E::sync();
-        if (ovf) { res.exit = EPA_OVERFLOW; return res; }
+        if (ovf) { res.exit = EPA_OVERFLOW; return true; }
         if (built == 0) {  // epa3.rs:409-413
             if (tol.best_on_failure) {
                 st.face_points(b0, b1, b2, res.p1, res.p2);
                 res.n = to_r(bn);
                 res.exit = EPA_OK_PRECISION;
                 res.status |= NCG_STATUS_EPA_PRECISION_LIMIT;
-                return res;
+                return true;
             }
             res.status |= NCG_STATUS_EPA_FAILED;
-            return res;
+            return true;
         }
         // ---- build the new faces, one lane per live edge
         for (int k = lane; k < nsil; k += E::W) {
@@ -589,7 +628,7 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
             st.face_points(f0, f1, f2, res.p1, res.p2);
             res.n = fnrm;
             res.exit = EPA_OK_NUMERIC;
-            return res;
+            return true;
         }
         if (outcome == 2) {
             if (tol.best_on_failure) {
@@ -597,18 +636,30 @@ NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& 
                 res.n = to_r(bn);
                 res.exit = EPA_OK_PRECISION;
                 res.status |= NCG_STATUS_EPA_PRECISION_LIMIT;
-                return res;
+                return true;
             }
             res.status |= NCG_STATUS_EPA_FAILED;
-            return res;
+            return true;
         }
-        if (outcome == 3) { res.exit = EPA_OVERFLOW; return res; }
+        if (outcome == 3) { res.exit = EPA_OVERFLOW; return true; }
         niter += 1;
         if (niter > max_iter) {
             res.status |= NCG_STATUS_EPA_MAX_ITER;
-            return res;
+            return true;
         }
     }
+    return false;
+}
+
+// EPA::closest_points from GJK's final simplex to the end.
+template <class E, class Scan>
+NCG_DEV EpaResult epa_run(const PairGeom& g, int dim, const CSO* sv, const Tol& tol, const Scan& scan, EpaStore& st,
+                          int max_iter) {
+    EpaState S;
+    if (epa_begin<E>(g, dim, sv, tol, scan, st, S)) return S.res;
+    while (!epa_step<E>(g, tol, scan, st, S, max_iter)) {
+    }
+    return S.res;
 }
 
 }  // namespace ncg

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include "ncg_pipeline.cuh"
+#include "ncg_tc.cuh"
 
 #ifndef NCG_GJK_THREAD_MIN_BLOCKS
 #define NCG_GJK_THREAD_MIN_BLOCKS 4
@@ -196,19 +197,89 @@ k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int wa
     warp_add(&s.ctr->gjk_iters, acc);
 }
 
-__global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int warp_buckets) {
+// Plans the shared-memory stage of pair i: its ConvexHull slices (one when
+// both shapes are the same slice) if they hold at least `stage_min` points
+// together; the first shape's slice, then the second's, each if it still fits
+// in `cap` points.  Every lane computes the same plan.
+NCG_DEV void plan_stage(const ncg_batch& b, uint32_t i, uint32_t stage_min, uint32_t cap, StagedWarpScan& sc) {
+    sc.n[0] = sc.n[1] = 0;
+    Shape a, c;
+    const bool oka = load_shape(b, b.g1[i], a), okc = load_shape(b, b.g2[i], c);
+    uint32_t na = (oka && a.kind == NCG_CONVEX_HULL) ? a.n : 0u;
+    uint32_t nc = (okc && c.kind == NCG_CONVEX_HULL) ? c.n : 0u;
+    if (na && nc && a.off == c.off && a.n == c.n) nc = 0;
+    if (na + nc < stage_min) return;
+    uint32_t used = 0;
+    int k = 0;
+    if (na && na <= cap) {
+        sc.off[k] = a.off; sc.n[k] = na; sc.at[k] = 0; used = na; ++k;
+    }
+    if (nc && used + nc <= cap) {
+        sc.off[k] = c.off; sc.n[k] = nc; sc.at[k] = used;
+    }
+}
+
+// One warp per pair over the ConvexHull pairs of the first `warp_buckets`
+// buckets, drained from a shared counter.  With STAGE, a pair whose hulls
+// hold at least `stage_min` points first has them copied into its warp's
+// shared-memory stage (`stage_cap` points per warp) by the bulk-copy engine
+// (cp.async.bulk completing on an mbarrier): the first of the pair's support
+// scans then no longer waits on scattered global loads and the later ones read
+// shared memory instead of L1/L2.  Every wait is bounded; a timeout sets
+// ctr->stage_err and the kernel reads global memory from then on.
+template <bool STAGE>
+__global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int warp_buckets,
+                                                  uint32_t stage_min, uint32_t stage_cap) {
+    extern __shared__ __align__(128) float4 stage[];  // [4 warps][stage_cap]
+    __shared__ __align__(8) uint64_t bar[4];
     const unsigned long long n = hull_warp_count(s, warp_buckets);
     const uint32_t* ids = s.sorted + *(volatile unsigned long long*)&s.ctr->n_analytic;
-    WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
-    const unsigned lane = threadIdx.x & 31u;
+    const float4* pts = reinterpret_cast<const float4*>(b.hull_points);
+    const unsigned lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    bool staging = STAGE && stage_min > 0 && stage_cap > 0 && (reinterpret_cast<uintptr_t>(pts) & 15u) == 0;
+    uint32_t parity = 0;
+    if (STAGE) {
+        if (lane == 0) tc::mbar_init(&bar[w], 1);
+        __syncwarp();
+    }
+    const uint32_t sbase = STAGE ? tc::smem_u32(stage + (size_t)w * stage_cap) : 0u;
     unsigned long long acc = 0;
     for (;;) {
         unsigned long long k = 0;
         if (lane == 0) k = atomicAdd(&s.ctr->hull_next, 1ull);
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= n) break;
+        const uint32_t i = ids[k];
         unsigned long long a = 0;
-        gjk_pair(b, qp, o, s, ids[k], scan, lane == 0, a, Q_WARP);
+        if constexpr (STAGE) {
+            StagedWarpScan scan{pts, sbase, {0u, 0u}, {0u, 0u}, {0u, 0u}};
+            if (staging) {
+                plan_stage(b, i, stage_min, stage_cap, scan);
+                const uint32_t bytes = 16u * (scan.n[0] + scan.n[1]);
+                if (bytes) {
+                    __syncwarp();  // every lane has finished reading the previous pair's stage
+                    if (lane == 0) {
+                        tc::fence_async_smem();  // those reads come before the copy's writes
+                        tc::mbar_arrive_expect_tx(&bar[w], bytes);
+                        tc::bulk_g2s(sbase + 16u * scan.at[0], pts + scan.off[0], 16u * scan.n[0], &bar[w]);
+                        if (scan.n[1]) tc::bulk_g2s(sbase + 16u * scan.at[1], pts + scan.off[1], 16u * scan.n[1], &bar[w]);
+                    }
+                    bool ok = tc::mbar_wait(&bar[w], parity, &s.ctr->stage_err);
+                    ok = __all_sync(0xffffffffu, ok);
+                    if (!ok) {
+                        // give the copies in flight a second bounded wait, then stop staging
+                        (void)tc::mbar_wait(&bar[w], parity, &s.ctr->stage_err);
+                        staging = false;
+                        scan.n[0] = scan.n[1] = 0;
+                    }
+                    parity ^= 1u;
+                }
+            }
+            gjk_pair(b, qp, o, s, i, scan, lane == 0, a, Q_WARP);
+        } else {
+            WarpScan scan{pts};
+            gjk_pair(b, qp, o, s, i, scan, lane == 0, a, Q_WARP);
+        }
         if (lane == 0) acc += a;
     }
     warp_add(&s.ctr->gjk_iters, acc);
@@ -228,13 +299,31 @@ void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, cons
 }
 
 void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                     int warp_buckets, cudaStream_t st) {
-    k_gjk_warp<<<grid, 128, 0, st>>>(b, qp, o, s, warp_buckets);
+                     int warp_buckets, uint32_t stage_min, uint32_t stage_cap, cudaStream_t st) {
+    if (stage_min > 0 && stage_cap > 0)
+        k_gjk_warp<true><<<grid, 128, gjk_warp_stage_bytes(stage_cap), st>>>(b, qp, o, s, warp_buckets, stage_min,
+                                                                             stage_cap);
+    else
+        k_gjk_warp<false><<<grid, 128, 0, st>>>(b, qp, o, s, warp_buckets, 0u, 0u);
 }
+
+size_t gjk_warp_stage_bytes(uint32_t stage_cap) { return 4u * 16u * (size_t)stage_cap; }
 
 void gjk_occupancy(int* occ_thread, int* occ_warp) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ_thread, k_gjk_thread, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ_warp, k_gjk_warp, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ_warp, k_gjk_warp<false>, 128, 0);
+}
+
+int gjk_warp_stage_occupancy(uint32_t stage_cap) {
+    // the attribute is per function: allow the largest stage so that contexts
+    // with different stage sizes can share the device
+    if (cudaFuncSetAttribute(k_gjk_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)gjk_warp_stage_bytes(2048)) != cudaSuccess)
+        return 0;
+    const size_t bytes = gjk_warp_stage_bytes(stage_cap);
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gjk_warp<true>, 128, bytes) != cudaSuccess) return 0;
+    return occ;
 }
 
 cudaError_t gjk_set_carveout(int pct) {

@@ -213,30 +213,55 @@ __global__ void __launch_bounds__(32, NCG_EPA_WARP_MIN_BLOCKS) k_epa(ncg_batch b
     }
     if (lane == 0 && acc) atomicAdd(&s.ctr->epa_iters, acc);
 }
+// The thread stage's scheduler: each thread takes the next EPA item from the
+// queue as soon as its current one finishes, and the loop advances every
+// thread's pair by one expansion step per pass, so a warp's 32 lanes stay on
+// the same step of the loop body whatever pairs they hold (a pair needs 1 to
+// ~60 steps here); with a fixed item per lane and round, the lanes whose pairs
+// finished early would idle until the round's longest pair was done.
+NCG_DEV void epa_thread_finish(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
+                               uint32_t item, const EpaResult& r, unsigned long long& acc) {
+    const EpaItem& it = s.items[item];
+    if (r.exit == EPA_OVERFLOW) {
+        // pairs of two curved shapes (their polytopes grow longest) go first;
+        // the shape kinds are re-read here (rare path) rather than kept live
+        const uint32_t k1 = s.bucket_kind1(b, it.pair), k2 = s.bucket_kind2(b, it.pair);
+        const bool curved = k1 != NCG_CUBOID && k1 != NCG_CONVEX_HULL && k2 != NCG_CUBOID && k2 != NCG_CONVEX_HULL;
+        const int qo = curved ? Q_WARP_LONG : Q_WARP;
+        unsigned long long pos = atomicAdd(&s.ctr->epa_count[qo], 1ull);
+        s.queue[qo][pos] = item;
+    } else {
+        acc += r.iters;
+        finish_epa(b, qp, o, it, r, 0);
+    }
+}
+
 NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
                              EpaStore& st) {
     const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[0];
     ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     unsigned long long acc = 0;
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-        const uint32_t item = s.queue[0][k];
-        const EpaItem& it = s.items[item];
-        PairGeom g = item_geom(b, it);
-        CSO sv[4];
-        load_simplex(it, sv);
-        EpaResult r = epa_run<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
-        if (r.exit == EPA_OVERFLOW) {
-            // pairs of two curved shapes (their polytopes grow longest) go first;
-            // the shape kinds are re-read here (rare path) rather than kept live
-            const uint32_t k1 = s.bucket_kind1(b, it.pair), k2 = s.bucket_kind2(b, it.pair);
-            const bool curved = k1 != NCG_CUBOID && k1 != NCG_CONVEX_HULL && k2 != NCG_CUBOID && k2 != NCG_CONVEX_HULL;
-            const int qo = curved ? Q_WARP_LONG : Q_WARP;
-            unsigned long long pos = atomicAdd(&s.ctr->epa_count[qo], 1ull);
-            s.queue[qo][pos] = item;
-        } else {
-            acc += r.iters;
-            finish_epa(b, qp, o, it, r, 0);
+    EpaState S;
+    PairGeom g;
+    uint32_t item = 0;
+    bool active = false;
+    for (;;) {
+        // take items until one needs expansion steps (or the queue is empty)
+        while (!active) {
+            const unsigned long long k = atomicAdd(&s.ctr->epa_next[0], 1ull);
+            if (k >= n) break;
+            item = s.queue[0][k];
+            const EpaItem& it = s.items[item];
+            g = item_geom(b, it);
+            CSO sv[4];
+            load_simplex(it, sv);
+            if (epa_begin<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, S)) epa_thread_finish(b, qp, o, s, item, S.res, acc);
+            else active = true;
+        }
+        if (!active) break;
+        if (epa_step<ThreadExec>(g, qp.tol, scan, st, S, qp.epa_max_iter)) {
+            epa_thread_finish(b, qp, o, s, item, S.res, acc);
+            active = false;
         }
     }
     warp_add(&s.ctr->epa_iters, acc);
@@ -315,6 +340,9 @@ struct ncg_ctx {
     int occ_smem[2] = {1, 1};  // warps per SM of k_epa with a store of EpaTier<1> / <2> in shared memory
     int occ_global = 1;        // warps per SM of k_epa on global slabs
     int gjk_blocks = 0, epa_blocks = 0, l1_carveout = 0;
+    // warp-per-pair hull GJK: stage the pair's hull points in shared memory
+    // when they number at least hstage_min (0: never), hstage_cap points per warp
+    int hstage_min = 0, hstage_cap = 1024, occ_hstage = 0;
     char* scratch = nullptr;
     size_t scratch_cap_pairs = 0;
     char* slabs = nullptr;  // warp-stage slabs, then wide-stage slabs
@@ -477,7 +505,11 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     const int warp_buckets = c->hull_gjk_warp == 0   ? 0
                              : c->hull_gjk_warp == 1 ? NB_HULL
                                                      : std::max(0, std::min(NB_HULL, 3 + NB_HULL - c->hull_gjk_warp));
-    if (warp_buckets > 0) gjk_launch_warp(c->num_sms * c->occ_warp, bb, qp, o, s, warp_buckets, st);
+    if (warp_buckets > 0) {
+        const bool staged = c->hstage_min > 0 && c->occ_hstage > 0;
+        gjk_launch_warp(c->num_sms * (staged ? c->occ_hstage : c->occ_warp), bb, qp, o, s, warp_buckets,
+                        staged ? (uint32_t)c->hstage_min : 0u, (uint32_t)c->hstage_cap, st);
+    }
     if (warp_buckets < NB_HULL) gjk_launch_thread(gjk_grid, bb, qp, o, s, 1, warp_buckets, st);
     mark(2);
     launches += 3 + (warp_buckets > 0 ? 1 : 0) + (warp_buckets < NB_HULL ? 1 : 0);
@@ -527,6 +559,7 @@ int ncg_ctx_create(ncg_ctx** out, int device) {
     c->occ_smem[0] = lim.occ_smem[0];
     c->occ_smem[1] = lim.occ_smem[1];
     set_carveout(c->l1_carveout);
+    c->occ_hstage = gjk_warp_stage_occupancy((uint32_t)c->hstage_cap);
     c->slab_bytes[0] = (tier_bytes<2>() + 255) & ~size_t(255);
     c->slab_bytes[1] = (tier_bytes<3>() + 255) & ~size_t(255);
     c->n_slabs[0] = c->num_sms * c->occ_global;
@@ -596,6 +629,19 @@ int ncg_ctx_set_tuning(ncg_ctx* c, int key, int value) {
         if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
         c->l1_carveout = value;
         return set_carveout(value) ? NCG_OK : NCG_ECUDA;
+    case NCG_TUNE_HULL_STAGE_MIN:
+        if (value < 0 || value > 2048) return NCG_EINVAL;
+        c->hstage_min = value;
+        return NCG_OK;
+    case NCG_TUNE_HULL_STAGE_CAP: {
+        if (value < 32 || value > 2048 || value % 32 != 0) return NCG_EINVAL;
+        if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+        const int occ = gjk_warp_stage_occupancy((uint32_t)value);
+        if (occ <= 0) { g_last_error = "hull stage does not fit in shared memory"; return NCG_EINVAL; }
+        c->hstage_cap = value;
+        c->occ_hstage = occ;
+        return NCG_OK;
+    }
     default:
         g_last_error = "unknown tuning key";
         return NCG_EINVAL;
@@ -658,7 +704,7 @@ int ncg_get_stats(ncg_ctx* c, ncg_stats* out) {
     out->gjk_iters = c->host_ctr->gjk_iters;
     out->epa_iters = c->host_ctr->epa_iters;
     out->kernels_launched = c->launches;
-    out->flags = c->host_ctr->mlp_err & 1u;
+    out->flags = (c->host_ctr->mlp_err & 1u) | ((c->host_ctr->stage_err & 1u) << 1);
     return NCG_OK;
 }
 
@@ -1161,3 +1207,205 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     k_epa<<<1, 32, 0, st>>>(bb, qp, o, s, caps<3>(4, -1, -1, 0));
     return cuda_ok(cudaGetLastError(), "noalloc kernel launch") ? NCG_OK : NCG_ECUDA;
 }
+
+// ------------------------------------------------------------------ autotuner
+namespace {
+
+// Order-independent digest of a byte buffer: the sum over 32-bit words of a
+// 64-bit mix (splitmix64's finaliser) of (word index, word).  A tail that is
+// not a whole word is zero-padded.
+__global__ void k_digest(const uint8_t* p, uint64_t nbytes, unsigned long long* out) {
+    const uint64_t nw = (nbytes + 3) / 4;
+    unsigned long long acc = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t w = 0;
+        if (4 * i + 4 <= nbytes) w = *reinterpret_cast<const uint32_t*>(p + 4 * i);
+        else
+            for (uint64_t k = 4 * i; k < nbytes; ++k) w |= (uint32_t)p[k] << (8 * (k - 4 * i));
+        uint64_t z = (i << 32) ^ w;
+        z += 0x9e3779b97f4a7c15ull;
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        acc += z ^ (z >> 31);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31u) == 0) atomicAdd(out, acc);
+}
+
+struct TuneOutputs {
+    char* buf = nullptr;
+    Outputs o{};
+    std::vector<std::pair<const uint8_t*, uint64_t>> parts;  // what the digest covers
+    unsigned long long* digest = nullptr;                    // 8-byte device slot
+};
+
+int tune_alloc(int query, uint64_t n, TuneOutputs& t) {
+    const uint64_t sz[7] = {query == Q_CONTACT ? 40 * n : 0, 1 * n, 12 * n, 4 * n, 24 * n, 4 * n, 8};
+    uint64_t off[7], total = 0;
+    for (int k = 0; k < 7; ++k) { off[k] = total; total += (sz[k] + 255) & ~uint64_t(255); }
+    if (!cuda_ok(cudaMalloc(&t.buf, total), "cudaMalloc(autotune outputs)")) return NCG_ENOMEM;
+    char* b = t.buf;
+    t.digest = (unsigned long long*)(b + off[6]);
+    t.o = Outputs{};
+    t.o.status = (uint32_t*)(b + off[3]);
+    t.parts.push_back({(const uint8_t*)t.o.status, 4 * n});
+    switch (query) {
+    case Q_CONTACT:
+        t.o.contact = (ncg_contact*)(b + off[0]);
+        t.o.tag = (uint8_t*)(b + off[1]);
+        t.o.dir = (float*)(b + off[2]);
+        t.parts.push_back({(const uint8_t*)t.o.contact, 40 * n});
+        t.parts.push_back({t.o.tag, n});
+        t.parts.push_back({(const uint8_t*)t.o.dir, 12 * n});
+        break;
+    case Q_DISTANCE:
+        t.o.value = (float*)(b + off[5]);
+        t.parts.push_back({(const uint8_t*)t.o.value, 4 * n});
+        break;
+    case Q_PROXIMITY:
+        t.o.tag = (uint8_t*)(b + off[1]);
+        t.o.dir = (float*)(b + off[2]);
+        t.parts.push_back({t.o.tag, n});
+        t.parts.push_back({(const uint8_t*)t.o.dir, 12 * n});
+        break;
+    default:
+        t.o.tag = (uint8_t*)(b + off[1]);
+        t.o.points = (float*)(b + off[4]);
+        t.parts.push_back({t.o.tag, n});
+        t.parts.push_back({(const uint8_t*)t.o.points, 24 * n});
+    }
+    return NCG_OK;
+}
+
+// Times one configuration: one untimed call, then `reps` timed calls; the
+// fastest is its time.  *digest covers the outputs of the last call.
+int tune_time(ncg_ctx* c, const ncg_batch* b, int query, float param, int reps, TuneOutputs& t, cudaStream_t st,
+              cudaEvent_t e0, cudaEvent_t e1, float* ms, unsigned long long* digest) {
+    float best = 0.0f;
+    for (int r = 0; r <= reps; ++r) {
+        if (!cuda_ok(cudaEventRecord(e0, st), "cudaEventRecord")) return NCG_ECUDA;
+        int rc = run_query(c, b, query, param, t.o, st);
+        if (rc != NCG_OK) return rc;
+        if (!cuda_ok(cudaEventRecord(e1, st), "cudaEventRecord") ||
+            !cuda_ok(cudaEventSynchronize(e1), "cudaEventSynchronize"))
+            return NCG_ECUDA;
+        float m = 0.0f;
+        if (!cuda_ok(cudaEventElapsedTime(&m, e0, e1), "cudaEventElapsedTime")) return NCG_ECUDA;
+        if (r > 0 && (r == 1 || m < best)) best = m;
+    }
+    unsigned long long* slot = t.digest;
+    if (!cuda_ok(cudaMemsetAsync(slot, 0, 8, st), "memset digest")) return NCG_ECUDA;
+    for (auto& p : t.parts) k_digest<<<c->num_sms * 4, 256, 0, st>>>(p.first, p.second, slot);
+    unsigned long long h = 0;
+    if (!cuda_ok(cudaMemcpyAsync(&h, slot, 8, cudaMemcpyDeviceToHost, st), "copy digest") ||
+        !cuda_ok(cudaStreamSynchronize(st), "cudaStreamSynchronize"))
+        return NCG_ECUDA;
+    *ms = best;
+    *digest = h;
+    return NCG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ncg_ctx_get_tuning(ncg_ctx* c, int key, int* value) {
+    if (!c || !value) return NCG_EINVAL;
+    switch (key) {
+    case NCG_TUNE_HULL_GJK_WARP: *value = c->hull_gjk_warp; return NCG_OK;
+    case NCG_TUNE_GJK_BLOCKS: *value = c->gjk_blocks; return NCG_OK;
+    case NCG_TUNE_EPA_BLOCKS: *value = c->epa_blocks; return NCG_OK;
+    case NCG_TUNE_L1_CARVEOUT: *value = c->l1_carveout; return NCG_OK;
+    case NCG_TUNE_HULL_STAGE_MIN: *value = c->hstage_min; return NCG_OK;
+    case NCG_TUNE_HULL_STAGE_CAP: *value = c->hstage_cap; return NCG_OK;
+    default: g_last_error = "unknown tuning key"; return NCG_EINVAL;
+    }
+}
+
+int ncg_autotune(ncg_ctx* c, const ncg_batch* b, int query, float param, int reps, int* out_values, float* out_ms,
+                 void* stream) {
+    if (!c || !b) { g_last_error = "null context or batch"; return NCG_EINVAL; }
+    if (query < NCG_QUERY_CONTACT || query > NCG_QUERY_CLOSEST_POINTS) { g_last_error = "unknown query"; return NCG_EINVAL; }
+    if (reps < 1 || reps > 64) { g_last_error = "reps must be 1..64"; return NCG_EINVAL; }
+    if (query == NCG_QUERY_PROXIMITY && !(param >= 0.0f)) {
+        g_last_error = "The proximity margin must be positive or zero.";
+        return NCG_EINVAL;
+    }
+    if (b->n_pairs == 0) { g_last_error = "empty batch"; return NCG_EINVAL; }
+    if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    TuneOutputs t;
+    int rc = tune_alloc(query, b->n_pairs, t);
+    if (rc != NCG_OK) return rc;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const int saved_profiling = c->profiling;
+    c->profiling = 0;
+    auto done = [&](int code) {
+        c->profiling = saved_profiling;
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaFree(t.buf);
+        return code;
+    };
+    if (!cuda_ok(cudaEventCreate(&e0), "cudaEventCreate") || !cuda_ok(cudaEventCreate(&e1), "cudaEventCreate"))
+        return done(NCG_ECUDA);
+    // candidate values per key, in the order the descent visits the keys
+    struct Cand { int key; std::vector<int> values; };
+    std::vector<Cand> space = {
+        {NCG_TUNE_HULL_GJK_WARP, {0, 1, 8, 9, 10, 11}},
+        {NCG_TUNE_HULL_STAGE_MIN, {0, 1, 64, 256, 512}},
+        {NCG_TUNE_HULL_STAGE_CAP, {1024, 2048}},
+        {NCG_TUNE_GJK_BLOCKS, {0, 1, 2, 3}},
+        {NCG_TUNE_EPA_BLOCKS, {0, 1, 2, 3}},
+        {NCG_TUNE_L1_CARVEOUT, {0, -1}},
+    };
+    int cur[NCG_N_TUNE];
+    for (int k = 0; k < NCG_N_TUNE; ++k) ncg_ctx_get_tuning(c, k, &cur[k]);
+    float best_ms = 0.0f;
+    unsigned long long ref = 0;
+    rc = tune_time(c, b, query, param, reps, t, st, e0, e1, &best_ms, &ref);
+    if (rc != NCG_OK) return done(rc);
+    for (int pass = 0; pass < 2; ++pass) {
+        bool changed = false;
+        for (const Cand& cd : space) {
+            // the stage keys only matter with warp-per-pair hull GJK, the
+            // stage size only with staging on
+            if (cd.key == NCG_TUNE_HULL_STAGE_MIN && cur[NCG_TUNE_HULL_GJK_WARP] == 0) continue;
+            if (cd.key == NCG_TUNE_HULL_STAGE_CAP &&
+                (cur[NCG_TUNE_HULL_GJK_WARP] == 0 || cur[NCG_TUNE_HULL_STAGE_MIN] == 0))
+                continue;
+            for (int v : cd.values) {
+                if (v == cur[cd.key]) continue;
+                if (ncg_ctx_set_tuning(c, cd.key, v) != NCG_OK) continue;  // not valid on this device
+                float ms = 0.0f;
+                unsigned long long h = 0;
+                rc = tune_time(c, b, query, param, reps, t, st, e0, e1, &ms, &h);
+                if (rc != NCG_OK) {
+                    ncg_ctx_set_tuning(c, cd.key, cur[cd.key]);
+                    return done(rc);
+                }
+                if (h != ref) {
+                    ncg_ctx_set_tuning(c, cd.key, cur[cd.key]);
+                    g_last_error = "autotune: outputs changed with tuning key " + std::to_string(cd.key) + " = " +
+                                   std::to_string(v);
+                    return done(NCG_EINTERNAL);
+                }
+                if (ms < best_ms * 0.99f) {
+                    best_ms = ms;
+                    cur[cd.key] = v;
+                    changed = true;
+                }
+                ncg_ctx_set_tuning(c, cd.key, cur[cd.key]);
+            }
+        }
+        if (!changed) break;
+    }
+    for (int k = 0; k < NCG_N_TUNE; ++k) {
+        if (ncg_ctx_set_tuning(c, k, cur[k]) != NCG_OK) return done(NCG_EINTERNAL);
+        if (out_values) out_values[k] = cur[k];
+    }
+    if (out_ms) *out_ms = best_ms;
+    return done(NCG_OK);
+}
+
+}  // extern "C"

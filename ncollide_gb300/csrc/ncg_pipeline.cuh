@@ -62,6 +62,7 @@ struct DevCounters {
     unsigned long long gjk_iters, epa_iters;
     uint32_t bucket_n[NB], bucket_fill[NB];
     uint32_t mlp_err;  // bit 0: a learned warm-start tensor-core wait timed out
+    uint32_t stage_err;  // bit 0: a hull-stage bulk-copy wait timed out (the pair read global memory)
 };
 constexpr size_t CTR_SLOT = 512;
 static_assert(sizeof(DevCounters) <= CTR_SLOT, "counters must fit their slot");
@@ -182,9 +183,16 @@ void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o
 void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
                        int list, int warp_buckets, cudaStream_t st);
 // One warp per pair over the ConvexHull pairs of the first `warp_buckets`
-// hull buckets (the largest hulls).
+// hull buckets (the largest hulls); with stage_min > 0, pairs whose hulls hold
+// at least stage_min points are staged in shared memory (stage_cap points
+// per warp) by bulk copies.
 void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                     int warp_buckets, cudaStream_t st);
+                     int warp_buckets, uint32_t stage_min, uint32_t stage_cap, cudaStream_t st);
+// Dynamic shared memory of a staged warp-GJK block (4 warps of stage_cap points).
+size_t gjk_warp_stage_bytes(uint32_t stage_cap);
+// Allows the staged kernel that much shared memory and returns its resident
+// blocks per SM (0 if it cannot run).
+int gjk_warp_stage_occupancy(uint32_t stage_cap);
 // Resident 128-thread blocks per SM of the thread and warp GJK kernels.
 void gjk_occupancy(int* occ_thread, int* occ_warp);
 // Shared-memory carveout preference of the thread GJK kernel.

@@ -26,6 +26,11 @@ import torch
 from . import _native as N
 from .shapes import CONTACT_DTYPE, PairBatch
 
+# Launch-tuning keys of ncg_ctx_set_tuning by name.
+TUNING_KEYS = {"hull_gjk_warp": N.TUNE_HULL_GJK_WARP, "gjk_blocks": N.TUNE_GJK_BLOCKS,
+               "epa_blocks": N.TUNE_EPA_BLOCKS, "l1_carveout": N.TUNE_L1_CARVEOUT,
+               "hull_stage_min": N.TUNE_HULL_STAGE_MIN, "hull_stage_cap": N.TUNE_HULL_STAGE_CAP}
+
 
 class Context:
     """Owns an ncg_ctx: scratch memory, EPA slabs and settings for one device."""
@@ -62,9 +67,37 @@ class Context:
     def set_tuning(self, key, value):
         """Launch tuning (ncg_ctx_set_tuning); results do not depend on it."""
         if isinstance(key, str):
-            key = {"hull_gjk_warp": N.TUNE_HULL_GJK_WARP, "gjk_blocks": N.TUNE_GJK_BLOCKS,
-                   "epa_blocks": N.TUNE_EPA_BLOCKS, "l1_carveout": N.TUNE_L1_CARVEOUT}[key]
+            key = TUNING_KEYS[key]
         N.check(self._L.ncg_ctx_set_tuning(self._p, int(key), int(value)), "ncg_ctx_set_tuning")
+
+    def tuning(self):
+        """The context's launch tuning by key name (ncg_ctx_get_tuning)."""
+        out = {}
+        for name, key in TUNING_KEYS.items():
+            v = ctypes.c_int32()
+            N.check(self._L.ncg_ctx_get_tuning(self._p, int(key), ctypes.byref(v)), "ncg_ctx_get_tuning")
+            out[name] = int(v.value)
+        return out
+
+    def apply_tuning(self, values):
+        """Sets every key of a {name: value} mapping (e.g. a saved autotune result)."""
+        for k, v in values.items():
+            self.set_tuning(k, int(v))
+
+    def autotune(self, batch, query="contact", param=0.0, reps=3, stream=None):
+        """Runs the library's autotuner (ncg_autotune) on a device-resident
+        batch and leaves the fastest launch tuning set in this context.
+        Returns {"values": {name: value}, "ms": time of one call}."""
+        q = {"contact": N.QUERY_CONTACT, "distance": N.QUERY_DISTANCE, "proximity": N.QUERY_PROXIMITY,
+             "closest_points": N.QUERY_CLOSEST_POINTS}[query] if isinstance(query, str) else int(query)
+        vals = (ctypes.c_int32 * N.N_TUNE)()
+        ms = ctypes.c_float()
+        st = stream if stream is not None else torch.cuda.current_stream(batch.m1.device)
+        cb = batch.c_struct()
+        N.check(self._L.ncg_autotune(self._p, ctypes.byref(cb), int(q), ctypes.c_float(param), int(reps), vals,
+                                     ctypes.byref(ms), ctypes.c_void_p(st.cuda_stream)), "ncg_autotune")
+        names = {v: k for k, v in TUNING_KEYS.items()}
+        return {"values": {names[i]: int(vals[i]) for i in range(N.N_TUNE)}, "ms": float(ms.value)}
 
     def set_warm_start(self, mode):
         N.check(self._L.ncg_ctx_set_warm_start(self._p, int(mode)), "ncg_ctx_set_warm_start")

@@ -286,3 +286,42 @@ def test_hull_gjk_warp_modes_bit_exact(ctx_factory, hull_warp, query, param):
         check_query(ctx, W.mixed_convex(8192, seed=19), query, param, N.TOL_PRECISE)
     finally:
         ctx.set_tuning(N.TUNE_HULL_GJK_WARP, 0)
+
+
+def _with_shared_hulls(batch, every=3):
+    """Every `every`-th ConvexHull pair collides the first shape with itself
+    (both shapes are the same slice of the point buffer)."""
+    k1, _ = batch.kinds()
+    g2 = batch.g2.copy()
+    idx = np.nonzero(k1 == S.CONVEX_HULL)[0][::every]
+    g2[idx] = batch.g1[idx]
+    return S.PairBatch(batch.shapes, batch.hull_points, batch.m1, batch.g1, batch.m2, g2, None, None, dict(batch.meta))
+
+
+@pytest.mark.parametrize("hull_warp,stage_min,stage_cap", [(1, 1, 1024), (1, 1, 64), (9, 256, 2048), (1, 8, 512)])
+@pytest.mark.parametrize("query,param", [(O.CONTACT_QUERY, 0.0), (O.DISTANCE, 0.0), (O.PROXIMITY, 0.1)])
+def test_hull_stage_bit_exact(ctx_factory, hull_warp, stage_min, stage_cap, query, param):
+    """Warp-per-pair hull GJK with the pair's hull points staged in shared
+    memory by bulk copies (all hull pairs or those from a point count on; a
+    stage too small for some hulls; pairs whose two shapes are one hull) gives
+    the oracle's results bit for bit, like the unstaged kernels."""
+    ctx = ctx_factory(tolerance=N.TOL_PRECISE)
+    ctx.set_tuning(N.TUNE_HULL_GJK_WARP, hull_warp)
+    ctx.set_tuning(N.TUNE_HULL_STAGE_CAP, stage_cap)
+    ctx.set_tuning(N.TUNE_HULL_STAGE_MIN, stage_min)
+    try:
+        b = _with_shared_hulls(W.mixed_convex(8192, seed=23))
+        check_query(ctx, b, query, param, N.TOL_PRECISE)
+        assert ctx.stats()["flags"] == 0
+    finally:
+        ctx.set_tuning(N.TUNE_HULL_STAGE_MIN, 0)
+        ctx.set_tuning(N.TUNE_HULL_STAGE_CAP, 1024)
+        ctx.set_tuning(N.TUNE_HULL_GJK_WARP, 0)
+
+
+def test_hull_stage_tuning_rejects_bad_values(ctx_factory):
+    ctx = ctx_factory()
+    for key, v in ((N.TUNE_HULL_STAGE_CAP, 0), (N.TUNE_HULL_STAGE_CAP, 100), (N.TUNE_HULL_STAGE_CAP, 4096),
+                   (N.TUNE_HULL_STAGE_MIN, -1), (N.TUNE_HULL_STAGE_MIN, 4096)):
+        with pytest.raises(Exception):
+            ctx.set_tuning(key, v)
