@@ -268,8 +268,8 @@ struct EpaStore {
         sift_up(size++, e);
         return true;
     }
-    // Pops the first live entry; false when none is left.
-    NCG_DEV bool pop_live(int& size, int& fid, real& key) {
+    // Pops the first live entry (returned whole in *popped); false when none is left.
+    NCG_DEV bool pop_live(int& size, int& fid, real& key, float4& popped) {
         while (size > 0) {
             float4 e = heap[0];
             size--;
@@ -278,11 +278,15 @@ struct EpaStore {
             if (live(r)) {
                 fid = rslot(r);
                 key = real(e.x, e.y);
+                popped = e;
                 return true;
             }
         }
         return false;
     }
+    // Puts a popped entry back unchanged (same key and push sequence, so the
+    // pop order is as if it had never left).
+    NCG_DEV void repush(int& size, float4 e) { sift_up(size++, e); }
 };
 
 // Execution policies.
@@ -455,8 +459,9 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
         // ---- pop the closest live face (lane 0)
         int fid = -1;
         real key(0.0f);
+        float4 popped = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (lane == 0) {
-            if (!st.pop_live(hsize, fid, key)) fid = -1;
+            if (!st.pop_live(hsize, fid, key, popped)) fid = -1;
         }
         fid = E::bcast(fid);
         key = E::bcast(key);
@@ -468,13 +473,22 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
             res.exit = EPA_OK_HEAP_EMPTY;
             return true;
         }
+        if (nv >= st.VC) {
+            // no room for this iteration's support point: put the face back and
+            // stop between two iterations, so that a larger store can resume
+            // from this state (epa_spill / epa_resume) with the same result
+            if (lane == 0) st.repush(hsize, popped);
+            hsize = E::bcast(hsize);
+            E::sync();
+            res.exit = EPA_OVERFLOW;
+            return true;
+        }
         res.iters++;
         int f0, f1, f2;
         st.pts(fid, f0, f1, f2);
         vec3<float> fnf = st.normalf(fid);
         vec3<real> fnrm = to_r(fnf);
         CSO c = cso_support(g, fnf, scan);
-        if (nv >= st.VC) { res.exit = EPA_OVERFLOW; return true; }
         const int sup = nv++;
         if (lane == 0) st.put_vertex(sup, c);
         real cand = dot(to_r(c.p), fnrm);
@@ -649,6 +663,84 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
         }
     }
     return false;
+}
+
+// A polytope between two expansion steps, copied out of a store: a 64-byte
+// header (the EpaState scalars), then the used parts of the store's vertex,
+// witness, face, heap and free-list arrays, each at the offset it would have
+// for a store of capacities (VC, FC).  Slots, generations, heap entries and
+// push sequences are copied unchanged, so a store with at least those
+// capacities continues exactly where this one stopped.
+struct EpaSpill {
+    static constexpr __host__ __device__ size_t bytes(int VC, int FC) {
+        return 64 + 16 * (size_t)VC + 24 * (size_t)VC + 32 * (size_t)FC + 16 * (size_t)FC + 4 * (size_t)FC;
+    }
+    NCG_DEV static float4* vpt(char* r) { return (float4*)(r + 64); }
+    NCG_DEV static float* vo(char* r, int VC) { return (float*)(r + 64 + 16 * (size_t)VC); }
+    NCG_DEV static float4* face(char* r, int VC) { return (float4*)(r + 64 + 40 * (size_t)VC); }
+    NCG_DEV static float4* heap(char* r, int VC, int FC) { return (float4*)(r + 64 + 40 * (size_t)VC + 32 * (size_t)FC); }
+    NCG_DEV static uint32_t* freel(char* r, int VC, int FC) {
+        return (uint32_t*)(r + 64 + 40 * (size_t)VC + 48 * (size_t)FC);
+    }
+};
+
+// Writes store `st` and state S (between two steps) to spill record r, laid
+// out for capacities (VC, FC) of the source store.  With WarpExec the lanes
+// share the copy.
+template <class E>
+NCG_DEV void epa_spill(const EpaStore& st, const EpaState& S, char* r) {
+    const int lane = E::lane();
+    if (lane == 0) {
+        int4* h = (int4*)r;
+        h[0] = make_int4(S.nv, S.nfresh, S.nfree, S.hsize);
+        h[1] = make_int4(S.niter, (int)S.seq, S.b0, S.b1);
+        h[2] = make_int4(S.b2, __float_as_int(S.bn.x), __float_as_int(S.bn.y), __float_as_int(S.bn.z));
+        h[3] = make_int4(__float_as_int(S.max_dist.h), __float_as_int(S.max_dist.l), (int)S.res.iters,
+                         (int)S.res.status);
+    }
+    float4* vp = EpaSpill::vpt(r);
+    float* vo = EpaSpill::vo(r, st.VC);
+    float4* fa = EpaSpill::face(r, st.VC);
+    float4* hp = EpaSpill::heap(r, st.VC, st.FC);
+    uint32_t* fl = EpaSpill::freel(r, st.VC, st.FC);
+    for (int i = lane; i < S.nv; i += E::W) vp[i] = st.vpt[i];
+    for (int i = lane; i < 6 * S.nv; i += E::W) vo[i] = st.vo[i];
+    for (int i = lane; i < 2 * S.nfresh; i += E::W) fa[i] = st.face[i];
+    for (int i = lane; i < S.hsize; i += E::W) hp[i] = st.heap[i];
+    for (int i = lane; i < S.nfree; i += E::W) fl[i] = st.freel[i];
+    E::sync();
+}
+
+// Loads spill record r (written from a store of capacities VC, FC) into store
+// `st` and state S; false when `st` is smaller than the source store.
+template <class E>
+NCG_DEV bool epa_resume(const char* rc, int VC, int FC, EpaStore& st, EpaState& S) {
+    if (st.VC < VC || st.FC < FC) return false;
+    char* r = const_cast<char*>(rc);
+    const int lane = E::lane();
+    const int4* h = (const int4*)r;
+    const int4 h0 = h[0], h1 = h[1], h2 = h[2], h3 = h[3];
+    S.nv = h0.x; S.nfresh = h0.y; S.nfree = h0.z; S.hsize = h0.w;
+    S.niter = h1.x; S.seq = (uint32_t)h1.y; S.b0 = h1.z; S.b1 = h1.w;
+    S.b2 = h2.x;
+    S.bn = mk(__int_as_float(h2.y), __int_as_float(h2.z), __int_as_float(h2.w));
+    S.max_dist = real(__int_as_float(h3.x), __int_as_float(h3.y));
+    S.res.exit = EPA_NONE;
+    S.res.p1 = S.res.p2 = S.res.n = zero3<real>();
+    S.res.iters = (uint32_t)h3.z;
+    S.res.status = (uint32_t)h3.w;
+    const float4* vp = EpaSpill::vpt(r);
+    const float* vo = EpaSpill::vo(r, VC);
+    const float4* fa = EpaSpill::face(r, VC);
+    const float4* hp = EpaSpill::heap(r, VC, FC);
+    const uint32_t* fl = EpaSpill::freel(r, VC, FC);
+    for (int i = lane; i < S.nv; i += E::W) st.vpt[i] = vp[i];
+    for (int i = lane; i < 6 * S.nv; i += E::W) st.vo[i] = vo[i];
+    for (int i = lane; i < 2 * S.nfresh; i += E::W) st.face[i] = fa[i];
+    for (int i = lane; i < S.hsize; i += E::W) st.heap[i] = hp[i];
+    for (int i = lane; i < S.nfree; i += E::W) st.freel[i] = fl[i];
+    E::sync();
+    return true;
 }
 
 // EPA::closest_points from GJK's final simplex to the end.

@@ -59,6 +59,7 @@ NCG_DEV void enqueue_epa(const Scratch& s, uint32_t i, int queue, const Simplex&
     it.dim = (uint8_t)sx.dim;
     it.mode = (uint8_t)mode;
     it.flip = flip ? 1 : 0;
+    it.spilled = 0;
     for (int k = 0; k <= sx.dim; ++k) {
         const CSO& c = sx.v[k];
         float* w = it.v[k];

@@ -189,9 +189,19 @@ __global__ void __launch_bounds__(32, NCG_EPA_WARP_MIN_BLOCKS) k_epa(ncg_batch b
         const uint32_t item = s.queue[q][k];
         const EpaItem& it = s.items[item];
         PairGeom g = item_geom(b, it);
-        CSO sv[4];
-        load_simplex(it, sv);
-        EpaResult r = epa_run<WarpExec>(g, it.dim, sv, qp.tol, scan, st, qp.epa_max_iter);
+        EpaState S;
+        bool done;
+        if (it.spilled && epa_resume<WarpExec>(s.spill + (size_t)s.spill_of[item] * s.spill_bytes, EpaTier<0>::VC,
+                                                EpaTier<0>::FC, st, S)) {
+            // the thread stage's polytope: continue where it stopped
+            done = false;
+        } else {
+            CSO sv[4];
+            load_simplex(it, sv);
+            done = epa_begin<WarpExec>(g, it.dim, sv, qp.tol, scan, st, S);
+        }
+        while (!done) done = epa_step<WarpExec>(g, qp.tol, scan, st, S, qp.epa_max_iter);
+        const EpaResult& r = S.res;
         if (r.exit == EPA_OVERFLOW && tc.q_out >= 0) {
             if (lane == 0) {
                 unsigned long long pos = atomicAdd(&s.ctr->epa_count[tc.q_out], 1ull);
@@ -220,9 +230,20 @@ __global__ void __launch_bounds__(32, NCG_EPA_WARP_MIN_BLOCKS) k_epa(ncg_batch b
 // ~60 steps here); with a fixed item per lane and round, the lanes whose pairs
 // finished early would idle until the round's longest pair was done.
 NCG_DEV void epa_thread_finish(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                               uint32_t item, const EpaResult& r, unsigned long long& acc) {
-    const EpaItem& it = s.items[item];
+                               uint32_t item, const EpaResult& r, unsigned long long& acc, const EpaStore& st,
+                               const EpaState& S) {
+    EpaItem& it = s.items[item];
     if (r.exit == EPA_OVERFLOW) {
+        // keep the polytope (when a spill record is free) so that the warp
+        // stage resumes it instead of repeating these iterations
+        if (s.spill) {
+            const unsigned long long rec = atomicAdd(&s.ctr->spill_next, 1ull);
+            if (rec < s.spill_cap) {
+                epa_spill<ThreadExec>(st, S, s.spill + (size_t)rec * s.spill_bytes);
+                s.spill_of[item] = (uint32_t)rec;
+                it.spilled = 1;
+            }
+        }
         // pairs of two curved shapes (their polytopes grow longest) go first;
         // the shape kinds are re-read here (rare path) rather than kept live
         const uint32_t k1 = s.bucket_kind1(b, it.pair), k2 = s.bucket_kind2(b, it.pair);
@@ -255,12 +276,14 @@ NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Ou
             g = item_geom(b, it);
             CSO sv[4];
             load_simplex(it, sv);
-            if (epa_begin<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, S)) epa_thread_finish(b, qp, o, s, item, S.res, acc);
-            else active = true;
+            if (epa_begin<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, S))
+                epa_thread_finish(b, qp, o, s, item, S.res, acc, st, S);
+            else
+                active = true;
         }
         if (!active) break;
         if (epa_step<ThreadExec>(g, qp.tol, scan, st, S, qp.epa_max_iter)) {
-            epa_thread_finish(b, qp, o, s, item, S.res, acc);
+            epa_thread_finish(b, qp, o, s, item, S.res, acc, st, S);
             active = false;
         }
     }
@@ -371,12 +394,19 @@ struct ncg_ctx {
 
 namespace {
 
+// Spill records of the thread stage: one per 32 pairs of capacity (the
+// thread stage's overflow is ~1-3% of the pairs on mixed workloads; beyond
+// the records, pairs restart from GJK's simplex as without them).
+constexpr size_t SPILL_BYTES = (EpaSpill::bytes(EpaTier<0>::VC, EpaTier<0>::FC) + 255) & ~size_t(255);
+uint64_t spill_records(uint64_t cap) { return cap / 32 < 256 ? 256 : cap / 32; }
+
 bool ensure_scratch(ncg_ctx* c, uint64_t n) {
     if (n <= c->scratch_cap_pairs && c->scratch) return true;
     if (c->scratch) cudaFree(c->scratch);
     c->scratch = nullptr;
     uint64_t cap = n < 1024 ? 1024 : n;
-    size_t bytes = (2 + N_EPA_QUEUES) * 4 * cap + sizeof(EpaItem) * cap + CTR_SLOT + 1024;
+    size_t bytes = (2 + N_EPA_QUEUES) * 4 * cap + sizeof(EpaItem) * cap + CTR_SLOT + 1024 + 4 * cap +
+                   SPILL_BYTES * spill_records(cap) + 256;
     if (!cuda_ok(cudaMalloc(&c->scratch, bytes), "cudaMalloc(scratch)")) return false;
     c->scratch_cap_pairs = cap;
     return true;
@@ -416,6 +446,11 @@ Scratch carve_scratch(ncg_ctx* c) {
     s.bucket = (uint8_t*)p; p += 4 * cap;
     s.sorted = (uint32_t*)p; p += 4 * cap;
     for (int q = 0; q < N_EPA_QUEUES; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * cap; }
+    s.spill_of = (uint32_t*)p; p += 4 * cap;
+    p = (char*)(((uintptr_t)p + 255) & ~uintptr_t(255));
+    s.spill = p;
+    s.spill_bytes = SPILL_BYTES;
+    s.spill_cap = (uint32_t)spill_records(cap);
     s.slabs[0] = c->slabs;
     s.slabs[1] = c->slabs + c->slab_bytes[0] * c->n_slabs[0];
     for (int t = 0; t < 2; ++t) {
@@ -1183,6 +1218,10 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     s.slabs[1] = nullptr;
     s.slab_bytes[1] = 0;
     s.n_slabs[1] = 0;
+    s.spill = nullptr;  // no spill records: overflowing pairs restart from GJK's simplex
+    s.spill_of = nullptr;
+    s.spill_bytes = 0;
+    s.spill_cap = 0;
 
     QueryParams qp;
     qp.query = Q_CONTACT;

@@ -39,11 +39,14 @@ struct QueryParams {
 // `mode` 0: contact_support_map_support_map; 1: point projection of a ball's
 // centre on a ConvexHull (query::contact dispatch), `flip` when the ball is
 // the second shape.
+// `spilled` 1: the thread stage's polytope was kept when the pair outgrew it,
+// in spill record Scratch::spill_of[item]; 0: the next stage starts from the
+// simplex.
 struct __align__(16) EpaItem {
     uint32_t pair;
     uint32_t gjk_iters;
     uint32_t status;
-    uint8_t dim, mode, flip, pad;
+    uint8_t dim, mode, flip, spilled;
     float v[4][9];
 };
 
@@ -63,6 +66,7 @@ struct DevCounters {
     uint32_t bucket_n[NB], bucket_fill[NB];
     uint32_t mlp_err;  // bit 0: a learned warm-start tensor-core wait timed out
     uint32_t stage_err;  // bit 0: a hull-stage bulk-copy wait timed out (the pair read global memory)
+    unsigned long long spill_next;  // spill records taken
 };
 constexpr size_t CTR_SLOT = 512;
 static_assert(sizeof(DevCounters) <= CTR_SLOT, "counters must fit their slot");
@@ -79,6 +83,10 @@ struct Scratch {
     char* slabs[2];  // global EPA stores of the warp stages that use them, one per block
     size_t slab_bytes[2];
     int n_slabs[2];
+    char* spill;          // spill records of the thread stage (nullptr: none)
+    uint32_t* spill_of;   // per EPA item: its spill record (valid when the item is `spilled`)
+    size_t spill_bytes;   // bytes per record
+    uint32_t spill_cap;   // records
 };
 
 NCG_DEV uint32_t pack_iters(uint32_t g, uint32_t e) { return (g > 0xffffu ? 0xffffu : g) | ((e > 0xffffu ? 0xffffu : e) << 16); }
