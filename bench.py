@@ -1008,11 +1008,15 @@ def main():
     epa = rs.counters[:, 1] > 0
     hull_pts = (sample.shapes["hull_n"][sample.g1].astype(np.float64) * (sample.shapes["kind"][sample.g1] == 5) +
                 sample.shapes["hull_n"][sample.g2].astype(np.float64) * (sample.shapes["kind"][sample.g2] == 5))
-    epa_item_bytes = 160.0 + 136.0 + 61.0 + (16.0 * hull_pts[epa].mean() if epa.any() else 0.0)
+    # the thread stage's items: pairs whose hull GJK ran one thread per pair
+    # (hull_gjk_warp v >= 2 sends pairs scanning >= 2^v hull points to the warp GJK)
+    hw = tuning.get("hull_gjk_warp", 0)
+    in_thread = epa & ((hull_pts < (1 << hw)) if hw >= 2 else ((hull_pts == 0) if hw == 1 else True))
+    epa_item_bytes = 160.0 + 136.0 + 61.0 + (16.0 * hull_pts[in_thread].mean() if in_thread.any() else 0.0)
     units, unit_bytes, unit_name = {
         "classify": (batch.n_pairs, 72.0, "pair"),
         "gjk_thread": (batch.n_pairs, bytes_pp, "pair"), "gjk_warp": (batch.n_pairs, bytes_pp, "pair"),
-        "epa_thread": (stats["n_epa"], epa_item_bytes, "EPA item"),
+        "epa_thread": (stats["n_epa_thread"], epa_item_bytes, "EPA item"),
         "epa_warp": (stats["n_epa_overflow"], epa_item_bytes, "EPA item"),
         "epa_wide": (stats["n_epa_overflow"], epa_item_bytes, "EPA item")}.get(dom, (batch.n_pairs, bytes_pp, "pair"))
     dom_s = mean_stage[dom] / 1e3

@@ -189,7 +189,7 @@ typedef struct ncg_ctx ncg_ctx;
 typedef struct ncg_stats {
     uint64_t n_pairs;
     uint64_t n_epa;          /* pairs that went through EPA                   */
-    uint64_t n_epa_overflow; /* pairs that outgrew the thread stage (warp EPA) */
+    uint64_t n_epa_overflow; /* pairs whose EPA ran in the warp stage          */
     uint64_t gjk_iters;      /* sum over pairs                                */
     uint64_t epa_iters;      /* sum over pairs                                */
     uint32_t kernels_launched;
@@ -197,6 +197,8 @@ typedef struct ncg_stats {
                                 timed out (directions fell back to default);
                                 bit 1: a hull-stage bulk-copy wait timed out
                                 (those pairs read global memory instead) */
+    uint64_t n_epa_thread;   /* pairs whose EPA started in the thread stage
+                                (the others started in the warp stage)      */
 } ncg_stats;
 
 /* ---- context --------------------------------------------------------------- */

@@ -63,7 +63,7 @@ class NcgBatch(ctypes.Structure):
 class NcgStats(ctypes.Structure):
     _fields_ = [("n_pairs", ctypes.c_uint64), ("n_epa", ctypes.c_uint64), ("n_epa_overflow", ctypes.c_uint64),
                 ("gjk_iters", ctypes.c_uint64), ("epa_iters", ctypes.c_uint64),
-                ("kernels_launched", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+                ("kernels_launched", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("n_epa_thread", ctypes.c_uint64)]
 
 
 class NcgError(RuntimeError):

@@ -17,6 +17,11 @@
 #ifndef NCG_GJK_THREAD_MIN_BLOCKS
 #define NCG_GJK_THREAD_MIN_BLOCKS 4
 #endif
+// Minimum resident 128-thread blocks per SM of the warp-per-pair GJK kernel
+// (1: no register cap).
+#ifndef NCG_GJK_WARP_MIN_BLOCKS
+#define NCG_GJK_WARP_MIN_BLOCKS 1
+#endif
 
 namespace ncg {
 namespace {
@@ -229,7 +234,7 @@ NCG_DEV void plan_stage(const ncg_batch& b, uint32_t i, uint32_t stage_min, uint
 // shared memory instead of L1/L2.  Every wait is bounded; a timeout sets
 // ctr->stage_err and the kernel reads global memory from then on.
 template <bool STAGE>
-__global__ void __launch_bounds__(128) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int warp_buckets,
+__global__ void __launch_bounds__(128, NCG_GJK_WARP_MIN_BLOCKS) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int warp_buckets,
                                                   uint32_t stage_min, uint32_t stage_cap) {
     extern __shared__ __align__(128) float4 stage[];  // [4 warps][stage_cap]
     __shared__ __align__(8) uint64_t bar[4];

@@ -738,6 +738,7 @@ int ncg_get_stats(ncg_ctx* c, ncg_stats* out) {
     out->n_epa_overflow = c->host_ctr->epa_count[Q_WARP_LONG] + c->host_ctr->epa_count[Q_WARP];
     out->gjk_iters = c->host_ctr->gjk_iters;
     out->epa_iters = c->host_ctr->epa_iters;
+    out->n_epa_thread = c->host_ctr->epa_count[0];
     out->kernels_launched = c->launches;
     out->flags = (c->host_ctr->mlp_err & 1u) | ((c->host_ctr->stage_err & 1u) << 1);
     return NCG_OK;

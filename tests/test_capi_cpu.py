@@ -38,7 +38,7 @@ def test_struct_layouts_match_header():
     assert S.SHAPE_DTYPE.itemsize == 32
     assert S.CONTACT_DTYPE.itemsize == 40
     assert ctypes.sizeof(N.NcgBatch) == 80
-    assert ctypes.sizeof(N.NcgStats) == 48
+    assert ctypes.sizeof(N.NcgStats) == 56
     from oracle import oracle as O
     assert O.MANIFOLD_DTYPE.itemsize == 16 + 36 * N.MANIFOLD_MAX  # ncg_manifold
 
