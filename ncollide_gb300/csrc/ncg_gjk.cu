@@ -184,9 +184,9 @@ NCG_DEV unsigned long long hull_warp_count(const Scratch& s, int warp_buckets) {
 
 // One thread per pair over a pair list (list 0: analytic pairs, list 1:
 // ConvexHull pairs after the warp kernel's, whose points the thread scans
-// itself); EPA starts in the thread stage.
+// itself); EPA starts in the thread stage, queue `epa_queue`.
 __global__ void __launch_bounds__(128, NCG_GJK_THREAD_MIN_BLOCKS)
-k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int warp_buckets) {
+k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int warp_buckets, int epa_queue) {
     const unsigned long long na = *(volatile unsigned long long*)&s.ctr->n_analytic;
     const unsigned long long nw = list == 0 ? 0ull : hull_warp_count(s, warp_buckets);
     const unsigned long long n = list == 0 ? na : *(volatile unsigned long long*)&s.ctr->n_hull - nw;
@@ -198,7 +198,7 @@ k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int wa
     const unsigned long long rounds = (n + stride - 1) / stride;
     for (unsigned long long r = 0; r < rounds; ++r) {
         unsigned long long k = start + r * stride;
-        if (k < n) gjk_pair(b, qp, o, s, ids[k], scan, true, acc, 0);
+        if (k < n) gjk_pair(b, qp, o, s, ids[k], scan, true, acc, epa_queue);
     }
     warp_add(&s.ctr->gjk_iters, acc);
 }
@@ -300,8 +300,8 @@ void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o
 }
 
 void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                       int list, int warp_buckets, cudaStream_t st) {
-    k_gjk_thread<<<grid, 128, 0, st>>>(b, qp, o, s, list, warp_buckets);
+                       int list, int warp_buckets, int epa_queue, cudaStream_t st) {
+    k_gjk_thread<<<grid, 128, 0, st>>>(b, qp, o, s, list, warp_buckets, epa_queue);
 }
 
 void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,

@@ -258,8 +258,8 @@ NCG_DEV void epa_thread_finish(const ncg_batch& b, const QueryParams& qp, const 
 }
 
 NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                             EpaStore& st) {
-    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[0];
+                             EpaStore& st, int q) {
+    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[q];
     ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     unsigned long long acc = 0;
     EpaState S;
@@ -269,9 +269,9 @@ NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Ou
     for (;;) {
         // take items until one needs expansion steps (or the queue is empty)
         while (!active) {
-            const unsigned long long k = atomicAdd(&s.ctr->epa_next[0], 1ull);
+            const unsigned long long k = atomicAdd(&s.ctr->epa_next[q], 1ull);
             if (k >= n) break;
-            item = s.queue[0][k];
+            item = s.queue[q][k];
             const EpaItem& it = s.items[item];
             g = item_geom(b, it);
             CSO sv[4];
@@ -299,11 +299,12 @@ template <int T> TierCaps caps(int q_in, int q_in2, int q_out, int slab) {
 // stores write through to L2).  A pair that outgrows it goes to warp tier A.
 constexpr size_t THREAD_STORE_BYTES =
     EpaStore::bytes(EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
-__global__ void __launch_bounds__(128, NCG_EPA_THREAD_MIN_BLOCKS) k_epa_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
+__global__ void __launch_bounds__(128, NCG_EPA_THREAD_MIN_BLOCKS)
+k_epa_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int q) {
     __align__(16) char buf[THREAD_STORE_BYTES];
     EpaStore st;
     st.carve(buf, EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
-    epa_thread_loop(b, qp, o, s, st);
+    epa_thread_loop(b, qp, o, s, st, q);
 }
 
 
@@ -352,6 +353,9 @@ Tol make_tol(int mode) {
 
 }  // namespace
 
+// Stage-timing events of one call: a start mark and one per launch group.
+constexpr int NCG_N_MARKS = NCG_N_STAGES + 2;
+
 struct ncg_ctx {
     int device = 0;
     int num_sms = 0;
@@ -378,6 +382,8 @@ struct ncg_ctx {
     char* stage = nullptr;
     size_t stage_cap = 0;
     cudaStream_t own_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // host entry points: the hull-point copy
+    cudaEvent_t hull_ready = nullptr;    // recorded on copy_stream after that copy
     int profiling = 0;
     std::vector<ncg_graph*> graphs;  // destroyed with the context
     float* mlp_params = nullptr;     // NCG_MLP_N_PARAMS floats (device)
@@ -388,8 +394,8 @@ struct ncg_ctx {
     size_t idir_cap = 0;
     uint32_t graph_launches = 0;     // kernels in a captured query
     int n_marks = 0;
-    int mark_stage[NCG_N_STAGES + 1];
-    cudaEvent_t marks[NCG_N_STAGES + 1] = {};
+    int mark_stage[NCG_N_MARKS];
+    cudaEvent_t marks[NCG_N_MARKS] = {};
 };
 
 namespace {
@@ -490,7 +496,14 @@ bool set_carveout(int pct) {
     return ok;
 }
 
-int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outputs& o, cudaStream_t st) {
+// Runs one batched query on stream st.  When `hull_ready` is given (the host
+// entry points), the hull points are still being copied on another stream:
+// the analytic pairs' GJK and, for contact, their thread-stage EPA (queue 0)
+// need none of them and overlap the copy; the stream waits for the event
+// before the first kernel that reads hull points, and the ConvexHull pairs'
+// thread-stage EPA runs after their GJK (queue 4).
+int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outputs& o, cudaStream_t st,
+              cudaEvent_t hull_ready = nullptr) {
     if (!c || !b) { g_last_error = "null context or batch"; return NCG_EINVAL; }
     if (b->n_pairs == 0) return NCG_OK;
     if (b->n_pairs > 0xffffffffull) { g_last_error = "more than 2^32-1 pairs"; return NCG_EINVAL; }
@@ -520,7 +533,9 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset counters")) return NCG_ECUDA;
     if (c->warm == NCG_WARM_MLP && (query == Q_CONTACT || query == Q_PROXIMITY)) {
         // the network's start direction replaces the default one (contact and
-        // proximity start from normalize(t2 - t1) in the reference)
+        // proximity start from normalize(t2 - t1) in the reference); the
+        // shape descriptors read hull points
+        if (hull_ready && !cuda_ok(cudaStreamWaitEvent(st, hull_ready, 0), "cudaStreamWaitEvent")) return NCG_ECUDA;
         int rc = ensure_mlp_buffers(c, b);
         if (rc != NCG_OK) return rc;
         rc = mlp_shape_desc(bb, c->desc_buf, st);
@@ -534,8 +549,21 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     gjk_launch_sort(bb, qp, o, s, st);
     mark(0);
     const int gjk_grid = c->num_sms * (c->gjk_blocks > 0 ? c->gjk_blocks : c->occ_thread);
-    gjk_launch_thread(gjk_grid, bb, qp, o, s, 0, 0, st);
+    const int epa_grid = c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread);
+    gjk_launch_thread(gjk_grid, bb, qp, o, s, 0, 0, 0, st);
     mark(1);
+    launches += 3;
+    // With the hull points still in flight, the analytic pairs' thread-stage
+    // EPA runs first (it reads no hull points); otherwise one thread-stage
+    // launch serves both lists (a second launch adds a tail of ~1 ms).
+    const bool split = query == Q_CONTACT && hull_ready != nullptr;
+    const int hull_queue = split ? Q_THREAD_HULL : 0;
+    if (split) {
+        k_epa_thread<<<epa_grid, 128, 0, st>>>(bb, qp, o, s, 0);
+        mark(3);
+        launches += 1;
+    }
+    if (hull_ready && !cuda_ok(cudaStreamWaitEvent(st, hull_ready, 0), "cudaStreamWaitEvent")) return NCG_ECUDA;
     // hull pairs of the first warp_buckets buckets (largest hulls) one warp per pair
     const int warp_buckets = c->hull_gjk_warp == 0   ? 0
                              : c->hull_gjk_warp == 1 ? NB_HULL
@@ -545,12 +573,11 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
         gjk_launch_warp(c->num_sms * (staged ? c->occ_hstage : c->occ_warp), bb, qp, o, s, warp_buckets,
                         staged ? (uint32_t)c->hstage_min : 0u, (uint32_t)c->hstage_cap, st);
     }
-    if (warp_buckets < NB_HULL) gjk_launch_thread(gjk_grid, bb, qp, o, s, 1, warp_buckets, st);
+    if (warp_buckets < NB_HULL) gjk_launch_thread(gjk_grid, bb, qp, o, s, 1, warp_buckets, hull_queue, st);
     mark(2);
-    launches += 3 + (warp_buckets > 0 ? 1 : 0) + (warp_buckets < NB_HULL ? 1 : 0);
+    launches += (warp_buckets > 0 ? 1 : 0) + (warp_buckets < NB_HULL ? 1 : 0);
     if (query == Q_CONTACT) {
-        k_epa_thread<<<c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread), 128, 0, st>>>(
-            bb, qp, o, s);
+        k_epa_thread<<<epa_grid, 128, 0, st>>>(bb, qp, o, s, hull_queue);
         mark(3);
         // warp stage: the thread stage's overflow, pairs of curved shapes first
         k_epa<<<c->n_slabs[0], 32, 0, st>>>(bb, qp, o, s, caps<2>(Q_WARP_LONG, Q_WARP, 3, 0));
@@ -622,7 +649,9 @@ int ncg_ctx_destroy(ncg_ctx* c) {
     if (c->stage) cudaFree(c->stage);
     if (c->host_ctr) cudaFreeHost(c->host_ctr);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
-    for (int i = 0; i <= NCG_N_STAGES; ++i)
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->hull_ready) cudaEventDestroy(c->hull_ready);
+    for (int i = 0; i < NCG_N_MARKS; ++i)
         if (c->marks[i]) cudaEventDestroy(c->marks[i]);
     delete c;
     return NCG_OK;
@@ -692,7 +721,7 @@ int ncg_ctx_set_dispatch(ncg_ctx* c, int dispatch) {
 int ncg_ctx_set_profiling(ncg_ctx* c, int enabled) {
     if (!c) return NCG_EINVAL;
     if (enabled && !c->marks[0]) {
-        for (int i = 0; i <= NCG_N_STAGES; ++i)
+        for (int i = 0; i < NCG_N_MARKS; ++i)
             if (!cuda_ok(cudaEventCreate(&c->marks[i]), "cudaEventCreate")) return NCG_ECUDA;
     }
     c->profiling = enabled ? 1 : 0;
@@ -710,7 +739,7 @@ int ncg_get_stage_ms(ncg_ctx* c, float* ms, int n_max) {
         float t = 0.0f;
         cudaEventElapsedTime(&t, c->marks[i - 1], c->marks[i]);
         if (stage >= 0 && stage < n_max) {
-            ms[stage] = t;
+            ms[stage] += t;
             if (stage + 1 > wrote) wrote = stage + 1;
         }
     }
@@ -738,7 +767,7 @@ int ncg_get_stats(ncg_ctx* c, ncg_stats* out) {
     out->n_epa_overflow = c->host_ctr->epa_count[Q_WARP_LONG] + c->host_ctr->epa_count[Q_WARP];
     out->gjk_iters = c->host_ctr->gjk_iters;
     out->epa_iters = c->host_ctr->epa_iters;
-    out->n_epa_thread = c->host_ctr->epa_count[0];
+    out->n_epa_thread = c->host_ctr->epa_count[0] + c->host_ctr->epa_count[Q_THREAD_HULL];
     out->kernels_launched = c->launches;
     out->flags = (c->host_ctr->mlp_err & 1u) | ((c->host_ctr->stage_err & 1u) << 1);
     return NCG_OK;
@@ -1041,26 +1070,50 @@ int stage_batch(ncg_ctx* c, const ncg_batch* h, size_t out_bytes, cudaStream_t s
     }
     char* p = c->stage;
     ncg_batch d = *h;
-    auto put = [&](const void* src, size_t bytes) -> char* {
+    auto put = [&](const void* src, size_t bytes, cudaStream_t s) -> char* {
         char* dst = p;
-        if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+        if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
         p += al(bytes);
         return dst;
     };
-    d.shapes = (const ncg_shape*)put(h->shapes, sizeof(ncg_shape) * h->n_shapes);
-    d.hull_points = (const float*)put(h->hull_points, 16 * h->n_hull_points);
-    d.m1 = (const ncg_pose*)put(h->m1, sizeof(ncg_pose) * n);
-    d.m2 = (const ncg_pose*)put(h->m2, sizeof(ncg_pose) * n);
-    d.g1 = (const uint32_t*)put(h->g1, 4 * n);
-    d.g2 = (const uint32_t*)put(h->g2, 4 * n);
-    d.init_dir = h->init_dir ? (const float*)put(h->init_dir, 12 * n) : nullptr;
+    // The small arrays first, on st; then the hull points (most of the bytes)
+    // on the copy stream once those are done (copies in one direction share
+    // the copy engines in issue order, so the query's first kernels would
+    // otherwise wait behind the hull points).  The query waits for hull_ready
+    // before its first kernel that reads hull points.
+    char* hull_dst = p;
+    p += al(16 * h->n_hull_points);
+    d.shapes = (const ncg_shape*)put(h->shapes, sizeof(ncg_shape) * h->n_shapes, st);
+    d.m1 = (const ncg_pose*)put(h->m1, sizeof(ncg_pose) * n, st);
+    d.m2 = (const ncg_pose*)put(h->m2, sizeof(ncg_pose) * n, st);
+    d.g1 = (const uint32_t*)put(h->g1, 4 * n, st);
+    d.g2 = (const uint32_t*)put(h->g2, 4 * n, st);
+    d.init_dir = h->init_dir ? (const float*)put(h->init_dir, 12 * n, st) : nullptr;
+    if (!cuda_ok(cudaEventRecord(c->hull_ready, st), "cudaEventRecord") ||
+        !cuda_ok(cudaStreamWaitEvent(c->copy_stream, c->hull_ready, 0), "cudaStreamWaitEvent"))
+        return NCG_ECUDA;
+    if (h->n_hull_points)
+        cudaMemcpyAsync(hull_dst, h->hull_points, 16 * h->n_hull_points, cudaMemcpyHostToDevice, c->copy_stream);
+    d.hull_points = (const float*)hull_dst;
+    if (!cuda_ok(cudaEventRecord(c->hull_ready, c->copy_stream), "cudaEventRecord")) return NCG_ECUDA;
     hr.dev = d;
     hr.out = p;
     return cuda_ok(cudaGetLastError(), "stage copies") ? NCG_OK : NCG_ECUDA;
 }
 
+// Ends a host entry point: the stream also waits for the hull-point copy (so
+// that no copy from the caller's buffers is in flight when the call returns,
+// whatever the query read), then the host waits for the stream.
+int host_finish(ncg_ctx* c, cudaStream_t st, int rc, const char* what) {
+    cudaStreamWaitEvent(st, c->hull_ready, 0);
+    const bool ok = cuda_ok(cudaStreamSynchronize(st), what);
+    return rc != NCG_OK ? rc : (ok ? NCG_OK : NCG_ECUDA);
+}
+
 cudaStream_t host_stream(ncg_ctx* c) {
     if (!c->own_stream) cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (!c->copy_stream) cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    if (!c->hull_ready) cudaEventCreateWithFlags(&c->hull_ready, cudaEventDisableTiming);
     return c->own_stream;
 }
 
@@ -1071,62 +1124,68 @@ extern "C" {
 int ncg_contact_batch_host(ncg_ctx* c, const ncg_batch* b, float prediction, ncg_contact* out, uint8_t* has_contact,
                            float* out_dir, uint32_t* status) {
     if (!c || !b || !out || !has_contact || !status) return NCG_EINVAL;
+    if (b->n_pairs == 0) return NCG_OK;
     cudaSetDevice(c->device);
     cudaStream_t st = host_stream(c);
     const uint64_t n = b->n_pairs;
     size_t ob = al(40 * n) + al(n) + al(12 * n) + al(4 * n);
     HostRun hr;
     int rc = stage_batch(c, b, ob, st, hr);
-    if (rc) return rc;
+    if (rc) return host_finish(c, st, rc, "contact_batch_host");
     ncg_contact* dc = (ncg_contact*)hr.out;
     uint8_t* dt = (uint8_t*)(hr.out + al(40 * n));
     float* dd = (float*)(hr.out + al(40 * n) + al(n));
     uint32_t* ds = (uint32_t*)(hr.out + al(40 * n) + al(n) + al(12 * n));
-    rc = ncg_contact_batch(c, &hr.dev, prediction, dc, dt, out_dir ? dd : nullptr, ds, nullptr, st);
-    if (rc) return rc;
+    Outputs o{dc, dt, out_dir ? dd : nullptr, nullptr, nullptr, ds, nullptr};
+    rc = run_query(c, &hr.dev, Q_CONTACT, prediction, o, st, c->hull_ready);
+    if (rc) return host_finish(c, st, rc, "contact_batch_host");
     cudaMemcpyAsync(out, dc, 40 * n, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(has_contact, dt, n, cudaMemcpyDeviceToHost, st);
     if (out_dir) cudaMemcpyAsync(out_dir, dd, 12 * n, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(status, ds, 4 * n, cudaMemcpyDeviceToHost, st);
-    return cuda_ok(cudaStreamSynchronize(st), "contact_batch_host") ? NCG_OK : NCG_ECUDA;
+    return host_finish(c, st, NCG_OK, "contact_batch_host");
 }
 
 int ncg_distance_batch_host(ncg_ctx* c, const ncg_batch* b, float* out_dist, uint32_t* status) {
     if (!c || !b || !out_dist || !status) return NCG_EINVAL;
+    if (b->n_pairs == 0) return NCG_OK;
     cudaSetDevice(c->device);
     cudaStream_t st = host_stream(c);
     const uint64_t n = b->n_pairs;
     HostRun hr;
     int rc = stage_batch(c, b, al(4 * n) + al(4 * n), st, hr);
-    if (rc) return rc;
+    if (rc) return host_finish(c, st, rc, "distance_batch_host");
     float* dd = (float*)hr.out;
     uint32_t* ds = (uint32_t*)(hr.out + al(4 * n));
-    rc = ncg_distance_batch(c, &hr.dev, dd, ds, nullptr, st);
-    if (rc) return rc;
+    Outputs o{nullptr, nullptr, nullptr, dd, nullptr, ds, nullptr};
+    rc = run_query(c, &hr.dev, Q_DISTANCE, 0.0f, o, st, c->hull_ready);
+    if (rc) return host_finish(c, st, rc, "distance_batch_host");
     cudaMemcpyAsync(out_dist, dd, 4 * n, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(status, ds, 4 * n, cudaMemcpyDeviceToHost, st);
-    return cuda_ok(cudaStreamSynchronize(st), "distance_batch_host") ? NCG_OK : NCG_ECUDA;
+    return host_finish(c, st, NCG_OK, "distance_batch_host");
 }
 
 int ncg_proximity_batch_host(ncg_ctx* c, const ncg_batch* b, float margin, uint8_t* out_prox, float* out_sep_axis,
                              uint32_t* status) {
     if (!c || !b || !out_prox || !status) return NCG_EINVAL;
     if (!(margin >= 0.0f)) { g_last_error = "The proximity margin must be positive or zero."; return NCG_EINVAL; }
+    if (b->n_pairs == 0) return NCG_OK;
     cudaSetDevice(c->device);
     cudaStream_t st = host_stream(c);
     const uint64_t n = b->n_pairs;
     HostRun hr;
     int rc = stage_batch(c, b, al(n) + al(12 * n) + al(4 * n), st, hr);
-    if (rc) return rc;
+    if (rc) return host_finish(c, st, rc, "proximity_batch_host");
     uint8_t* dt = (uint8_t*)hr.out;
     float* dd = (float*)(hr.out + al(n));
     uint32_t* ds = (uint32_t*)(hr.out + al(n) + al(12 * n));
-    rc = ncg_proximity_batch(c, &hr.dev, margin, dt, out_sep_axis ? dd : nullptr, ds, nullptr, st);
-    if (rc) return rc;
+    Outputs o{nullptr, dt, out_sep_axis ? dd : nullptr, nullptr, nullptr, ds, nullptr};
+    rc = run_query(c, &hr.dev, Q_PROXIMITY, margin, o, st, c->hull_ready);
+    if (rc) return host_finish(c, st, rc, "proximity_batch_host");
     cudaMemcpyAsync(out_prox, dt, n, cudaMemcpyDeviceToHost, st);
     if (out_sep_axis) cudaMemcpyAsync(out_sep_axis, dd, 12 * n, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(status, ds, 4 * n, cudaMemcpyDeviceToHost, st);
-    return cuda_ok(cudaStreamSynchronize(st), "proximity_batch_host") ? NCG_OK : NCG_ECUDA;
+    return host_finish(c, st, NCG_OK, "proximity_batch_host");
 }
 
 }  // extern "C"
@@ -1238,9 +1297,9 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     // The array keeps the previous call's contents: reset the counters and queues' heads.
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset noalloc counters")) return NCG_ECUDA;
     gjk_launch_sort(bb, qp, o, s, st);
-    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 0, 0, st);
-    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 1, 0, st);
-    k_epa_thread<<<d.num_sms * d.lim.occ_ethread, 128, 0, st>>>(bb, qp, o, s);
+    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 0, 0, 0, st);
+    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 1, 0, 0, st);
+    k_epa_thread<<<d.num_sms * d.lim.occ_ethread, 128, 0, st>>>(bb, qp, o, s, 0);
     // warp stages in shared memory (128, then 1280 vertices), then the one global slab
     k_epa<<<d.num_sms * d.lim.occ_smem[0], 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>(Q_WARP_LONG, Q_WARP, 3, -1));
     k_epa<<<d.num_sms * d.lim.occ_smem[1], 32, tier_bytes<2>(), st>>>(bb, qp, o, s, caps<2>(3, -1, 4, -1));

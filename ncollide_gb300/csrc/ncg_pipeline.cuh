@@ -52,9 +52,11 @@ struct __align__(16) EpaItem {
 
 // EPA queues: 0 the thread stage; 1 and 2 the first warp stage (1: pairs of two
 // curved shapes, whose polytopes grow longest, drained first; 2: the rest);
-// 3 and 4 the later warp stages.
+// 3 the later warp stage; 4 the thread stage's ConvexHull pairs (a query
+// runs the thread stage over queue 0 before the ConvexHull GJK, then over
+// queue 4) or, in the no-allocation path, the last warp stage.
 constexpr int N_EPA_QUEUES = 5;
-constexpr int Q_WARP_LONG = 1, Q_WARP = 2;
+constexpr int Q_WARP_LONG = 1, Q_WARP = 2, Q_THREAD_HULL = 4;
 
 struct DevCounters {
     unsigned long long n_analytic, n_hull;
@@ -187,9 +189,10 @@ NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
 // rest into s.sorted (k_classify, k_bucket): two launches over n pairs.
 void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, cudaStream_t st);
 // One thread per pair over list 0 (analytic pairs) or 1 (the ConvexHull
-// pairs after the first `warp_buckets` hull buckets).
+// pairs after the first `warp_buckets` hull buckets); EPA work items go to
+// thread-stage queue `epa_queue`.
 void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                       int list, int warp_buckets, cudaStream_t st);
+                       int list, int warp_buckets, int epa_queue, cudaStream_t st);
 // One warp per pair over the ConvexHull pairs of the first `warp_buckets`
 // hull buckets (the largest hulls); with stage_min > 0, pairs whose hulls hold
 // at least stage_min points are staged in shared memory (stage_cap points
