@@ -325,3 +325,39 @@ def test_hull_stage_tuning_rejects_bad_values(ctx_factory):
                    (N.TUNE_HULL_STAGE_MIN, -1), (N.TUNE_HULL_STAGE_MIN, 4096)):
         with pytest.raises(Exception):
             ctx.set_tuning(key, v)
+
+
+@pytest.mark.parametrize("tol", TOLS)
+def test_resumed_long_polytopes_bit_exact(ctx_factory, tol):
+    """Deep, nearly concentric curved pairs (Ball, Capsule, Cone centres within
+    5% of the summed radii): EPA refines a ring of equidistant faces for
+    hundreds of steps, so most pairs outgrow the thread stage's store and the
+    warp stage resumes them from the spilled polytope.  Bit-exact against the
+    oracle, which never splits a run."""
+    ctx = ctx_factory(tolerance=tol, dispatch="query")
+    b = W.mixed_convex(2048, seed=71, kinds=(S.BALL, S.CAPSULE, S.CONE), dmax=0.05)
+    g, r = check_query(ctx, b, O.CONTACT_QUERY, 0.0, tol)
+    st = ctx.stats()
+    assert st["n_epa_overflow"] > 100
+    assert int(np.max(g["iters"].view(np.uint32) >> 16)) > 200  # long runs, resumed past the thread store
+
+
+def test_host_entry_points_overlap_copies_correctly(ctx_factory):
+    """The host entry points copy the hull points on a second stream while the
+    analytic pairs run.  Two different hull-heavy batches in a row (the second
+    one's hull points differ at the same offsets) must give exactly the
+    device-resident results, for contact, distance and proximity."""
+    ctx = ctx_factory(tolerance=N.TOL_PRECISE, dispatch="query")
+    kinds = (S.CUBOID, S.CONVEX_HULL, S.BALL, S.CAPSULE)
+    for seed in (81, 82):
+        b = W.mixed_convex(4096, seed=seed, kinds=kinds)
+        h = Q.contact_batch_host(ctx, b, 0.0)
+        g = run_gpu(ctx, b, O.CONTACT_QUERY, 0.0)
+        assert np.array_equal(h["has_contact"], g["has_contact"])
+        c = h["contact"]
+        flat = np.concatenate([c["world1"], c["world2"], c["normal"], c["depth"][:, None]], 1)
+        assert np.array_equal(flat[h["has_contact"] == 1], g["contact"][g["has_contact"] == 1])
+        assert np.array_equal(h["status"].view(np.uint32), g["status"].view(np.uint32))
+        assert np.array_equal(Q.distance_batch_host(ctx, b)["distance"], run_gpu(ctx, b, O.DISTANCE, 0.0)["distance"])
+        assert np.array_equal(Q.proximity_batch_host(ctx, b, 0.1)["proximity"],
+                              run_gpu(ctx, b, O.PROXIMITY, 0.1)["proximity"])
