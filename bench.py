@@ -812,8 +812,8 @@ def main():
     ap.add_argument("--accuracy-sample", type=int, default=32768)
     ap.add_argument("--pairs", type=int, default=N_PAIRS,
                     help="workload size (profiling runs only: the reported config is 1048576 pairs)")
-    ap.add_argument("--coherent-pairs", type=int, default=1 << 21,
-                    help="pairs of the coherent warm-start workload (16777216 for the full configuration)")
+    ap.add_argument("--coherent-pairs", type=int, default=1 << 24,
+                    help="pairs of the coherent warm-start workload (the configuration's 16777216 by default)")
     ap.add_argument("--no-coherent", action="store_true")
     ap.add_argument("--mlp-pairs", type=int, default=1 << 22)
     ap.add_argument("--mlp-epochs", type=int, default=20)
@@ -836,7 +836,7 @@ def main():
     ap.add_argument("--tuning-file", default=None,
                     help="saved tuning (default: ncollide_gb300/tuning/gb300.json)")
     ap.add_argument("--no-saved-tuning", action="store_true", help="library defaults, not the saved tuning")
-    ap.add_argument("--only", choices=["toi", "ray", "scene", "manifold", "stress", "cuboid"],
+    ap.add_argument("--only", choices=["toi", "ray", "scene", "manifold", "stress", "cuboid", "coherent"],
                     help="run one secondary report alone and print it (not a bench line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -858,7 +858,12 @@ def main():
                   "scene": lambda: scene_pipeline_report(args, local, args.tolerance, args.dispatch),
                   "manifold": lambda: manifold_report(args, local, args.tolerance),
                   "stress": lambda: precision_stress(args, local, args.tolerance),
-                  "cuboid": lambda: cuboid_small(args, local, args.tolerance)}[args.only]()
+                  "cuboid": lambda: cuboid_small(args, local, args.tolerance),
+                  "coherent": lambda: coherent_warm_start(args, local, args.tolerance,
+                                                          float(peaks().get("hbm_gbs", 6800.0)),
+                                                          torch.cuda.get_device_properties(local).multi_processor_count
+                                                          * 128 * 2 * float(peaks().get("sm_max_mhz", 2070.0)) / 1e6)
+                  }[args.only]()
         print(json.dumps({"report": args.only, **report}), flush=True)
         return 0
     dist = None

@@ -269,7 +269,15 @@ NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Ou
     for (;;) {
         // take items until one needs expansion steps (or the queue is empty)
         while (!active) {
-            const unsigned long long k = atomicAdd(&s.ctr->epa_next[q], 1ull);
+            // one atomic per group of lanes taking items together; the group
+            // gets consecutive queue entries (pairs of one kind, adjacent)
+            const unsigned m = __activemask();
+            const int lead = __ffs(m) - 1;
+            const unsigned rank = __popc(m & ((1u << (threadIdx.x & 31u)) - 1u));
+            unsigned long long base = 0;
+            if ((int)(threadIdx.x & 31u) == lead) base = atomicAdd(&s.ctr->epa_next[q], (unsigned long long)__popc(m));
+            base = __shfl_sync(m, base, lead);
+            const unsigned long long k = base + rank;
             if (k >= n) break;
             item = s.queue[q][k];
             const EpaItem& it = s.items[item];
