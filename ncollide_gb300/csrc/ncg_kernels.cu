@@ -224,11 +224,9 @@ __global__ void __launch_bounds__(32, NCG_EPA_WARP_MIN_BLOCKS) k_epa(ncg_batch b
     if (lane == 0 && acc) atomicAdd(&s.ctr->epa_iters, acc);
 }
 // The thread stage's scheduler: each thread takes the next EPA item from the
-// queue as soon as its current one finishes, and the loop advances every
-// thread's pair by one expansion step per pass, so a warp's 32 lanes stay on
-// the same step of the loop body whatever pairs they hold (a pair needs 1 to
-// ~60 steps here); with a fixed item per lane and round, the lanes whose pairs
-// finished early would idle until the round's longest pair was done.
+// queue as soon as its current one finishes (a pair needs 1 to ~60 steps
+// here); with a fixed item per lane and round, the lanes whose pairs finished
+// early would idle until the round's longest pair was done.
 NCG_DEV void epa_thread_finish(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
                                uint32_t item, const EpaResult& r, unsigned long long& acc, const EpaStore& st,
                                const EpaState& S) {
@@ -257,6 +255,28 @@ NCG_DEV void epa_thread_finish(const ncg_batch& b, const QueryParams& qp, const 
     }
 }
 
+// Takes the next thread-stage queue entry: one atomic per group of lanes
+// asking together, which get consecutive entries (pairs of one kind, adjacent).
+NCG_DEV unsigned long long epa_thread_fetch(const Scratch& s, int q) {
+    const unsigned m = __activemask();
+    const int lead = __ffs(m) - 1;
+    const unsigned rank = __popc(m & ((1u << (threadIdx.x & 31u)) - 1u));
+    unsigned long long base = 0;
+    if ((int)(threadIdx.x & 31u) == lead) base = atomicAdd(&s.ctr->epa_next[q], (unsigned long long)__popc(m));
+    base = __shfl_sync(m, base, lead);
+    return base + rank;
+}
+
+// Thread-stage scheduling (compile-time): 0 runs each item to its end, then
+// takes the next (default); 1 advances every thread's pair by one expansion
+// step per pass of one loop, taking a new item as soon as a pair ends (the
+// lanes stay on the same step of the loop body whatever pairs they hold).
+// Both take items dynamically; 1 measured 12% slower on mixed pairs and 11%
+// on short cuboid pairs (a larger loop body around the step).
+#ifndef NCG_EPA_THREAD_SCHED
+#define NCG_EPA_THREAD_SCHED 0
+#endif
+
 NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
                              EpaStore& st, int q) {
     const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[q];
@@ -265,19 +285,25 @@ NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Ou
     EpaState S;
     PairGeom g;
     uint32_t item = 0;
+#if NCG_EPA_THREAD_SCHED == 0
+    for (;;) {
+        const unsigned long long k = epa_thread_fetch(s, q);
+        if (k >= n) break;
+        item = s.queue[q][k];
+        const EpaItem& it = s.items[item];
+        g = item_geom(b, it);
+        CSO sv[4];
+        load_simplex(it, sv);
+        bool done = epa_begin<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, S);
+        while (!done) done = epa_step<ThreadExec>(g, qp.tol, scan, st, S, qp.epa_max_iter);
+        epa_thread_finish(b, qp, o, s, item, S.res, acc, st, S);
+    }
+#else
     bool active = false;
     for (;;) {
         // take items until one needs expansion steps (or the queue is empty)
         while (!active) {
-            // one atomic per group of lanes taking items together; the group
-            // gets consecutive queue entries (pairs of one kind, adjacent)
-            const unsigned m = __activemask();
-            const int lead = __ffs(m) - 1;
-            const unsigned rank = __popc(m & ((1u << (threadIdx.x & 31u)) - 1u));
-            unsigned long long base = 0;
-            if ((int)(threadIdx.x & 31u) == lead) base = atomicAdd(&s.ctr->epa_next[q], (unsigned long long)__popc(m));
-            base = __shfl_sync(m, base, lead);
-            const unsigned long long k = base + rank;
+            const unsigned long long k = epa_thread_fetch(s, q);
             if (k >= n) break;
             item = s.queue[q][k];
             const EpaItem& it = s.items[item];
@@ -295,6 +321,7 @@ NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Ou
             active = false;
         }
     }
+#endif
     warp_add(&s.ctr->epa_iters, acc);
 }
 
