@@ -229,13 +229,17 @@ NCG_DEV void plan_stage(const ncg_batch& b, uint32_t i, uint32_t stage_min, uint
 // buckets, drained from a shared counter.  With STAGE, a pair whose hulls
 // hold at least `stage_min` points first has them copied into its warp's
 // shared-memory stage (`stage_cap` points per warp) by the bulk-copy engine
-// (cp.async.bulk completing on an mbarrier): the first of the pair's support
-// scans then no longer waits on scattered global loads and the later ones read
-// shared memory instead of L1/L2.  Every wait is bounded; a timeout sets
+// (cp.async.bulk completing on an mbarrier), and its scans read shared memory
+// instead of global memory.  On the mixed convex workload the stage costs more
+// than it saves (every pair waits for its whole copy before its first scan,
+// and a GJK run makes only a few scans, which L1 serves; a 2048-point stage
+// also leaves one block per SM instead of two): off by default, a tuning key
+// for the autotuner.  Every wait is bounded; a timeout sets
 // ctr->stage_err and the kernel reads global memory from then on.
 template <bool STAGE>
-__global__ void __launch_bounds__(128, NCG_GJK_WARP_MIN_BLOCKS) k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int warp_buckets,
-                                                  uint32_t stage_min, uint32_t stage_cap) {
+__global__ void __launch_bounds__(128, NCG_GJK_WARP_MIN_BLOCKS)
+k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int warp_buckets, uint32_t stage_min,
+           uint32_t stage_cap) {
     extern __shared__ __align__(128) float4 stage[];  // [4 warps][stage_cap]
     __shared__ __align__(8) uint64_t bar[4];
     const unsigned long long n = hull_warp_count(s, warp_buckets);
