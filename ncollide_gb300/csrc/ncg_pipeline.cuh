@@ -61,6 +61,7 @@ constexpr int Q_WARP_LONG = 1, Q_WARP = 2, Q_THREAD_HULL = 4;
 struct DevCounters {
     unsigned long long n_analytic, n_hull;
     unsigned long long hull_next;
+    unsigned long long gjk_next[2];  // next entry of the thread GJK kernels' lists (dynamic fetch)
     unsigned long long n_items;       // EPA work items written
     unsigned long long epa_count[N_EPA_QUEUES];  // items per queue
     unsigned long long epa_next[N_EPA_QUEUES];
