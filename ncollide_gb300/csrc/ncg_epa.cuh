@@ -333,8 +333,9 @@ struct EpaState {
 // iteration of the expansion loop (epa3.rs:323-428).  Each returns true when
 // EPA has finished, with the result in S.res.  With WarpExec all 32 lanes of a
 // warp call them with identical arguments and every lane gets the same state;
-// with ThreadExec one thread runs them alone, so a thread can interleave
-// several pairs' steps with others' (the thread stage's per-thread scheduler).
+// with ThreadExec one thread runs them alone.  Between two steps the state and
+// the store are all there is, which lets a larger store resume a run
+// (epa_spill, epa_resume) and lets a thread interleave steps of several pairs.
 template <class E, class Scan>
 NCG_DEV bool epa_begin(const PairGeom& g, int dim, const CSO* sv, const Tol& tol, const Scan& scan, EpaStore& st,
                        EpaState& S) {
