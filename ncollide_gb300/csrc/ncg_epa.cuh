@@ -47,11 +47,6 @@
 #ifndef NCG_EPA_HEAP_ARITY
 #define NCG_EPA_HEAP_ARITY 2
 #endif
-// Silhouette flood fill: 1 loads each visited face's record once into
-// registers (and the new support point once); 0 reads the store per use.
-#ifndef NCG_EPA_FLOOD_CACHED
-#define NCG_EPA_FLOOD_CACHED 0
-#endif
 
 namespace ncg {
 
@@ -198,17 +193,6 @@ struct EpaStore {
         if (a == id) return 1;
         if (b == id) return 2;
         return 0;
-    }
-    // seen_by on a face whose normal and three vertex indices are already in
-    // registers, against the point x: the same arithmetic.
-    NCG_DEV bool seen_by_rec(vec3<float> nrm, const int* P, vec3<float> x, int opp, const Tol& tol) const {
-        const int i0 = opp == 0 ? P[0] : (opp == 1 ? P[1] : P[2]);
-        const int i1 = opp == 0 ? P[1] : (opp == 1 ? P[2] : P[0]);
-        const int i2 = opp == 0 ? P[2] : (opp == 1 ? P[0] : P[1]);
-        vec3<float> p0 = vf(i0), p1 = vf(i1), p2 = vf(i2);
-        if (dot(x - p0, nrm) >= -tol.eps_tol_f) return true;
-        float s = norm_sq(cross(p2 - p1, x - p1));
-        return s == 0.0f || fabsf(s) <= tol.affine_eps_f;
     }
     // epa3.rs:143-156 and utils/triangle.rs:85-102 (f32).
     NCG_DEV bool seen_by(int f, int point, int opp, const Tol& tol) const {
@@ -538,44 +522,22 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
                 st.tref[top] = a1; st.topp[top++] = (uint8_t)o1;
                 st.tref[top] = a0; st.topp[top++] = (uint8_t)o0;
             }
-#if NCG_EPA_FLOOD_CACHED
-            // each visited face's two 16-byte halves are loaded once, together,
-            // and the new support point once for the whole fill
-            const vec3<float> xs = st.vf(sup);
-#endif
             while (top > 0 && !ovf) {
                 --top;
                 uint32_t r = st.tref[top];
                 int opp = st.topp[top];
-#if NCG_EPA_FLOOD_CACHED
-                const int id = rslot(r);
-                const float4 fa = st.FA(id);
-                const uint4 fb = st.FB(id);
-                if ((fb.x >> 16) != (r >> 16)) continue;  // deleted face (stale reference)
-                const uint32_t pab = __float_as_uint(fa.w);
-                const int P[3] = {(int)(pab & 0xffffu), (int)(pab >> 16), (int)(fb.x & 0xffffu)};
-                if (!st.seen_by_rec(mk(fa.x, fa.y, fa.z), P, xs, opp, tol)) {
-#else
                 if (!st.live(r)) continue;
                 int id = rslot(r);
                 if (!st.seen_by(id, sup, opp, tol)) {
-#endif
                     if (nsil >= st.SC) { ovf = 1; break; }
                     st.sref[nsil] = r;
                     st.sopp[nsil] = (uint8_t)opp;
                     nsil++;
                 } else {
                     int k1 = (opp + 2) % 3, k2 = opp;
-#if NCG_EPA_FLOOD_CACHED
-                    uint32_t r1 = k1 == 0 ? fb.y : (k1 == 1 ? fb.z : fb.w);
-                    uint32_t r2 = k2 == 0 ? fb.y : (k2 == 1 ? fb.z : fb.w);
-                    int q1 = st.next_ccw(rslot(r1), P[k1]);
-                    int q2 = st.next_ccw(rslot(r2), P[k2]);
-#else
                     uint32_t r1 = st.adj(id, k1), r2 = st.adj(id, k2);
                     int q1 = st.next_ccw(rslot(r1), st.pt(id, k1));
                     int q2 = st.next_ccw(rslot(r2), st.pt(id, k2));
-#endif
                     st.kill(id, nfree);
                     if (top + 2 > st.TC) { ovf = 1; break; }
                     st.tref[top] = r2; st.topp[top++] = (uint8_t)q2;
