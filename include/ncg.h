@@ -32,7 +32,9 @@
 extern "C" {
 #endif
 
-#define NCG_ABI_VERSION 1
+/* 2: ncg_stats gained n_epa_thread (56 bytes); NCG_TUNE_HULL_STAGE_*, ncg_autotune,
+ * ncg_ctx_get_tuning and NCG_EINTERNAL added.  ncg_abi_version() returns it. */
+#define NCG_ABI_VERSION 2
 
 /* ---- shape kinds: the ncollide3d shapes that implement SupportMap ------- */
 enum ncg_shape_kind {

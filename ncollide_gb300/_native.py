@@ -13,6 +13,7 @@ from . import build as _build
 
 LIB_PATH = _build.LIB_PATH
 
+ABI_VERSION = 2  # NCG_ABI_VERSION of include/ncg.h
 NCG_OK, NCG_EINVAL, NCG_ECUDA, NCG_ENOMEM, NCG_ENOTBUILT, NCG_EINTERNAL = 0, -1, -2, -3, -4, -5
 TOL_REFERENCE, TOL_PRECISE = 0, 1
 WARM_NONE, WARM_INIT_DIR, WARM_MLP = 0, 1, 2
@@ -83,6 +84,10 @@ def load(build_if_missing=True):
     if not os.path.exists(LIB_PATH):
         raise NcgError(f"libncg.so is not built ({LIB_PATH}); run ncollide_gb300.build.build()")
     L = ctypes.CDLL(LIB_PATH)
+    L.ncg_abi_version.restype = ctypes.c_int
+    if L.ncg_abi_version() != ABI_VERSION:
+        raise NcgError(f"{LIB_PATH} has C ABI version {L.ncg_abi_version()}, this binding expects {ABI_VERSION}: "
+                       "rebuild it (ncollide_gb300.build.build(force=True))")
     vp, i32, f32, u32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_uint32
     P = ctypes.POINTER
     L.ncg_ctx_create.argtypes = [P(vp), i32]

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared_functions():
         assert hasattr(L, name), name
     assert set(declared_functions()) <= set(N.EXPORTED) | {"ncg_last_error"}
-    assert L.ncg_abi_version() == 1
+    assert L.ncg_abi_version() == 2
 
 
 def test_struct_layouts_match_header():
@@ -73,3 +73,9 @@ def test_ctx_create_reports_missing_gpu():
     rc = L.ncg_ctx_create(ctypes.byref(p), 0)
     assert rc == N.NCG_ECUDA
     assert L.ncg_last_error()
+
+
+def test_binding_abi_version_matches_header():
+    src = open(os.path.join(ROOT, "include", "ncg.h")).read()
+    m = re.search(r"#define NCG_ABI_VERSION (\d+)", src)
+    assert m and int(m.group(1)) == N.ABI_VERSION == N.load().ncg_abi_version()
