@@ -462,8 +462,18 @@ int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
  * call clears what must start at zero), so calls that overlap on the GPU —
  * different streams, or concurrent host threads — race and corrupt each
  * other's results: serialise them.
+ * `stream` must belong to the current device (checked: NCG_EINVAL otherwise).
  * `tolerance` is an ncg_tolerance; batch->init_dir, when not NULL, is the
- * first GJK direction of every pair.  Results equal ncg_contact_batch's.
+ * first GJK direction of every pair.  Every pair runs
+ * contact_support_map_support_map (NCG_DISPATCH_SUPPORT_MAP): results equal
+ * those of ncg_contact_batch on a context with that dispatch (the default),
+ * the same tolerance set and, when init_dir is given, NCG_WARM_INIT_DIR; a
+ * context using NCG_DISPATCH_QUERY routes Ball pairs differently.
+ * EPA runs in three stores: 128 vertices, then 1280 (both in shared memory),
+ * then the array's one 10240-vertex slab, which a single warp drains: pairs
+ * whose polytope outgrows 1280 vertices (deep, nearly concentric curved
+ * pairs) run one after another there, which bounds a call's latency from
+ * below by their summed EPA time.
  * This entry point has no counterpart in the reference. */
 #define NCG_NOALLOC_MAX_PAIRS 32768
 #define NCG_NOALLOC_SCRATCH_BYTES 7827200

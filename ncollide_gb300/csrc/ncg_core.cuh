@@ -128,6 +128,24 @@ struct ThreadScan {
     }
 };
 
+// Butterfly reduction of the lanes' (dot, index) keys, larger dot then smaller
+// index, so that every lane gets the first maximum.  The serial scan starts
+// from point 0's dot and keeps it when that dot is NaN (no comparison with a
+// NaN is true): lane 0 reports that case (nan0) and the result is then 0.
+NCG_DEV uint32_t warp_argmax_finish(float best, uint32_t bi, bool nan0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        bool take = ob > best || (ob == best && oi < bi);
+        if (take) {
+            best = ob;
+            bi = oi;
+        }
+    }
+    return __shfl_sync(0xffffffffu, (int)nan0, 0) ? 0u : bi;
+}
+
 // All 32 lanes of a warp call argmax with the same arguments; lane l scans
 // points l, l+32, ... (one coalesced 128-bit load per lane per step), then a
 // butterfly reduction keeps (larger dot, smaller index) so every lane gets
@@ -141,26 +159,18 @@ struct WarpScan {
         // rank as -inf so that every lane pair agrees (a strict total order).
         float best = -INFINITY;
         uint32_t bi = 0xffffffffu;
+        bool nan0 = false;
         for (uint32_t i = lane; i < s.n; i += 32) {
             float4 v = __ldg(p + i);
             float x = dot(vec3<float>{v.x, v.y, v.z}, d);
+            if (i == 0) nan0 = x != x;
             x = (x != x) ? -INFINITY : x;
             if (bi == 0xffffffffu || x > best) {
                 best = x;
                 bi = i;
             }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            float ob = __shfl_xor_sync(0xffffffffu, best, o);
-            uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            bool take = ob > best || (ob == best && oi < bi);
-            if (take) {
-                best = ob;
-                bi = oi;
-            }
-        }
-        return bi;
+        return warp_argmax_finish(best, bi, nan0);
     }
 };
 
@@ -183,6 +193,7 @@ struct StagedWarpScan {
         const uint32_t base = sbase + 16u * at[k];
         float best = -INFINITY;
         uint32_t bi = 0xffffffffu;
+        bool nan0 = false;
         for (uint32_t i = lane; i < s.n; i += 32) {
             float4 v;
             // volatile: the stage is written by the async proxy; these reads
@@ -191,23 +202,14 @@ struct StagedWarpScan {
                          : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
                          : "r"(base + 16u * i));
             float x = dot(vec3<float>{v.x, v.y, v.z}, d);
+            if (i == 0) nan0 = x != x;
             x = (x != x) ? -INFINITY : x;
             if (bi == 0xffffffffu || x > best) {
                 best = x;
                 bi = i;
             }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            float ob = __shfl_xor_sync(0xffffffffu, best, o);
-            uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            bool take = ob > best || (ob == best && oi < bi);
-            if (take) {
-                best = ob;
-                bi = oi;
-            }
-        }
-        return bi;
+        return warp_argmax_finish(best, bi, nan0);
     }
 };
 

@@ -56,9 +56,12 @@ enum EpaExit : int {
     EPA_OK_NUMERIC = 3,
     EPA_OK_HEAP_EMPTY = 4,
     EPA_NONE = 5,        // EPA returned None
-    EPA_OVERFLOW = 6,    // store capacity exceeded (result not valid)
+    EPA_OVERFLOW = 6,    // no room for the next support point, stopped between two steps (resumable)
     EPA_OK_PRECISION = 7,  // PRECISE set: a failed expansion step answered with the best face
+    EPA_OVERFLOW_MID = 8,  // a silhouette, stack, slot or heap limit hit inside a step: the store is
+                           // left half-updated, so a larger store restarts from GJK's simplex
 };
+NCG_DEV bool epa_overflow(int e) { return e == EPA_OVERFLOW || e == EPA_OVERFLOW_MID; }
 NCG_DEV bool epa_ok(int e) { return (e >= EPA_OK_DIM0 && e <= EPA_OK_HEAP_EMPTY) || e == EPA_OK_PRECISION; }
 
 NCG_DEV uint32_t mkref(int slot, uint32_t gen) { return (uint32_t)slot | (gen << 16); }
@@ -549,7 +552,7 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
         ovf = E::bcast(ovf);
         nfree = E::bcast(nfree);
         E::sync();
-        if (ovf) { res.exit = EPA_OVERFLOW; return true; }
+        if (ovf) { res.exit = EPA_OVERFLOW_MID; return true; }
         if (nsil == 0) {
             if (tol.best_on_failure) {
                 st.face_points(b0, b1, b2, res.p1, res.p2);
@@ -593,7 +596,7 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
         nfree = E::bcast(nfree);
         nfresh = E::bcast(nfresh);
         E::sync();
-        if (ovf) { res.exit = EPA_OVERFLOW; return true; }
+        if (ovf) { res.exit = EPA_OVERFLOW_MID; return true; }
         if (built == 0) {  // epa3.rs:409-413
             if (tol.best_on_failure) {
                 st.face_points(b0, b1, b2, res.p1, res.p2);
@@ -656,7 +659,7 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
             res.status |= NCG_STATUS_EPA_FAILED;
             return true;
         }
-        if (outcome == 3) { res.exit = EPA_OVERFLOW; return true; }
+        if (outcome == 3) { res.exit = EPA_OVERFLOW_MID; return true; }
         niter += 1;
         if (niter > max_iter) {
             res.status |= NCG_STATUS_EPA_MAX_ITER;

@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(32, NCG_EPA_WARP_MIN_BLOCKS) k_epa(ncg_batch b
         }
         while (!done) done = epa_step<WarpExec>(g, qp.tol, scan, st, S, qp.epa_max_iter);
         const EpaResult& r = S.res;
-        if (r.exit == EPA_OVERFLOW && tc.q_out >= 0) {
+        if (epa_overflow(r.exit) && tc.q_out >= 0) {
             if (lane == 0) {
                 unsigned long long pos = atomicAdd(&s.ctr->epa_count[tc.q_out], 1ull);
                 s.queue[tc.q_out][pos] = item;
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(32, NCG_EPA_WARP_MIN_BLOCKS) k_epa(ncg_batch b
         } else {
             acc += r.iters;
             if (lane == 0) {
-                if (r.exit == EPA_OVERFLOW) {
+                if (epa_overflow(r.exit)) {
                     EpaResult none = r;
                     none.exit = EPA_NONE;
                     finish_epa(b, qp, o, it, none, NCG_STATUS_EPA_CAPACITY);
@@ -231,10 +231,11 @@ NCG_DEV void epa_thread_finish(const ncg_batch& b, const QueryParams& qp, const 
                                uint32_t item, const EpaResult& r, unsigned long long& acc, const EpaStore& st,
                                const EpaState& S) {
     EpaItem& it = s.items[item];
-    if (r.exit == EPA_OVERFLOW) {
-        // keep the polytope (when a spill record is free) so that the warp
-        // stage resumes it instead of repeating these iterations
-        if (s.spill) {
+    if (epa_overflow(r.exit)) {
+        // keep the polytope (when a spill record is free and the store
+        // stopped between two steps) so that the warp stage resumes it
+        // instead of repeating these iterations
+        if (s.spill && r.exit == EPA_OVERFLOW) {
             const unsigned long long rec = atomicAdd(&s.ctr->spill_next, 1ull);
             if (rec < s.spill_cap) {
                 epa_spill<ThreadExec>(st, S, s.spill + (size_t)rec * s.spill_bytes);
@@ -1295,11 +1296,18 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return NCG_ECUDA;
     if (dev < 0 || dev >= NA_MAX_DEVICES) { g_last_error = "device index out of range"; return NCG_EINVAL; }
+    cudaStream_t st = (cudaStream_t)stream;
+    int sdev = -1;
+    if (!cuda_ok(cudaStreamGetDevice(st, &sdev), "cudaStreamGetDevice")) return NCG_EINVAL;
+    if (sdev != dev) {
+        g_last_error = "ncg_contact_batch_noalloc: the stream belongs to device " + std::to_string(sdev) +
+                       ", not to the current device " + std::to_string(dev);
+        return NCG_EINVAL;
+    }
     NoallocDevice d;
     int rc = noalloc_setup(dev, d);
     if (rc) return rc;
 
-    cudaStream_t st = (cudaStream_t)stream;
     Scratch s;
     char* p = d.base;
     s.ctr = (DevCounters*)p; p += CTR_SLOT;

@@ -361,3 +361,34 @@ def test_host_entry_points_overlap_copies_correctly(ctx_factory):
         assert np.array_equal(Q.distance_batch_host(ctx, b)["distance"], run_gpu(ctx, b, O.DISTANCE, 0.0)["distance"])
         assert np.array_equal(Q.proximity_batch_host(ctx, b, 0.1)["proximity"],
                               run_gpu(ctx, b, O.PROXIMITY, 0.1)["proximity"])
+
+
+@pytest.mark.parametrize("hull_warp", [0, 1])
+def test_hull_with_nan_first_point_matches_serial_argmax(ctx_factory, hull_warp):
+    """point_cloud_support_point starts from point 0's dot product and only
+    replaces it by a larger one, so a NaN at point 0 makes it return 0 for
+    every direction (no comparison with NaN is true).  The warp-parallel
+    arg-max must do the same (its reduction ranks NaN below every number)."""
+    rng = np.random.default_rng(91)
+    pairs = []
+    for k in range(96):
+        n = int(rng.integers(40, 600))
+        pts = rng.normal(size=(n, 3)).astype(np.float32) * 0.5
+        if k % 3 == 0:
+            pts[0] = np.nan
+        elif k % 3 == 1:
+            pts[0] = (np.inf, -np.inf, 0.0)   # NaN dot products for half of the directions
+        q = W.random_unit_quaternions(rng, 2)
+        t = rng.uniform(-0.8, 0.8, 3)
+        other = S.ConvexHull(rng.normal(size=(64, 3)).astype(np.float32) * 0.4) if k % 2 else S.Cuboid((0.3, 0.2, 0.4))
+        pairs.append((S.isometry((0, 0, 0), q[0]), S.ConvexHull(pts), S.isometry(t, q[1]), other))
+    b = S.pack_pairs(pairs)
+    ctx = ctx_factory(tolerance=N.TOL_REFERENCE)
+    ctx.set_tuning(N.TUNE_HULL_GJK_WARP, hull_warp)
+    try:
+        # GJK-only queries: with a NaN or infinite support point the contact
+        # query's EPA runs to its 10 000-iteration cap on every such pair
+        for q, p in ((O.DISTANCE, 0.0), (O.PROXIMITY, 0.1), (O.CLOSEST, 1.0)):
+            check_query(ctx, b, q, p, N.TOL_REFERENCE)
+    finally:
+        ctx.set_tuning(N.TUNE_HULL_GJK_WARP, 0)
