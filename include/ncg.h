@@ -33,8 +33,10 @@ extern "C" {
 #endif
 
 /* 2: ncg_stats gained n_epa_thread (56 bytes); NCG_TUNE_HULL_STAGE_*, ncg_autotune,
- * ncg_ctx_get_tuning and NCG_EINTERNAL added.  ncg_abi_version() returns it. */
-#define NCG_ABI_VERSION 2
+ * ncg_ctx_get_tuning and NCG_EINTERNAL added.
+ * 3: ncg_ctx_set_arithmetic (NCG_ARITH_SPLIT, NCG_ARITH_F32) added.
+ * ncg_abi_version() returns it. */
+#define NCG_ABI_VERSION 3
 
 /* ---- shape kinds: the ncollide3d shapes that implement SupportMap ------- */
 enum ncg_shape_kind {
@@ -167,6 +169,19 @@ enum ncg_toi_status {
  * that results land within 1e-5 relative of the f64 reference. */
 enum ncg_tolerance { NCG_TOL_REFERENCE = 0, NCG_TOL_PRECISE = 1 };
 
+/* Arithmetic of GJK, EPA and the query wrappers (contact, distance,
+ * proximity, closest points, the manifold's contact query).
+ * NCG_ARITH_SPLIT (default): support mapping, CSO points and EPA's expansion
+ *   in f32; the Voronoi-simplex sub-solve, GJK's bounds and EPA's face
+ *   normals, distances and termination in double-word arithmetic (~48-bit
+ *   significand on the FP32 pipes); EPA's queue pops equal distances first
+ *   in, first out.
+ * NCG_ARITH_F32: the reference's f32 path as the reference computes it
+ *   (N = f32 throughout: the f32 sub-solve and constants, and Rust
+ *   BinaryHeap's order among equal EPA distances), for callers that need its
+ *   results bit for bit rather than the split's FP64-class accuracy. */
+enum ncg_arithmetic { NCG_ARITH_SPLIT = 0, NCG_ARITH_F32 = 1 };
+
 /* Pair dispatch of ncg_contact_batch.
  * NCG_DISPATCH_SUPPORT_MAP: every pair through contact_support_map_support_map
  *   (GJK, then EPA) — the (&dyn SupportMap, &dyn SupportMap) semantics.
@@ -209,6 +224,9 @@ typedef struct ncg_stats {
 int ncg_ctx_create(ncg_ctx** out, int device);
 int ncg_ctx_destroy(ncg_ctx* ctx);
 int ncg_ctx_set_tolerance(ncg_ctx* ctx, int tolerance);
+/* Selects an ncg_arithmetic (no reference counterpart: the reference picks its
+ * arithmetic by instantiating N = f32 or f64). */
+int ncg_ctx_set_arithmetic(ncg_ctx* ctx, int arithmetic);
 int ncg_ctx_set_warm_start(ncg_ctx* ctx, int warm_start);
 int ncg_ctx_set_dispatch(ncg_ctx* ctx, int dispatch);
 /* Launch tuning (no reference counterpart).  Keys:

@@ -13,9 +13,10 @@ from . import build as _build
 
 LIB_PATH = _build.LIB_PATH
 
-ABI_VERSION = 2  # NCG_ABI_VERSION of include/ncg.h
+ABI_VERSION = 3  # NCG_ABI_VERSION of include/ncg.h
 NCG_OK, NCG_EINVAL, NCG_ECUDA, NCG_ENOMEM, NCG_ENOTBUILT, NCG_EINTERNAL = 0, -1, -2, -3, -4, -5
 TOL_REFERENCE, TOL_PRECISE = 0, 1
+ARITH_SPLIT, ARITH_F32 = 0, 1
 WARM_NONE, WARM_INIT_DIR, WARM_MLP = 0, 1, 2
 
 STATUS_GJK_MAX_ITER = 1 << 0
@@ -37,7 +38,7 @@ EXPORTED = [
     "ncg_mlp_grad", "ncg_mlp_adam", "ncg_time_of_impact_batch",
     "ncg_ray_cast_batch", "ncg_aabb_batch", "ncg_bp_create", "ncg_bp_update", "ncg_bp_results",
     "ncg_bp_destroy", "ncg_bp_copy", "ncg_gather_pairs", "ncg_manifold_batch", "ncg_autotune",
-    "ncg_ctx_get_tuning",
+    "ncg_ctx_get_tuning", "ncg_ctx_set_arithmetic",
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
 TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT, TUNE_HULL_STAGE_MIN, TUNE_HULL_STAGE_CAP = range(6)
@@ -93,6 +94,7 @@ def load(build_if_missing=True):
     L.ncg_ctx_create.argtypes = [P(vp), i32]
     L.ncg_ctx_destroy.argtypes = [vp]
     L.ncg_ctx_set_tolerance.argtypes = [vp, i32]
+    L.ncg_ctx_set_arithmetic.argtypes = [vp, i32]
     L.ncg_ctx_set_warm_start.argtypes = [vp, i32]
     L.ncg_sync.argtypes = [vp, vp]
     L.ncg_get_stats.argtypes = [vp, P(NcgStats)]

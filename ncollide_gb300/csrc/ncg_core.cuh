@@ -32,7 +32,21 @@
 
 namespace ncg {
 
+// The arithmetic of the sub-solve, GJK's bounds and EPA's distances: double-word
+// (FP64-class on the FP32 pipes) by default; plain f32, the reference's own f32
+// path, in the translation units built with NCG_REAL_F32.  The stage kernels
+// and launchers of a translation unit live in namespace NCG_ARITH_NS (dwa or
+// f32a), so that one library holds both builds of the GJK and EPA stages.
+#ifdef NCG_REAL_F32
+using real = f32r;
+#define NCG_ARITH_NS f32a
+#else
 using real = dw;
+#define NCG_ARITH_NS dwa
+#endif
+// A host-computed constant (split into two floats) in `real`.
+NCG_DEV real from_host(dw_host x) { return real(x.h, x.l); }
+NCG_DEV real dw_max() { return real(FLT_MAX); }
 
 // ------------------------------------------------------------------ vectors
 template <class T> struct vec3 {

@@ -55,7 +55,6 @@ inline dw_host dw_split(double d) {
     float h = (float)d;
     return dw_host{h, (float)(d - (double)h)};
 }
-NCG_DEV dw from_host(dw_host x) { return dw(x.h, x.l); }
 
 NCG_DEV dw two_sum(float a, float b) {
     float s = a + b;
@@ -122,6 +121,30 @@ NCG_DEV bool operator>=(dw a, dw b) { return b <= a; }
 NCG_DEV bool operator==(dw a, dw b) { return a.h == b.h && a.l == b.l; }
 NCG_DEV bool operator!=(dw a, dw b) { return !(a == b); }
 
-NCG_DEV dw dw_max() { return dw(FLT_MAX); }
+// ---------------------------------------------------------------- f32r
+// Plain f32 arithmetic behind the same interface: the reference's f32 path
+// (every sub-solve, bound and EPA distance in f32), used by the translation
+// units built with NCG_REAL_F32.  `l` is always zero, so records laid out
+// for double-words (heap keys, spill headers) hold the same bits.
+struct f32r {
+    float h, l;
+    NCG_DEV f32r() : h(0.0f), l(0.0f) {}
+    NCG_DEV f32r(float a) : h(a), l(0.0f) {}
+    NCG_DEV f32r(float a, float) : h(a), l(0.0f) {}
+    NCG_DEV explicit operator float() const { return h; }
+};
+NCG_DEV f32r operator+(f32r x, f32r y) { return f32r(__fadd_rn(x.h, y.h)); }
+NCG_DEV f32r operator-(f32r x) { return f32r(-x.h); }
+NCG_DEV f32r operator-(f32r x, f32r y) { return f32r(__fsub_rn(x.h, y.h)); }
+NCG_DEV f32r operator*(f32r x, f32r y) { return f32r(__fmul_rn(x.h, y.h)); }
+NCG_DEV f32r operator/(f32r x, f32r y) { return f32r(__fdiv_rn(x.h, y.h)); }
+NCG_DEV f32r sqrt(f32r x) { return f32r(__fsqrt_rn(x.h)); }
+NCG_DEV f32r fabs(f32r x) { return f32r(fabsf(x.h)); }
+NCG_DEV bool operator<(f32r a, f32r b) { return a.h < b.h; }
+NCG_DEV bool operator<=(f32r a, f32r b) { return a.h <= b.h; }
+NCG_DEV bool operator>(f32r a, f32r b) { return a.h > b.h; }
+NCG_DEV bool operator>=(f32r a, f32r b) { return a.h >= b.h; }
+NCG_DEV bool operator==(f32r a, f32r b) { return a.h == b.h; }
+NCG_DEV bool operator!=(f32r a, f32r b) { return a.h != b.h; }
 
 }  // namespace ncg

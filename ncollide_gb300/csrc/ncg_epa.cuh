@@ -27,13 +27,14 @@
 // strict total order the pop sequence depends only on the set of entries, not
 // on how the heap is arranged, so the entries of deleted faces can be dropped
 // whenever the heap fills up.  Equal keys (the only case where this differs
-// from Rust's BinaryHeap) pop first-in first-out.
+// from Rust's BinaryHeap) pop first-in first-out.  The f32 build
+// (NCG_REAL_F32) keeps Rust's BinaryHeap instead, deleted entries included.
 //
 // Arithmetic: the expansion (Face::new's projection of the origin, the
 // visibility test of the silhouette) runs in f32; each face normal is the
 // double-word cross product of exact double-word edge vectors, normalised in
 // f32 and stored in f32; face distances, queue keys and the termination tests
-// are double-word.
+// are double-word (all f32 in the f32 build: `real`).
 //
 // Work split inside a warp (WarpExec): the support point along the popped
 // face's normal uses every lane (the hull arg-max is warp-parallel); the faces
@@ -71,7 +72,7 @@ struct EpaStore {
     float4* vpt;      // [VC]
     float* vo;        // [VC][6] orig1 xyz, orig2 xyz
     float4* face;     // [FC][2] float4 (normal xyz, pts p0 | p1 << 16), uint4 (p2 | gen << 16, adj0..2)
-    float4* heap;     // [FC] key hi, key lo, seq, ref
+    float4* heap;     // [HC] key hi, key lo, seq, ref
     uint32_t* freel;  // [FC] free slots (stack)
     uint32_t* sref;   // [SC] silhouette face references
     uint32_t* snew;   // [SC] reference of the face built on edge k
@@ -83,21 +84,22 @@ struct EpaStore {
     uint32_t* tref;   // [TC] flood-fill stack: references
     uint8_t* topp;    // [TC] flood-fill stack: opposite vertex
     int VC, FC, SC, TC;
+    int HC;  // heap entries: FC, or more for the f32 build's largest store (its heap keeps deleted faces)
 
     static constexpr __host__ __device__ size_t r16(size_t b) { return (b + 15) & ~size_t(15); }
     // Bytes of one store.
-    static constexpr __host__ __device__ size_t bytes(int VC, int FC, int SC, int TC) {
-        return r16(16 * (size_t)VC) + r16(32 * (size_t)FC) + r16(16 * (size_t)FC) +
+    static constexpr __host__ __device__ size_t bytes(int VC, int FC, int SC, int TC, int HC) {
+        return r16(16 * (size_t)VC) + r16(32 * (size_t)FC) + r16(16 * (size_t)HC) +
                r16(4 * (size_t)FC) + 4 * r16(4 * (size_t)SC) + r16(8 * (size_t)SC) + 2 * r16((size_t)SC) +
                r16(4 * (size_t)TC) + r16((size_t)TC) + r16(24 * (size_t)VC);
     }
 
-    NCG_DEV void carve(char* base, int vc, int fc, int sc, int tc) {
-        VC = vc; FC = fc; SC = sc; TC = tc;
+    NCG_DEV void carve(char* base, int vc, int fc, int sc, int tc, int hc) {
+        VC = vc; FC = fc; SC = sc; TC = tc; HC = hc;
         char* p = base;
         vpt = (float4*)p; p += r16(16 * (size_t)VC);
         face = (float4*)p; p += r16(32 * (size_t)FC);
-        heap = (float4*)p; p += r16(16 * (size_t)FC);
+        heap = (float4*)p; p += r16(16 * (size_t)HC);
         freel = (uint32_t*)p; p += r16(4 * (size_t)FC);
         sref = (uint32_t*)p; p += r16(4 * (size_t)SC);
         snew = (uint32_t*)p; p += r16(4 * (size_t)SC);
@@ -211,6 +213,7 @@ struct EpaStore {
         return s == 0.0f || fabsf(s) <= tol.affine_eps_f;
     }
 
+#ifndef NCG_REAL_F32
     // ---- d-ary heap on (neg_dist, earlier push) — one thread only.  With a
     // strict total order the pop sequence does not depend on the arity
     // (NCG_EPA_HEAP_ARITY; 4- and 8-ary heaps measured no faster than binary:
@@ -263,9 +266,9 @@ struct EpaStore {
     }
     // Returns false when the heap is full even after purging.
     NCG_DEV bool push(int& size, uint32_t& seq, uint32_t ref, real key) {
-        if (size >= FC) {
+        if (size >= HC) {
             purge(size);
-            if (size >= FC) return false;
+            if (size >= HC) return false;
         }
         float4 e = make_float4(key.h, key.l, __uint_as_float(seq++), __uint_as_float(ref));
         sift_up(size++, e);
@@ -287,9 +290,70 @@ struct EpaStore {
         }
         return false;
     }
+#else
+    // ---- Rust's BinaryHeap on neg_dist alone (the reference f32 path): push
+    // sifts up while the entry is greater than its parent; pop moves the last
+    // entry to the root, sifts that hole to the bottom along the greater child
+    // (the right one on ties) and back up (alloc/collections/binary_heap).  The
+    // order among equal distances then follows the reference exactly, which
+    // needs the deleted faces' entries kept as the reference keeps them: a
+    // full heap is an overflow, never purged.
+    NCG_DEV static bool le(float4 a, float4 b) { return a.x <= b.x; }  // PartialOrd::le (false with NaN)
+    NCG_DEV void sift_up_from(int pos, float4 e) {
+        while (pos > 0) {
+            const int parent = (pos - 1) / 2;
+            const float4 p = heap[parent];
+            if (le(e, p)) break;
+            heap[pos] = p;
+            pos = parent;
+        }
+        heap[pos] = e;
+    }
+    NCG_DEV bool push(int& size, uint32_t& seq, uint32_t ref, real key) {
+        if (size >= HC) return false;
+        float4 e = make_float4(key.h, 0.0f, __uint_as_float(seq++), __uint_as_float(ref));
+        sift_up_from(size++, e);
+        return true;
+    }
+    NCG_DEV float4 pop_one(int& size) {
+        float4 item = heap[--size];
+        if (size > 0) {
+            const float4 top = heap[0];
+            int pos = 0, child = 1;
+            while (size >= 2 && child <= size - 2) {
+                child += le(heap[child], heap[child + 1]) ? 1 : 0;
+                heap[pos] = heap[child];
+                pos = child;
+                child = 2 * pos + 1;
+            }
+            if (child == size - 1) {
+                heap[pos] = heap[child];
+                pos = child;
+            }
+            sift_up_from(pos, item);
+            item = top;
+        }
+        return item;
+    }
+    NCG_DEV bool pop_live(int& size, int& fid, real& key, float4& popped) {
+        while (size > 0) {
+            const float4 e = pop_one(size);
+            const uint32_t r = __float_as_uint(e.w);
+            if (live(r)) {
+                fid = rslot(r);
+                key = real(e.x, e.y);
+                popped = e;
+                return true;
+            }
+        }
+        return false;
+    }
+#endif
+#ifndef NCG_REAL_F32
     // Puts a popped entry back unchanged (same key and push sequence, so the
     // pop order is as if it had never left).
     NCG_DEV void repush(int& size, float4 e) { sift_up(size++, e); }
+#endif
 };
 
 // Execution policies.
@@ -464,6 +528,14 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
         int fid = -1;
         real key(0.0f);
         float4 popped = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#ifdef NCG_REAL_F32
+        // Rust's heap cannot take a popped entry back unchanged: stop before
+        // the pop when no room is left for this iteration's support point
+        if (nv >= st.VC) {
+            res.exit = EPA_OVERFLOW;
+            return true;
+        }
+#endif
         if (lane == 0) {
             if (!st.pop_live(hsize, fid, key, popped)) fid = -1;
         }
@@ -477,6 +549,7 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
             res.exit = EPA_OK_HEAP_EMPTY;
             return true;
         }
+#ifndef NCG_REAL_F32
         if (nv >= st.VC) {
             // no room for this iteration's support point: put the face back and
             // stop between two iterations, so that a larger store can resume
@@ -487,6 +560,7 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
             res.exit = EPA_OVERFLOW;
             return true;
         }
+#endif
         res.iters++;
         int f0, f1, f2;
         st.pts(fid, f0, f1, f2);
@@ -672,7 +746,7 @@ NCG_DEV bool epa_step(const PairGeom& g, const Tol& tol, const Scan& scan, EpaSt
 // A polytope between two expansion steps, copied out of a store: a 64-byte
 // header (the EpaState scalars), then the used parts of the store's vertex,
 // witness, face, heap and free-list arrays, each at the offset it would have
-// for a store of capacities (VC, FC).  Slots, generations, heap entries and
+// for a store of capacities (VC, FC) whose heap holds FC entries.  Slots, generations, heap entries and
 // push sequences are copied unchanged, so a store with at least those
 // capacities continues exactly where this one stopped.
 struct EpaSpill {
@@ -719,7 +793,7 @@ NCG_DEV void epa_spill(const EpaStore& st, const EpaState& S, char* r) {
 // `st` and state S; false when `st` is smaller than the source store.
 template <class E>
 NCG_DEV bool epa_resume(const char* rc, int VC, int FC, EpaStore& st, EpaState& S) {
-    if (st.VC < VC || st.FC < FC) return false;
+    if (st.VC < VC || st.FC < FC || st.HC < FC) return false;
     char* r = const_cast<char*>(rc);
     const int lane = E::lane();
     const int4* h = (const int4*)r;

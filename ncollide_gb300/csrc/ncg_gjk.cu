@@ -2,6 +2,9 @@
 // counting sort by cost bucket, then GJK one thread per pair (analytic list,
 // and the ConvexHull list by default) or one warp per pair (ConvexHull list).
 // Pairs whose contact needs EPA leave their final simplex in the EPA queue.
+// Compiled twice into the library: as is (namespace dwa, the double-word
+// sub-solve) and through ncg_gjk_f32.cu with NCG_REAL_F32 (namespace f32a,
+// the reference's f32 path).
 //
 // The double-word sum, quotient and square root are kept out of line in this
 // translation unit: the GJK loop is bound by instruction fetch (its warps sit
@@ -24,6 +27,7 @@
 #endif
 
 namespace ncg {
+namespace NCG_ARITH_NS {
 namespace {
 
 // First search direction of each *_with_params wrapper.  An all-zero
@@ -363,4 +367,5 @@ cudaError_t gjk_set_carveout(int pct) {
     return cudaFuncSetAttribute(k_gjk_thread, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
 }
 
+}  // namespace NCG_ARITH_NS
 }  // namespace ncg

@@ -50,300 +50,6 @@ namespace {
 
 thread_local std::string g_last_error;
 
-// EPA store capacities: vertices, live face slots (about twice the vertices),
-// silhouette edges, flood-fill stack.  Store 0 is the per-thread store, 1-4
-// the warp stores (shared memory or one global slab per block).
-template <int T> struct EpaTier;
-// Compile-time tuning: the thread stage's capacity and its minimum resident
-// blocks per SM (which caps its registers).
-#ifndef NCG_EPA_THREAD_VC
-#define NCG_EPA_THREAD_VC 64
-#endif
-#ifndef NCG_EPA_THREAD_MIN_BLOCKS
-#define NCG_EPA_THREAD_MIN_BLOCKS 4
-#endif
-template <> struct EpaTier<0> {
-    static constexpr int VC = NCG_EPA_THREAD_VC, FC = 2 * VC + 16, SC = VC < 64 ? 32 : VC / 2, TC = 2 * VC;
-};
-// 1: shared-memory warp store (the no-allocation path); 2: the warp stage's
-// global slabs; 3: the wide stage (one global slab per SM).
-template <> struct EpaTier<1> { static constexpr int VC = 128, FC = 2 * 128 + 64, SC = 64, TC = 256; };
-template <> struct EpaTier<2> { static constexpr int VC = 1280, FC = 2 * 1280 + 64, SC = 512, TC = 2048; };
-template <> struct EpaTier<3> { static constexpr int VC = 10240, FC = 2 * 10240 + 64, SC = 4096, TC = 16384; };
-static_assert(EpaTier<3>::FC < 65536 && EpaTier<3>::VC < 65536, "16-bit face and vertex indices");
-// Warps per SM of the warp stage (registers allow 12 at 168 per thread).
-#ifndef NCG_WARP_STAGE_PER_SM
-#define NCG_WARP_STAGE_PER_SM 12
-#endif
-constexpr int WARP_STAGE_MAX_PER_SM = NCG_WARP_STAGE_PER_SM;
-template <int T> size_t tier_bytes() {
-    return EpaStore::bytes(EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC);
-}
-
-// Writes a contact finished by EPA.
-NCG_DEV void write_epa(const Outputs& o, const EpaItem& it, const EpaResult& r, uint32_t extra_status) {
-    const uint32_t i = it.pair;
-    ncg_contact c;
-    memset(&c, 0, sizeof(c));
-    uint8_t tag = 0;
-    vec3<real> dir = mk(real(1.0f), real(0.0f), real(0.0f));
-    if (epa_ok(r.exit)) {
-        tag = 1;
-        wr3(c.world1, r.p1);
-        wr3(c.world2, r.p2);
-        wr3(c.normal, r.n);
-        c.depth = (-dot(r.n, r.p2 - r.p1)).h;
-        dir = r.n;
-    }
-    o.contact[i] = c;
-    o.tag[i] = tag;
-    if (o.dir) wr3(o.dir + 3 * (size_t)i, dir);
-    o.status[i] = it.status | r.status | extra_status;
-    if (o.iters) o.iters[i] = pack_iters(it.gjk_iters, r.iters);
-}
-
-NCG_DEV PairGeom load_geom(const ncg_batch& b, uint32_t i) {
-    PairGeom g;
-    load_shape(b, b.g1[i], g.g1);
-    load_shape(b, b.g2[i], g.g2);
-    g.m1 = load_pose(b.m1 + i);
-    g.m2 = load_pose(b.m2 + i);
-    return g;
-}
-
-// The geometry an EPA work item runs on (mode 1: the translated hull against
-// ConstantOrigin).
-NCG_DEV PairGeom item_geom(const ncg_batch& b, const EpaItem& it) {
-    PairGeom g = load_geom(b, it.pair);
-    if (it.mode == 0) return g;
-    const Pose& pb = it.flip ? g.m2 : g.m1;
-    const Pose& pp = it.flip ? g.m1 : g.m2;
-    const Shape& sp = it.flip ? g.g1 : g.g2;
-    return projection_geom(pp, sp, pb.t);
-}
-
-// Finishes an EPA work item: a contact (mode 0) or the ball-hull contact from
-// the EPA projection of the ball's centre (mode 1).
-NCG_DEV void finish_epa(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const EpaItem& it,
-                        const EpaResult& r, uint32_t extra_status) {
-    if (it.mode == 0) {
-        write_epa(o, it, r, extra_status);
-        return;
-    }
-    PairGeom g = load_geom(b, it.pair);
-    const Pose& pb = it.flip ? g.m2 : g.m1;
-    const Shape& sb = it.flip ? g.g2 : g.g1;
-    const bool ok = epa_ok(r.exit);
-    vec3<real> w2 = ok ? r.p1 + to_r(pb.t) : to_r(pb.t);
-    QContact q = ball_polyhedron_assemble(pb.t, sb.p0, true, w2, F_UNKNOWN, 0, false, from_host(qp.param), it.flip != 0);
-    write_qcontact(o, it.pair, q, it.status | r.status | extra_status, pack_iters(it.gjk_iters, r.iters));
-}
-
-NCG_DEV void load_simplex(const EpaItem& it, CSO* sv) {
-    for (int k = 0; k <= it.dim; ++k) {
-        const float* w = it.v[k];
-        sv[k] = CSO{{w[0], w[1], w[2]}, {w[3], w[4], w[5]}, {w[6], w[7], w[8]}};
-    }
-}
-
-// A warp EPA stage: one warp per pair (one warp per block), the polytope in
-// dynamic shared memory or in a global-memory slab per block.  It drains queue
-// q_in, then q_in2 (when >= 0); a pair whose polytope outgrows the store is
-// queued on q_out and re-run there from GJK's simplex, or, when q_out < 0,
-// ends with NCG_STATUS_EPA_CAPACITY.  One kernel serves every stage (runtime
-// capacities) to keep the code footprint small.
-struct TierCaps {
-    int q_in, q_in2, q_out;
-    int slab;  // -1: shared memory; else index into Scratch::slabs
-    int VC, FC, SC, TC;
-};
-#ifndef NCG_EPA_WARP_MIN_BLOCKS
-#define NCG_EPA_WARP_MIN_BLOCKS 1
-#endif
-__global__ void __launch_bounds__(32, NCG_EPA_WARP_MIN_BLOCKS) k_epa(ncg_batch b, QueryParams qp, Outputs o, Scratch s, TierCaps tc) {
-    extern __shared__ __align__(16) char smem[];
-    const unsigned lane = threadIdx.x & 31u;
-    EpaStore st;
-    if (tc.slab < 0) {
-        st.carve(smem, tc.VC, tc.FC, tc.SC, tc.TC);
-    } else {
-        if (blockIdx.x >= (unsigned)s.n_slabs[tc.slab]) return;
-        st.carve(s.slabs[tc.slab] + (size_t)blockIdx.x * s.slab_bytes[tc.slab], tc.VC, tc.FC, tc.SC, tc.TC);
-    }
-    WarpScan scan{reinterpret_cast<const float4*>(b.hull_points)};
-    unsigned long long acc = 0;
-    int q = tc.q_in;
-    unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[q];
-    for (;;) {
-        unsigned long long k = 0;
-        if (lane == 0) k = atomicAdd(&s.ctr->epa_next[q], 1ull);
-        k = __shfl_sync(0xffffffffu, k, 0);
-        if (k >= n) {
-            if (q == tc.q_in && tc.q_in2 >= 0) {
-                q = tc.q_in2;
-                n = *(volatile unsigned long long*)&s.ctr->epa_count[q];
-                continue;
-            }
-            break;
-        }
-        const uint32_t item = s.queue[q][k];
-        const EpaItem& it = s.items[item];
-        PairGeom g = item_geom(b, it);
-        EpaState S;
-        bool done;
-        if (it.spilled && epa_resume<WarpExec>(s.spill + (size_t)s.spill_of[item] * s.spill_bytes, EpaTier<0>::VC,
-                                                EpaTier<0>::FC, st, S)) {
-            // the thread stage's polytope: continue where it stopped
-            done = false;
-        } else {
-            CSO sv[4];
-            load_simplex(it, sv);
-            done = epa_begin<WarpExec>(g, it.dim, sv, qp.tol, scan, st, S);
-        }
-        while (!done) done = epa_step<WarpExec>(g, qp.tol, scan, st, S, qp.epa_max_iter);
-        const EpaResult& r = S.res;
-        if (epa_overflow(r.exit) && tc.q_out >= 0) {
-            if (lane == 0) {
-                unsigned long long pos = atomicAdd(&s.ctr->epa_count[tc.q_out], 1ull);
-                s.queue[tc.q_out][pos] = item;
-            }
-        } else {
-            acc += r.iters;
-            if (lane == 0) {
-                if (epa_overflow(r.exit)) {
-                    EpaResult none = r;
-                    none.exit = EPA_NONE;
-                    finish_epa(b, qp, o, it, none, NCG_STATUS_EPA_CAPACITY);
-                } else {
-                    finish_epa(b, qp, o, it, r, 0);
-                }
-            }
-        }
-        __syncwarp();
-    }
-    if (lane == 0 && acc) atomicAdd(&s.ctr->epa_iters, acc);
-}
-// The thread stage's scheduler: each thread takes the next EPA item from the
-// queue as soon as its current one finishes (a pair needs 1 to ~60 steps
-// here); with a fixed item per lane and round, the lanes whose pairs finished
-// early would idle until the round's longest pair was done.
-NCG_DEV void epa_thread_finish(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                               uint32_t item, const EpaResult& r, unsigned long long& acc, const EpaStore& st,
-                               const EpaState& S) {
-    EpaItem& it = s.items[item];
-    if (epa_overflow(r.exit)) {
-        // keep the polytope (when a spill record is free and the store
-        // stopped between two steps) so that the warp stage resumes it
-        // instead of repeating these iterations
-        if (s.spill && r.exit == EPA_OVERFLOW) {
-            const unsigned long long rec = atomicAdd(&s.ctr->spill_next, 1ull);
-            if (rec < s.spill_cap) {
-                epa_spill<ThreadExec>(st, S, s.spill + (size_t)rec * s.spill_bytes);
-                s.spill_of[item] = (uint32_t)rec;
-                it.spilled = 1;
-            }
-        }
-        // pairs of two curved shapes (their polytopes grow longest) go first;
-        // the shape kinds are re-read here (rare path) rather than kept live
-        const uint32_t k1 = s.bucket_kind1(b, it.pair), k2 = s.bucket_kind2(b, it.pair);
-        const bool curved = k1 != NCG_CUBOID && k1 != NCG_CONVEX_HULL && k2 != NCG_CUBOID && k2 != NCG_CONVEX_HULL;
-        const int qo = curved ? Q_WARP_LONG : Q_WARP;
-        unsigned long long pos = atomicAdd(&s.ctr->epa_count[qo], 1ull);
-        s.queue[qo][pos] = item;
-    } else {
-        acc += r.iters;
-        finish_epa(b, qp, o, it, r, 0);
-    }
-}
-
-// Takes the next thread-stage queue entry: one atomic per group of lanes
-// asking together, which get consecutive entries (pairs of one kind, adjacent).
-NCG_DEV unsigned long long epa_thread_fetch(const Scratch& s, int q) {
-    const unsigned m = __activemask();
-    const int lead = __ffs(m) - 1;
-    const unsigned rank = __popc(m & ((1u << (threadIdx.x & 31u)) - 1u));
-    unsigned long long base = 0;
-    if ((int)(threadIdx.x & 31u) == lead) base = atomicAdd(&s.ctr->epa_next[q], (unsigned long long)__popc(m));
-    base = __shfl_sync(m, base, lead);
-    return base + rank;
-}
-
-// Thread-stage scheduling (compile-time): 0 runs each item to its end, then
-// takes the next (default); 1 advances every thread's pair by one expansion
-// step per pass of one loop, taking a new item as soon as a pair ends (the
-// lanes stay on the same step of the loop body whatever pairs they hold).
-// Both take items dynamically; 1 measured 12% slower on mixed pairs and 11%
-// on short cuboid pairs (a larger loop body around the step).
-#ifndef NCG_EPA_THREAD_SCHED
-#define NCG_EPA_THREAD_SCHED 0
-#endif
-
-NCG_DEV void epa_thread_loop(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                             EpaStore& st, int q) {
-    const unsigned long long n = *(volatile unsigned long long*)&s.ctr->epa_count[q];
-    ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
-    unsigned long long acc = 0;
-    EpaState S;
-    PairGeom g;
-    uint32_t item = 0;
-#if NCG_EPA_THREAD_SCHED == 0
-    for (;;) {
-        const unsigned long long k = epa_thread_fetch(s, q);
-        if (k >= n) break;
-        item = s.queue[q][k];
-        const EpaItem& it = s.items[item];
-        g = item_geom(b, it);
-        CSO sv[4];
-        load_simplex(it, sv);
-        bool done = epa_begin<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, S);
-        while (!done) done = epa_step<ThreadExec>(g, qp.tol, scan, st, S, qp.epa_max_iter);
-        epa_thread_finish(b, qp, o, s, item, S.res, acc, st, S);
-    }
-#else
-    bool active = false;
-    for (;;) {
-        // take items until one needs expansion steps (or the queue is empty)
-        while (!active) {
-            const unsigned long long k = epa_thread_fetch(s, q);
-            if (k >= n) break;
-            item = s.queue[q][k];
-            const EpaItem& it = s.items[item];
-            g = item_geom(b, it);
-            CSO sv[4];
-            load_simplex(it, sv);
-            if (epa_begin<ThreadExec>(g, it.dim, sv, qp.tol, scan, st, S))
-                epa_thread_finish(b, qp, o, s, item, S.res, acc, st, S);
-            else
-                active = true;
-        }
-        if (!active) break;
-        if (epa_step<ThreadExec>(g, qp.tol, scan, st, S, qp.epa_max_iter)) {
-            epa_thread_finish(b, qp, o, s, item, S.res, acc, st, S);
-            active = false;
-        }
-    }
-#endif
-    warp_add(&s.ctr->epa_iters, acc);
-}
-
-template <int T> TierCaps caps(int q_in, int q_in2, int q_out, int slab) {
-    return TierCaps{q_in, q_in2, q_out, slab, EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC};
-}
-
-// Thread stage: one thread per pair, the polytope in the thread's local
-// memory (L1 write-back; a per-thread global slab measured 17% slower, its
-// stores write through to L2).  A pair that outgrows it goes to warp tier A.
-constexpr size_t THREAD_STORE_BYTES =
-    EpaStore::bytes(EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
-__global__ void __launch_bounds__(128, NCG_EPA_THREAD_MIN_BLOCKS)
-k_epa_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int q) {
-    __align__(16) char buf[THREAD_STORE_BYTES];
-    EpaStore st;
-    st.carve(buf, EpaTier<0>::VC, EpaTier<0>::FC, EpaTier<0>::SC, EpaTier<0>::TC);
-    epa_thread_loop(b, qp, o, s, st, q);
-}
-
-
 // ------------------------------------------------------------------ host side
 }  // namespace
 namespace ncg {
@@ -387,6 +93,45 @@ Tol make_tol(int mode) {
     return t;
 }
 
+// The same sets for the f32 build, each constant computed in f32 as the
+// reference's f32 path computes it (eps_tol = 10 eps, eps_rel = sqrt(eps_tol),
+// 100 eps, (100 eps)^2); the PRECISE set's f64 constants rounded to f32.
+Tol make_tol_f32(int mode) {
+    Tol t;
+    const float e = FLT_EPSILON;
+    const float et = e * 10.0f, e100 = e * 100.0f;
+    auto f = [](float x) { return dw_host{x, 0.0f}; };
+    t.eps = f(e);
+    t.eps_tol = f(et);
+    t.eps_rel = f(sqrtf(et));
+    t.epa_eps_tol = f(e100);
+    t.affine_eps = f(e100 * e100);
+    t.add_tol = t.eps_tol;
+    if (mode == NCG_TOL_PRECISE) {
+        t.eps_rel = f((float)std::sqrt(10.0 * (double)DBL_EPSILON));
+        t.add_tol = f((float)(10.0 * (double)DBL_EPSILON));
+        t.epa_eps_tol = f((float)1e-6);
+    }
+    t.best_on_failure = mode == NCG_TOL_PRECISE ? 1 : 0;
+    t.eps_tol_f = t.eps_tol.h;
+    t.affine_eps_f = t.affine_eps.h;
+    t.init_eps = FLT_EPSILON;
+    return t;
+}
+
+// The launchers of one build of the GJK and EPA stages.
+struct Stages {
+    decltype(&dwa::gjk_launch_sort) sort;
+    decltype(&dwa::gjk_launch_thread) gjk_thread;
+    decltype(&dwa::gjk_launch_warp) gjk_warp;
+    decltype(&dwa::epa_launch_thread) epa_thread;
+    decltype(&dwa::epa_launch_warp) epa_warp;
+};
+const Stages STAGES_SPLIT{dwa::gjk_launch_sort, dwa::gjk_launch_thread, dwa::gjk_launch_warp, dwa::epa_launch_thread,
+                          dwa::epa_launch_warp};
+const Stages STAGES_F32{f32a::gjk_launch_sort, f32a::gjk_launch_thread, f32a::gjk_launch_warp,
+                        f32a::epa_launch_thread, f32a::epa_launch_warp};
+
 }  // namespace
 
 // Stage-timing events of one call: a start mark and one per launch group.
@@ -396,6 +141,7 @@ struct ncg_ctx {
     int device = 0;
     int num_sms = 0;
     int tol_mode = NCG_TOL_REFERENCE;
+    int arith = NCG_ARITH_SPLIT;
     int warm = NCG_WARM_NONE;
     int dispatch = NCG_DISPATCH_SUPPORT_MAP;
     int hull_gjk_warp = 0;  // GJK of ConvexHull pairs: 0 one thread per pair, 1 one warp per pair
@@ -439,7 +185,6 @@ namespace {
 // Spill records of the thread stage: one per 32 pairs of capacity (the
 // thread stage's overflow is ~1-3% of the pairs on mixed workloads; beyond
 // the records, pairs restart from GJK's simplex as without them).
-constexpr size_t SPILL_BYTES = (EpaSpill::bytes(EpaTier<0>::VC, EpaTier<0>::FC) + 255) & ~size_t(255);
 uint64_t spill_records(uint64_t cap) { return cap / 32 < 256 ? 256 : cap / 32; }
 
 bool ensure_scratch(ncg_ctx* c, uint64_t n) {
@@ -509,12 +254,10 @@ struct Limits {
 };
 Limits launch_limits() {
     Limits l;
-    cudaFuncSetAttribute(k_epa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tier_bytes<2>());
-    gjk_occupancy(&l.occ_thread, &l.occ_warp);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_ethread, k_epa_thread, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_global, k_epa, 32, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_smem[0], k_epa, 32, tier_bytes<1>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l.occ_smem[1], k_epa, 32, tier_bytes<2>());
+    // grids are sized from the double-word build's kernels (the f32 build's
+    // use no more registers)
+    dwa::gjk_occupancy(&l.occ_thread, &l.occ_warp);
+    dwa::epa_occupancy(&l.occ_ethread, &l.occ_global, l.occ_smem);
     int* all[] = {&l.occ_thread, &l.occ_warp, &l.occ_ethread, &l.occ_global, &l.occ_smem[0], &l.occ_smem[1]};
     for (int* v : all)
         if (*v < 1) *v = 1;
@@ -526,9 +269,10 @@ Limits launch_limits() {
 // (their local-memory and hull traffic wants the largest L1).
 bool set_carveout(int pct) {
     bool ok = true;
-    ok &= cuda_ok(gjk_set_carveout(pct), "carveout(k_gjk_thread)");
-    ok &= cuda_ok(cudaFuncSetAttribute(k_epa_thread, cudaFuncAttributePreferredSharedMemoryCarveout, pct),
-                  "carveout(k_epa_thread)");
+    ok &= cuda_ok(dwa::gjk_set_carveout(pct), "carveout(k_gjk_thread)");
+    ok &= cuda_ok(dwa::epa_set_carveout(pct), "carveout(k_epa_thread)");
+    ok &= cuda_ok(f32a::gjk_set_carveout(pct), "carveout(k_gjk_thread, f32)");
+    ok &= cuda_ok(f32a::epa_set_carveout(pct), "carveout(k_epa_thread, f32)");
     return ok;
 }
 
@@ -556,8 +300,10 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     qp.use_init_dir = (c->warm == NCG_WARM_INIT_DIR && b->init_dir) ? 1 : 0;
     qp.gjk_max_iter = 10000;
     qp.epa_max_iter = 10000;
-    qp.param = dw_split((double)param);
-    qp.tol = make_tol(c->tol_mode);
+    const bool f32 = c->arith == NCG_ARITH_F32;
+    const Stages& sg = f32 ? STAGES_F32 : STAGES_SPLIT;
+    qp.param = f32 ? dw_host{param, 0.0f} : dw_split((double)param);
+    qp.tol = f32 ? make_tol_f32(c->tol_mode) : make_tol(c->tol_mode);
     ncg_batch bb = *b;
     uint32_t launches = 0;
     c->n_marks = 0;
@@ -582,11 +328,11 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
         launches += 2;
     }
     mark(-1);
-    gjk_launch_sort(bb, qp, o, s, st);
+    sg.sort(bb, qp, o, s, st);
     mark(0);
     const int gjk_grid = c->num_sms * (c->gjk_blocks > 0 ? c->gjk_blocks : c->occ_thread);
     const int epa_grid = c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread);
-    gjk_launch_thread(gjk_grid, bb, qp, o, s, 0, 0, 0, st);
+    sg.gjk_thread(gjk_grid, bb, qp, o, s, 0, 0, 0, st);
     mark(1);
     launches += 3;
     // With the hull points still in flight, the analytic pairs' thread-stage
@@ -595,7 +341,7 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     const bool split = query == Q_CONTACT && hull_ready != nullptr;
     const int hull_queue = split ? Q_THREAD_HULL : 0;
     if (split) {
-        k_epa_thread<<<epa_grid, 128, 0, st>>>(bb, qp, o, s, 0);
+        sg.epa_thread(epa_grid, bb, qp, o, s, 0, st);
         mark(3);
         launches += 1;
     }
@@ -606,19 +352,19 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
                                                      : std::max(0, std::min(NB_HULL, 3 + NB_HULL - c->hull_gjk_warp));
     if (warp_buckets > 0) {
         const bool staged = c->hstage_min > 0 && c->occ_hstage > 0;
-        gjk_launch_warp(c->num_sms * (staged ? c->occ_hstage : c->occ_warp), bb, qp, o, s, warp_buckets,
-                        staged ? (uint32_t)c->hstage_min : 0u, (uint32_t)c->hstage_cap, st);
+        sg.gjk_warp(c->num_sms * (staged ? c->occ_hstage : c->occ_warp), bb, qp, o, s, warp_buckets,
+                    staged ? (uint32_t)c->hstage_min : 0u, (uint32_t)c->hstage_cap, st);
     }
-    if (warp_buckets < NB_HULL) gjk_launch_thread(gjk_grid, bb, qp, o, s, 1, warp_buckets, hull_queue, st);
+    if (warp_buckets < NB_HULL) sg.gjk_thread(gjk_grid, bb, qp, o, s, 1, warp_buckets, hull_queue, st);
     mark(2);
     launches += (warp_buckets > 0 ? 1 : 0) + (warp_buckets < NB_HULL ? 1 : 0);
     if (query == Q_CONTACT) {
-        k_epa_thread<<<epa_grid, 128, 0, st>>>(bb, qp, o, s, hull_queue);
+        sg.epa_thread(epa_grid, bb, qp, o, s, hull_queue, st);
         mark(3);
         // warp stage: the thread stage's overflow, pairs of curved shapes first
-        k_epa<<<c->n_slabs[0], 32, 0, st>>>(bb, qp, o, s, caps<2>(Q_WARP_LONG, Q_WARP, 3, 0));
+        sg.epa_warp(c->n_slabs[0], 0, bb, qp, o, s, caps<2>(Q_WARP_LONG, Q_WARP, 3, 0), st);
         mark(4);
-        k_epa<<<c->n_slabs[1], 32, 0, st>>>(bb, qp, o, s, caps<3>(3, -1, -1, 1));
+        sg.epa_warp(c->n_slabs[1], 0, bb, qp, o, s, caps<3>(3, -1, -1, 1), st);
         mark(5);
         launches += 3;
     }
@@ -657,7 +403,8 @@ int ncg_ctx_create(ncg_ctx** out, int device) {
     c->occ_smem[0] = lim.occ_smem[0];
     c->occ_smem[1] = lim.occ_smem[1];
     set_carveout(c->l1_carveout);
-    c->occ_hstage = gjk_warp_stage_occupancy((uint32_t)c->hstage_cap);
+    c->occ_hstage = dwa::gjk_warp_stage_occupancy((uint32_t)c->hstage_cap);
+    (void)f32a::gjk_warp_stage_occupancy((uint32_t)c->hstage_cap);
     c->slab_bytes[0] = (tier_bytes<2>() + 255) & ~size_t(255);
     c->slab_bytes[1] = (tier_bytes<3>() + 255) & ~size_t(255);
     c->n_slabs[0] = c->num_sms * c->occ_global;
@@ -699,6 +446,12 @@ int ncg_ctx_set_tolerance(ncg_ctx* c, int tol) {
     return NCG_OK;
 }
 
+int ncg_ctx_set_arithmetic(ncg_ctx* c, int arith) {
+    if (!c || (arith != NCG_ARITH_SPLIT && arith != NCG_ARITH_F32)) return NCG_EINVAL;
+    c->arith = arith;
+    return NCG_OK;
+}
+
 int ncg_ctx_set_mlp_params(ncg_ctx* c, const float* params, int n) {
     if (!c || !params || n != NCG_MLP_N_PARAMS) { g_last_error = "expected NCG_MLP_N_PARAMS parameters"; return NCG_EINVAL; }
     if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
@@ -736,7 +489,8 @@ int ncg_ctx_set_tuning(ncg_ctx* c, int key, int value) {
     case NCG_TUNE_HULL_STAGE_CAP: {
         if (value < 32 || value > 2048 || value % 32 != 0) return NCG_EINVAL;
         if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
-        const int occ = gjk_warp_stage_occupancy((uint32_t)value);
+        const int occ = dwa::gjk_warp_stage_occupancy((uint32_t)value);
+        (void)f32a::gjk_warp_stage_occupancy((uint32_t)value);
         if (occ <= 0) { g_last_error = "hull stage does not fit in shared memory"; return NCG_EINVAL; }
         c->hstage_cap = value;
         c->occ_hstage = occ;
@@ -1234,7 +988,8 @@ int ncg_proximity_batch_host(ncg_ctx* c, const ncg_batch* b, float margin, uint8
 namespace {
 constexpr uint64_t NA_MAX_PAIRS = NCG_NOALLOC_MAX_PAIRS;
 constexpr size_t NA_SLAB_BYTES =
-    (EpaStore::bytes(EpaTier<3>::VC, EpaTier<3>::FC, EpaTier<3>::SC, EpaTier<3>::TC) + 255) & ~size_t(255);
+    (EpaStore::bytes(EpaTier<3>::VC, EpaTier<3>::FC, EpaTier<3>::SC, EpaTier<3>::TC, EpaTier<3>::FC) + 255) &
+    ~size_t(255);
 constexpr size_t NA_ITEMS_BYTES = sizeof(EpaItem) * NA_MAX_PAIRS;
 constexpr size_t NA_LISTS_BYTES = (2 + N_EPA_QUEUES) * 4 * NA_MAX_PAIRS;
 constexpr size_t NA_BYTES = CTR_SLOT + NA_ITEMS_BYTES + NA_LISTS_BYTES + NA_SLAB_BYTES;
@@ -1339,14 +1094,17 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
 
     // The array keeps the previous call's contents: reset the counters and queues' heads.
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset noalloc counters")) return NCG_ECUDA;
-    gjk_launch_sort(bb, qp, o, s, st);
-    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 0, 0, 0, st);
-    gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 1, 0, 0, st);
-    k_epa_thread<<<d.num_sms * d.lim.occ_ethread, 128, 0, st>>>(bb, qp, o, s, 0);
+    dwa::gjk_launch_sort(bb, qp, o, s, st);
+    dwa::gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 0, 0, 0, st);
+    dwa::gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 1, 0, 0, st);
+    dwa::epa_launch_thread(d.num_sms * d.lim.occ_ethread, bb, qp, o, s, 0, st);
     // warp stages in shared memory (128, then 1280 vertices), then the one global slab
-    k_epa<<<d.num_sms * d.lim.occ_smem[0], 32, tier_bytes<1>(), st>>>(bb, qp, o, s, caps<1>(Q_WARP_LONG, Q_WARP, 3, -1));
-    k_epa<<<d.num_sms * d.lim.occ_smem[1], 32, tier_bytes<2>(), st>>>(bb, qp, o, s, caps<2>(3, -1, 4, -1));
-    k_epa<<<1, 32, 0, st>>>(bb, qp, o, s, caps<3>(4, -1, -1, 0));
+    dwa::epa_launch_warp(d.num_sms * d.lim.occ_smem[0], tier_bytes<1>(), bb, qp, o, s, caps<1>(Q_WARP_LONG, Q_WARP, 3, -1),
+                         st);
+    dwa::epa_launch_warp(d.num_sms * d.lim.occ_smem[1], tier_bytes<2>(), bb, qp, o, s, caps<2>(3, -1, 4, -1), st);
+    TierCaps last = caps<3>(4, -1, -1, 0);
+    last.HC = last.FC;  // the slab above: the double-word build's heap never holds more than FC entries
+    dwa::epa_launch_warp(1, 0, bb, qp, o, s, last, st);
     return cuda_ok(cudaGetLastError(), "noalloc kernel launch") ? NCG_OK : NCG_ECUDA;
 }
 

@@ -8,6 +8,7 @@
 #include <cstring>
 
 #include "ncg_core.cuh"
+#include "ncg_epa.cuh"
 #include "ncg_query.cuh"
 #include "ncg_sort.cuh"
 
@@ -185,29 +186,107 @@ NCG_DEV void warp_add(unsigned long long* dst, unsigned long long v) {
     if ((threadIdx.x & 31u) == 0 && v) atomicAdd(dst, v);
 }
 
-// ---- GJK stage (ncg_gjk.cu) -------------------------------------------------
-// Validates the pairs, writes the outputs of bad ones and counting-sorts the
-// rest into s.sorted (k_classify, k_bucket): two launches over n pairs.
-void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, cudaStream_t st);
-// One thread per pair over list 0 (analytic pairs) or 1 (the ConvexHull
-// pairs after the first `warp_buckets` hull buckets); EPA work items go to
-// thread-stage queue `epa_queue`.
-void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                       int list, int warp_buckets, int epa_queue, cudaStream_t st);
-// One warp per pair over the ConvexHull pairs of the first `warp_buckets`
-// hull buckets (the largest hulls); with stage_min > 0, pairs whose hulls hold
-// at least stage_min points are staged in shared memory (stage_cap points
-// per warp) by bulk copies.
-void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                     int warp_buckets, uint32_t stage_min, uint32_t stage_cap, cudaStream_t st);
-// Dynamic shared memory of a staged warp-GJK block (4 warps of stage_cap points).
-size_t gjk_warp_stage_bytes(uint32_t stage_cap);
-// Allows the staged kernel that much shared memory and returns its resident
-// blocks per SM (0 if it cannot run).
-int gjk_warp_stage_occupancy(uint32_t stage_cap);
-// Resident 128-thread blocks per SM of the thread and warp GJK kernels.
-void gjk_occupancy(int* occ_thread, int* occ_warp);
-// Shared-memory carveout preference of the thread GJK kernel.
-cudaError_t gjk_set_carveout(int pct);
+// ---- EPA store capacities ------------------------------------------------------
+// EPA store capacities: vertices, live face slots (about twice the vertices),
+// silhouette edges, flood-fill stack.  Store 0 is the per-thread store, 1-4
+// the warp stores (shared memory or one global slab per block).
+template <int T> struct EpaTier;
+// Compile-time tuning: the thread stage's capacity and its minimum resident
+// blocks per SM (which caps its registers).
+#ifndef NCG_EPA_THREAD_VC
+#define NCG_EPA_THREAD_VC 64
+#endif
+#ifndef NCG_EPA_THREAD_MIN_BLOCKS
+#define NCG_EPA_THREAD_MIN_BLOCKS 4
+#endif
+template <> struct EpaTier<0> {
+    static constexpr int VC = NCG_EPA_THREAD_VC, FC = 2 * VC + 16, SC = VC < 64 ? 32 : VC / 2, TC = 2 * VC, HC = FC;
+};
+// 1: shared-memory warp store (the no-allocation path); 2: the warp stage's
+// global slabs; 3: the wide stage (one global slab per SM).
+template <> struct EpaTier<1> { static constexpr int VC = 128, FC = 2 * 128 + 64, SC = 64, TC = 256, HC = FC; };
+template <> struct EpaTier<2> { static constexpr int VC = 1280, FC = 2 * 1280 + 64, SC = 512, TC = 2048, HC = FC; };
+// The wide stage's heap holds 64Ki entries: the f32 build keeps every deleted
+// face's entry, as Rust's heap does (a 10 000-step run creates ~50 000 faces).
+template <> struct EpaTier<3> {
+    static constexpr int VC = 10240, FC = 2 * 10240 + 64, SC = 4096, TC = 16384, HC = 65536;
+};
+static_assert(EpaTier<0>::HC == EpaTier<0>::FC, "spill records lay the heap out with FC entries");
+static_assert(EpaTier<3>::FC < 65536 && EpaTier<3>::VC < 65536, "16-bit face and vertex indices");
+// Warps per SM of the warp stage (registers allow 12 at 168 per thread).
+#ifndef NCG_WARP_STAGE_PER_SM
+#define NCG_WARP_STAGE_PER_SM 12
+#endif
+constexpr int WARP_STAGE_MAX_PER_SM = NCG_WARP_STAGE_PER_SM;
+template <int T> constexpr size_t tier_bytes() {
+    return EpaStore::bytes(EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC, EpaTier<T>::HC);
+}
+
+
+// A warp EPA stage's queues and store: it drains queue q_in, then q_in2 (when
+// >= 0); a pair whose polytope outgrows the store is queued on q_out and
+// continues there, or, when q_out < 0, ends with NCG_STATUS_EPA_CAPACITY.
+struct TierCaps {
+    int q_in, q_in2, q_out;
+    int slab;  // -1: shared memory; else index into Scratch::slabs
+    int VC, FC, SC, TC, HC;
+};
+template <int T> TierCaps caps(int q_in, int q_in2, int q_out, int slab) {
+    return TierCaps{q_in, q_in2, q_out, slab, EpaTier<T>::VC, EpaTier<T>::FC, EpaTier<T>::SC, EpaTier<T>::TC,
+                    EpaTier<T>::HC};
+}
+// Bytes of a thread-stage spill record (the thread store's polytope).
+constexpr size_t SPILL_BYTES = (EpaSpill::bytes(EpaTier<0>::VC, EpaTier<0>::FC) + 255) & ~size_t(255);
+
+// ---- the stage launchers ------------------------------------------------------
+// The GJK stage (ncg_gjk.cu) and the EPA stages (ncg_epa_stages.cu) are each
+// built twice: in namespace dwa with the double-word sub-solve (the default
+// arithmetic) and in namespace f32a with the reference's f32 path throughout
+// (NCG_ARITH_F32).  Both builds share these declarations.
+#define NCG_STAGE_API                                                                                              \
+    /* Validates the pairs, writes the outputs of bad ones and counting-sorts */                                  \
+    /* the rest into s.sorted (k_classify, k_bucket): two launches over n pairs. */                               \
+    void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,           \
+                         cudaStream_t st);                                                                         \
+    /* One thread per pair over list 0 (analytic pairs) or 1 (the ConvexHull pairs */                             \
+    /* after the first `warp_buckets` hull buckets); EPA work items go to */                                      \
+    /* thread-stage queue `epa_queue`. */                                                                          \
+    void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o,                 \
+                           const Scratch& s, int list, int warp_buckets, int epa_queue, cudaStream_t st);         \
+    /* One warp per pair over the ConvexHull pairs of the first `warp_buckets` */                                 \
+    /* hull buckets (the largest hulls); with stage_min > 0, pairs whose hulls */                                 \
+    /* hold at least stage_min points are staged in shared memory (stage_cap */                                   \
+    /* points per warp) by bulk copies. */                                                                         \
+    void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, \
+                         int warp_buckets, uint32_t stage_min, uint32_t stage_cap, cudaStream_t st);               \
+    /* Dynamic shared memory of a staged warp-GJK block (4 warps of stage_cap points). */                        \
+    size_t gjk_warp_stage_bytes(uint32_t stage_cap);                                                               \
+    /* Allows the staged kernel that much shared memory and returns its resident */                              \
+    /* blocks per SM (0 if it cannot run). */                                                                      \
+    int gjk_warp_stage_occupancy(uint32_t stage_cap);                                                              \
+    /* Resident 128-thread blocks per SM of the thread and warp GJK kernels. */                                  \
+    void gjk_occupancy(int* occ_thread, int* occ_warp);                                                            \
+    /* Shared-memory carveout preference of the thread GJK kernel. */                                            \
+    cudaError_t gjk_set_carveout(int pct);                                                                         \
+    /* The thread EPA stage over queue q (one thread per pair, 128-thread blocks). */                            \
+    void epa_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o,                 \
+                           const Scratch& s, int q, cudaStream_t st);                                              \
+    /* A warp EPA stage (one warp per block); smem > 0 holds the store in */                                     \
+    /* dynamic shared memory (tc.slab < 0). */                                                                     \
+    void epa_launch_warp(int grid, size_t smem, const ncg_batch& b, const QueryParams& qp, const Outputs& o,      \
+                         const Scratch& s, TierCaps tc, cudaStream_t st);                                          \
+    /* Resident blocks per SM of the EPA kernels: the thread stage, a warp stage */                              \
+    /* on global slabs, and with the stores of EpaTier<1> / <2> in shared memory */                              \
+    /* (allows the warp kernel that much shared memory). */                                                        \
+    void epa_occupancy(int* occ_thread, int* occ_global, int occ_smem[2]);                                         \
+    /* Shared-memory carveout preference of the thread EPA kernel. */                                            \
+    cudaError_t epa_set_carveout(int pct);
+
+namespace dwa {
+NCG_STAGE_API
+}  // namespace dwa
+namespace f32a {
+NCG_STAGE_API
+}  // namespace f32a
 
 }  // namespace ncg

@@ -35,7 +35,8 @@ TUNING_KEYS = {"hull_gjk_warp": N.TUNE_HULL_GJK_WARP, "gjk_blocks": N.TUNE_GJK_B
 class Context:
     """Owns an ncg_ctx: scratch memory, EPA slabs and settings for one device."""
 
-    def __init__(self, device=0, tolerance=N.TOL_REFERENCE, warm_start=N.WARM_NONE, dispatch=N.DISPATCH_SUPPORT_MAP):
+    def __init__(self, device=0, tolerance=N.TOL_REFERENCE, warm_start=N.WARM_NONE, dispatch=N.DISPATCH_SUPPORT_MAP,
+                 arithmetic=N.ARITH_SPLIT):
         self._L = N.load()
         self._p = ctypes.c_void_p()
         if isinstance(device, torch.device):
@@ -45,6 +46,7 @@ class Context:
         self.set_tolerance(tolerance)
         self.set_warm_start(warm_start)
         self.set_dispatch(dispatch)
+        self.set_arithmetic(arithmetic)
 
     @property
     def handle(self):
@@ -55,6 +57,14 @@ class Context:
             mode = {"reference": N.TOL_REFERENCE, "precise": N.TOL_PRECISE}[mode]
         N.check(self._L.ncg_ctx_set_tolerance(self._p, int(mode)), "ncg_ctx_set_tolerance")
         self.tolerance = int(mode)
+
+    def set_arithmetic(self, mode):
+        """NCG_ARITH_SPLIT (f32 supports, double-word sub-solve; the default) or
+        NCG_ARITH_F32 (the reference's f32 path bit for bit)."""
+        if isinstance(mode, str):
+            mode = {"split": N.ARITH_SPLIT, "f32": N.ARITH_F32}[mode]
+        N.check(self._L.ncg_ctx_set_arithmetic(self._p, int(mode)), "ncg_ctx_set_arithmetic")
+        self.arithmetic = int(mode)
 
     def set_dispatch(self, mode):
         """NCG_DISPATCH_SUPPORT_MAP (every pair by GJK/EPA) or NCG_DISPATCH_QUERY

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared_functions():
         assert hasattr(L, name), name
     assert set(declared_functions()) <= set(N.EXPORTED) | {"ncg_last_error"}
-    assert L.ncg_abi_version() == 2
+    assert L.ncg_abi_version() == 3
 
 
 def test_struct_layouts_match_header():

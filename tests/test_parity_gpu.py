@@ -21,10 +21,10 @@ pytestmark = pytest.mark.gpu
 DBL_EPS = float(np.finfo(np.float64).eps)
 
 
-def oracle_mixed(batch, query, param, tol):
+def oracle_mixed(batch, query, param, tol, policy=O.MIXED):
     # eps < 0 selects the oracle's PRECISE tolerance set (the kernels' NCG_TOL_PRECISE)
     eps, epa_tol = (0.0, 0.0) if tol == N.TOL_REFERENCE else (-1.0, 1e-6)
-    return O.query(batch, query, O.MIXED, param=float(np.float32(param)), eps=eps, epa_tol=epa_tol)
+    return O.query(batch, query, policy, param=float(np.float32(param)), eps=eps, epa_tol=epa_tol)
 
 
 def run_gpu(ctx, batch, query, param):
@@ -66,9 +66,11 @@ def assert_same(name, got, want, batch):
         raise AssertionError("\n".join(lines))
 
 
-def check_query(ctx, batch, query, param, tol):
+def check_query(ctx, batch, query, param, tol, policy=O.MIXED):
+    """The kernels against the oracle instantiation `policy`: MIXED for the
+    default arithmetic, F32 (the reference's f32 path) for NCG_ARITH_F32."""
     g = run_gpu(ctx, batch, query, param)
-    r = oracle_mixed(batch, query, param, tol)
+    r = oracle_mixed(batch, query, param, tol, policy)
     assert_same("status", g["status"].view(np.uint32), r.status, batch)
     it = g["iters"].view(np.uint32)
     assert_same("gjk iterations", it & 0xffff, np.minimum(r.counters[:, 0], 0xffff), batch)
