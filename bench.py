@@ -136,23 +136,28 @@ def oracle_contacts(r):
     return np.concatenate([r.p1, r.p2, r.dir, r.value[:, None]], 1)
 
 
-def mixed_parity(batch, query, param, tolerance, gpu, distance=None):
-    """Bit-exact check of a whole batch's GPU outputs against the oracle's
-    mixed-precision instantiation (the kernels' arithmetic split): the number
-    of pairs whose tag, status or any output float differs (NaN equal to NaN).
+def mixed_parity(batch, query, param, tolerance, gpu, distance=None, policy=None, r=None):
+    """Bit-exact check of a whole batch's GPU outputs against the oracle: the
+    mixed-precision instantiation (the kernels' default arithmetic split) or,
+    with policy F32, the reference's f32 path (NCG_ARITH_F32).  Counts the
+    pairs whose tag, status or any output float differs (NaN equal to NaN).
     gpu: contact outputs (has_contact, contact n x 10, dir, status); distance:
-    distance outputs (distance, status)."""
+    distance outputs (distance, status); r: the oracle's result when already
+    computed."""
     from oracle import oracle as O
+    policy = O.MIXED if policy is None else policy
     eps, epa_tol = (-1.0, 1e-6) if tolerance == "precise" else (0.0, 0.0)
     t0 = time.perf_counter()
-    r = O.query(batch, query, O.MIXED, param=float(np.float32(param)), eps=eps, epa_tol=epa_tol)
+    if r is None:
+        r = O.query(batch, query, policy, param=float(np.float32(param)), eps=eps, epa_tol=epa_tol)
 
     def differ(a, b):
         a, b = np.asarray(a), np.asarray(b)
         bad = (a != b) & ~(np.isnan(a) & np.isnan(b)) if np.issubdtype(a.dtype, np.floating) else a != b
         return bad.reshape(len(a), -1).any(1)
-    out = {"pairs": int(batch.n_pairs), "oracle": "MIXED (f32 support points, double-word sub-solve)",
-           "tolerance": tolerance}
+    out = {"pairs": int(batch.n_pairs), "tolerance": tolerance,
+           "oracle": "MIXED (f32 support points, double-word sub-solve)" if policy == O.MIXED else
+                     "F32 (the reference's f32 path: f32 sub-solve, Rust heap order)"}
     if distance is None:
         m = r.tag == 1
         want = oracle_contacts(r).astype(np.float32)
@@ -481,6 +486,12 @@ def precision_stress(args, local, tolerance):
     has = gpu_c["has_contact"]
     dist = gpu_d["distance"].astype(np.float64)
     ctx.close()
+    # the reference's f32 path on the GPU (NCG_ARITH_F32, reference tolerances)
+    ctx32 = Q.Context(local, tolerance="reference", dispatch="support_map", arithmetic="f32")
+    o32 = Q.contact_batch(ctx32, db, 0.0)
+    torch.cuda.synchronize()
+    gpu32 = {k: v.cpu().numpy() for k, v in o32.items() if v is not None}
+    ctx32.close()
     r64c = O.query(b, O.CONTACT, O.F64, param=0.0)
     r64d = O.query(b, O.DISTANCE, O.F64)
     r32c = O.query(b, O.CONTACT, O.F32, param=0.0)
@@ -518,6 +529,11 @@ def precision_stress(args, local, tolerance):
                 "f32_reference_vs_f64_mismatches": int(((ref_int != f64_int) & ~band).sum())},
             "parity_vs_oracle_contact": mixed_parity(b, O.CONTACT, 0.0, tolerance, gpu_c),
             "parity_vs_oracle_distance": mixed_parity(b, O.DISTANCE, 0.0, tolerance, None, gpu_d),
+            "f32_arithmetic": {
+                "classification_vs_f32_reference_mismatches_outside_band":
+                    int(((gpu32["has_contact"] == 1) != ref_int)[~band].sum()),
+                "parity_vs_f32_reference_path": mixed_parity(b, O.CONTACT, 0.0, "reference", gpu32, policy=O.F32,
+                                                             r=r32c)},
             "ball_ball_pairs_excluded": int(ballball.sum())}
 
 
@@ -873,6 +889,33 @@ def sharded_report(args, ctx, rank, world, local, batch0, out0):
             "gathered_equals_single_gpu": bool(same)}
 
 
+def f32_arithmetic_report(args, local, db, batch):
+    """The headline workload in the reference's f32 arithmetic (NCG_ARITH_F32,
+    reference tolerances, query dispatch): throughput with inputs resident and
+    every pair bit for bit against the oracle's f32 instantiation."""
+    import torch
+    from ncollide_gb300 import query as Q
+    from oracle import oracle as O
+    ctx = Q.Context(local, tolerance="reference", dispatch=args.dispatch, arithmetic="f32")
+    for _ in range(3):
+        o = Q.contact_batch(ctx, db, 0.0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 5
+    e0.record()
+    for _ in range(n):
+        o = Q.contact_batch(ctx, db, 0.0)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    gpu = {k: v.cpu().numpy() for k, v in o.items() if v is not None}
+    ctx.close()
+    q = O.CONTACT_QUERY if args.dispatch == "query" else O.CONTACT
+    return {"workload": "mixed_convex_1M, contact, reference tolerances", "pairs_per_s": batch.n_pairs / (ms / 1e3),
+            "ms_per_step": ms, "parity_vs_f32_reference_path": mixed_parity(batch, q, 0.0, "reference", gpu,
+                                                                              policy=O.F32)}
+
+
 def cpu_baseline(batch, threads, query):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -1182,8 +1225,9 @@ def main():
         # the last timed step's outputs, every pair, bit for bit
         parity = mixed_parity(batch, qo, 0.0, args.tolerance, out_h)
 
-    stress = cuboids = toi_rep = ray_rep = scene = manifolds = queries = None
+    stress = cuboids = toi_rep = ray_rep = scene = manifolds = queries = arith32 = None
     if not args.no_extras:
+        arith32 = f32_arithmetic_report(args, local, db, batch)
         queries = other_queries_report(args, local, args.tolerance, db, batch)
         scene = scene_pipeline_report(args, local, args.tolerance, args.dispatch)
         manifolds = manifold_report(args, local, args.tolerance)
@@ -1214,7 +1258,7 @@ def main():
             "precision_stress": stress, "cuboid_pairs_65536": cuboids, "time_of_impact": toi_rep, "ray_cast": ray_rep, "scene_pipeline": scene, "manifolds": manifolds, "other_queries": queries,
             "other_dispatch": {"dispatch": other, "value": batch.n_pairs / (other_ms / 1e3), "ms_per_step": other_ms,
                                "stage_ms": other_stage},
-            "sharded_headline_batch": sharded,
+            "sharded_headline_batch": sharded, "f32_arithmetic": arith32,
             "epa": {"pairs": stats["n_epa"], "warp_stage_pairs": stats["n_epa_overflow"],
                     "gjk_iters_per_pair": stats["gjk_iters"] / batch.n_pairs,
                     "epa_iters_per_epa_pair": stats["epa_iters"] / max(1, stats["n_epa"])}}
