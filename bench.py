@@ -406,6 +406,26 @@ def learned_warm_start(args, local, tolerance, dispatch, headline_db, headline_b
                 "epa_iters_mean": float(e.mean()), "flags": ctx.stats()["flags"]}, o
 
     held = {"plain": run(dhe, Nn.WARM_NONE, 3)[0], "mlp": run(dhe, Nn.WARM_MLP, 3)[0]}
+
+    def run_closest(db, warm, steps):
+        # closest points with prediction 0.1: GJK refines to convergence there,
+        # so the start direction changes its iteration count
+        ctx.set_warm_start(warm)
+        for _ in range(2):
+            Q.closest_points_batch(ctx, db, 0.1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            o = Q.closest_points_batch(ctx, db, 0.1, with_iters=True)
+        e1.record()
+        torch.cuda.synchronize()
+        g = (o["iters"].cpu().numpy().view(np.uint32) & 0xffff).astype(np.float64)
+        return {"pairs_per_s": db.n_pairs * steps / (e0.elapsed_time(e1) / 1e3), "ms_per_step": e0.elapsed_time(e1) / steps,
+                "gjk_iters_mean": float(g.mean()), "gjk_iters_p99": float(np.percentile(g, 99))}
+    closest = {"plain": run_closest(dhe, Nn.WARM_NONE, 3), "mlp": run_closest(dhe, Nn.WARM_MLP, 3)}
+    closest["gjk_iteration_reduction"] = 1.0 - closest["mlp"]["gjk_iters_mean"] / closest["plain"]["gjk_iters_mean"]
+    closest["speedup_mlp_vs_plain"] = closest["mlp"]["pairs_per_s"] / closest["plain"]["pairs_per_s"]
     head_plain, op = run(headline_db, Nn.WARM_NONE, args.steps)
     head_mlp, om = run(headline_db, Nn.WARM_MLP, args.steps)
     ctx.set_warm_start(Nn.WARM_NONE)
@@ -429,7 +449,8 @@ def learned_warm_start(args, local, tolerance, dispatch, headline_db, headline_b
                       "optimizer": "Adam lr 2e-3", "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1],
                       "seconds_generate_host": gen_s, "seconds_label_gpu": label_s, "seconds_train_gpu": train_s,
                       "data": "mixed_convex over a pool of 131072 shapes, seed 3 (train) / 4 (held out)"},
-            "held_out": {"pairs": held_b.n_pairs, "loss": held_loss, **held},
+            "held_out": {"pairs": held_b.n_pairs, "loss": held_loss, **held,
+                         "closest_points_prediction_0.1": closest},
             "headline_batch": {"plain": head_plain, "mlp": head_mlp,
                                "speedup_mlp_vs_plain": head_mlp["pairs_per_s"] / head_plain["pairs_per_s"],
                                "accuracy_vs_f64_first_4096": acc}}

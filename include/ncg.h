@@ -313,8 +313,12 @@ int ncg_contact_batch(ncg_ctx* ctx, const ncg_batch* batch, float prediction,
  * W1[128][48], b1[128], W2[128][128], b2[128], W3[4][128], b3[4] (inputs
  * 39..47 are zero padding).  With NCG_WARM_MLP the context runs the network
  * (tcgen05 tensor cores, bf16 operands, f32 accumulation) before GJK and uses
- * its unit direction as init_dir; GJK and EPA still run to their own
- * termination.  Training entry points work on device buffers:
+ * its unit direction as init_dir of every query (contact, distance, proximity,
+ * closest points); GJK and EPA still run to their own termination.  Measured:
+ * contact with prediction 0 stops at the first separating axis and its GJK
+ * iterations hardly change; closest points gain only from the exact final
+ * direction, and an approximate one (the network's) costs a few percent more
+ * iterations than the reference's default start.   Training entry points work on device buffers:
  *   ncg_mlp_features   shape descriptors (desc: 16 floats per shape) and the
  *                      48 input features of every pair (X: 48 floats per pair)
  *   ncg_mlp_infer      the network's world-space unit direction per pair

@@ -313,10 +313,11 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
         cudaEventRecord(c->marks[c->n_marks++], st);
     };
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset counters")) return NCG_ECUDA;
-    if (c->warm == NCG_WARM_MLP && (query == Q_CONTACT || query == Q_PROXIMITY)) {
+    if (c->warm == NCG_WARM_MLP) {
         // the network's start direction replaces the default one (contact and
-        // proximity start from normalize(t2 - t1) in the reference); the
-        // shape descriptors read hull points
+        // proximity start from normalize(t2 - t1) in the reference, distance
+        // and closest points from t1 - t2; the *_with_params wrappers take it
+        // as init_dir); the shape descriptors read hull points
         if (hull_ready && !cuda_ok(cudaStreamWaitEvent(st, hull_ready, 0), "cudaStreamWaitEvent")) return NCG_ECUDA;
         int rc = ensure_mlp_buffers(c, b);
         if (rc != NCG_OK) return rc;
