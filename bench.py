@@ -825,7 +825,69 @@ def manifold_report(args, local, tolerance):
             "contacts_per_pair": float(man["n"].mean()),
             "manifold_size_histogram": np.bincount(man["n"], minlength=9)[:9].tolist(),
             "cpu_reference_path_pairs_per_s": sample / cpu_s, "cpu_cores": threads,
-            "cpu_sample": f"first {sample} pairs, f32 reference path (oracle contact and manifold step)"}
+            "cpu_sample": f"first {sample} pairs, f32 reference path (oracle contact and manifold step)",
+            "convex_hull_pairs": hull_manifold_report(args, local, tolerance)}
+
+
+def hull_manifold_report(args, local, tolerance):
+    """Contact manifolds of ConvexHull and Cuboid pairs (hull_pairs_pooled:
+    2^18 pairs over 4,096 shared shapes of 8..256 points, prediction 0.1,
+    angular tolerances 0.05) with the hulls' face topology: the topology build
+    (host, once per shape), the GPU call with inputs resident, the manifold
+    step bit for bit against the oracle on the GPU's contacts, and the f32
+    reference path on a 65,536-pair sample with every host core."""
+    import torch
+    from ncollide_gb300 import hulls as H
+    from ncollide_gb300 import query as Q
+    from ncollide_gb300 import workloads as W
+    from oracle import oracle as O
+    n = 1 << 18
+    b = W.hull_pairs_pooled(n, seed=17, pool=4096)
+    t0 = time.perf_counter()
+    topo = H.HostTopology(b)
+    build_s = time.perf_counter() - t0
+    dt = topo.to_device(f"cuda:{local}")
+    db = Q.DeviceBatch.from_host(b, device=f"cuda:{local}")
+    ctx = Q.Context(local, tolerance=tolerance)
+    for _ in range(3):
+        o = Q.manifold_batch(ctx, db, 0.1, 0.05, 0.05, topology=dt)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        o = Q.manifold_batch(ctx, db, 0.1, 0.05, 0.05, topology=dt)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    man = o["manifold"].cpu().numpy().view(O.MANIFOLD_DTYPE).reshape(-1)
+    has = o["has_contact"].cpu().numpy()
+    c9 = o["contact"].cpu().numpy()[:, :9].copy()
+    st = o["status"].cpu().numpy().view(np.uint32)
+    ctx.close()
+    want, wst = O.manifold(b, c9, has, linear=0.1, angular1=0.05, angular2=0.05, topology=topo)
+    same = np.array_equal(man["n"], want["n"]) and np.array_equal(st & 0x600, wst)
+    for k in range(O.MANIFOLD_MAX):
+        m = man["n"] > k
+        for f in ("world1", "world2", "depth", "feature1", "feature2"):
+            same = same and np.array_equal(man["points"][f][m, k], want["points"][f][m, k])
+    sample = min(65536, n)
+    sb = b.subset(np.arange(sample))
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    r = O.query(sb, O.CONTACT, O.F32, param=0.1, threads=threads)
+    r9 = np.concatenate([r.p1, r.p2, r.dir], 1).astype(np.float32)
+    O.manifold(sb, r9, r.tag, linear=0.1, angular1=0.05, angular2=0.05, threads=threads, topology=topo)
+    cpu_s = time.perf_counter() - t0
+    k = b.shapes["kind"]
+    return {"workload": f"hull_pairs_pooled {n} pairs over 4096 shapes (Cuboid, ConvexHull of 8..256 points), seed 17, "
+                        "prediction 0.1, angular 0.05",
+            "topology_build_s": build_s, "hulls_without_topology": topo.n_failed,
+            "hulls": int((k == W.CONVEX_HULL).sum()),
+            "pairs_per_s": n / (ms / 1e3), "ms_per_step": ms, "contacts_per_pair": float(man["n"][has == 1].mean()),
+            "not_polyhedra_pairs": int(((st & 0x200) != 0).sum()), "manifold_full_pairs": int(((st & 0x400) != 0).sum()),
+            "manifold_bit_exact_vs_oracle": bool(same),
+            "cpu_reference_path_pairs_per_s": sample / cpu_s, "cpu_cores": threads}
 
 
 def other_queries_report(args, local, tolerance, db, batch):

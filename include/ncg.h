@@ -111,6 +111,9 @@ enum ncg_closest_points { NCG_CP_INTERSECTING = 0, NCG_CP_WITHIN_MARGIN = 1, NCG
 #define NCG_STATUS_BAD_INPUT     (1u << 6) /* shape index out of range, bad hull slice */
 #define NCG_STATUS_UNSUPPORTED_FEATURE (1u << 7) /* query dispatch: ball centre on a ConvexHull's
                                                     surface needs the hull's face topology */
+#define NCG_STATUS_MANIFOLD_FULL (1u << 10) /* manifold: clipping produced more than
+                                                    NCG_MANIFOLD_MAX contacts; the first
+                                                    NCG_MANIFOLD_MAX are kept */
 #define NCG_STATUS_NOT_POLYHEDRA (1u << 9) /* manifold: not a Cuboid pair; the manifold is the
                                               single GJK/EPA contact with unknown features  */
 #define NCG_STATUS_EPA_PRECISION_LIMIT (1u << 8) /* NCG_TOL_PRECISE: EPA's expansion would have
@@ -420,6 +423,50 @@ int ncg_ray_cast_batch(ncg_ctx* ctx, const ncg_batch* batch, const float* rays, 
 int ncg_manifold_batch(ncg_ctx* ctx, const ncg_batch* batch, float prediction, float angular1,
                        float angular2, ncg_contact* contact, uint8_t* has_contact, float* out_dir,
                        ncg_manifold* out, uint32_t* status, void* stream);
+
+/* ---- ConvexHull face topology ----------------------------------------------
+ * The polyhedral structure of every ConvexHull shape of a shape table, as
+ * ConvexHull::try_new (src/shape/convex.rs:88-328) builds it from the hull's
+ * points and the triangles of their convex hull: polygonal faces (triangles
+ * whose normals differ by less than sqrt(f32::EPSILON) merged), edges with
+ * their unit directions, and the faces and edges around each vertex.  Ids are
+ * local to the hull (point i of a hull is vertex i: the points are not
+ * reordered; this is try_new on the hull's own points, not try_from_points,
+ * whose hull step renormalises and reorders them).  ncg_hull_topology_build
+ * fills `out` with host arrays it allocates (free them with
+ * ncg_hull_topology_release); n_failed counts hulls left without a topology
+ * (degenerate points, or a check of try_new failed).  For
+ * ncg_manifold_batch_hulls, copy the arrays to the device and pass a struct of
+ * device pointers with the same counts.  Shape set-up, not part of a query. */
+typedef struct ncg_hull_topology {
+    uint64_t n_shapes, n_hull_points, n_faces, n_face_slots, n_edges, n_vertex_slots;
+    const uint32_t* shape;         /* [n_shapes][4]: first face, face count, first edge, edge count */
+    const float* face_normal;      /* [n_faces][4]: unit outward normal, 0 */
+    const uint32_t* face_range;    /* [n_faces][2]: first slot in face_vertex / face_edge, count */
+    const uint32_t* face_vertex;   /* [n_face_slots]: hull-local point id, counter-clockwise */
+    const uint32_t* face_edge;     /* [n_face_slots]: hull-local id of the edge to the next vertex */
+    const uint32_t* edge_vertex;   /* [n_edges][2]: hull-local point ids */
+    const float* edge_dir;         /* [n_edges][4]: unit direction, 0 */
+    const uint32_t* vertex_range;  /* [n_hull_points][2]: first slot in vertex_face / vertex_edge, count */
+    const uint32_t* vertex_face;   /* [n_vertex_slots]: hull-local face id */
+    const uint32_t* vertex_edge;   /* [n_vertex_slots]: hull-local edge id */
+} ncg_hull_topology;
+int ncg_hull_topology_build(const ncg_shape* shapes, uint32_t n_shapes, const float* hull_points,
+                            uint64_t n_hull_points, ncg_hull_topology* out, uint32_t* n_failed);
+int ncg_hull_topology_release(ncg_hull_topology* topology);
+/* ncg_manifold_batch with ConvexHull shapes as polyhedra (ConvexHull's
+ * ConvexPolyhedron impl, convex.rs:425-546: support_face_toward takes the face
+ * whose normal has the largest dot product with the direction,
+ * support_feature_toward the support point's adjacent face or edge within the
+ * angular tolerance, else the vertex) for every pair of Cuboid and ConvexHull
+ * shapes; `topology` holds device pointers (NULL: as ncg_manifold_batch).  A
+ * ConvexHull face of more than NCG_POLY_MAX vertices, or a hull without a
+ * topology, gives the pair its single contact with NCG_STATUS_NOT_POLYHEDRA. */
+#define NCG_POLY_MAX 32
+int ncg_manifold_batch_hulls(ncg_ctx* ctx, const ncg_batch* batch, const ncg_hull_topology* topology,
+                             float prediction, float angular1, float angular2, ncg_contact* contact,
+                             uint8_t* has_contact, float* out_dir, ncg_manifold* out, uint32_t* status,
+                             void* stream);
 
 /* ---- bounding volumes and the broad phase ----------------------------------
  * ncg_aabb_batch: HasBoundingVolume<AABB>::bounding_volume of shapes[g1[i]] at

@@ -38,7 +38,8 @@ EXPORTED = [
     "ncg_mlp_grad", "ncg_mlp_adam", "ncg_time_of_impact_batch",
     "ncg_ray_cast_batch", "ncg_aabb_batch", "ncg_bp_create", "ncg_bp_update", "ncg_bp_results",
     "ncg_bp_destroy", "ncg_bp_copy", "ncg_gather_pairs", "ncg_manifold_batch", "ncg_autotune",
-    "ncg_ctx_get_tuning", "ncg_ctx_set_arithmetic",
+    "ncg_ctx_get_tuning", "ncg_ctx_set_arithmetic", "ncg_hull_topology_build", "ncg_hull_topology_release",
+    "ncg_manifold_batch_hulls",
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
 TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT, TUNE_HULL_STAGE_MIN, TUNE_HULL_STAGE_CAP = range(6)
@@ -49,6 +50,8 @@ TOI_OUT_OF_ITERATIONS, TOI_CONVERGED, TOI_FAILED, TOI_PENETRATING = range(4)
 STATUS_UNSUPPORTED_FEATURE = 1 << 7
 STATUS_EPA_PRECISION_LIMIT = 1 << 8
 STATUS_NOT_POLYHEDRA = 1 << 9
+STATUS_MANIFOLD_FULL = 1 << 10
+POLY_MAX = 32
 MANIFOLD_MAX = 16
 NOALLOC_MAX_PAIRS = 32768
 NOALLOC_SCRATCH_BYTES = 7827200
@@ -60,6 +63,15 @@ class NcgBatch(ctypes.Structure):
                 ("pad0", ctypes.c_uint32), ("n_hull_points", ctypes.c_uint64), ("m1", ctypes.c_void_p),
                 ("g1", ctypes.c_void_p), ("m2", ctypes.c_void_p), ("g2", ctypes.c_void_p),
                 ("n_pairs", ctypes.c_uint64), ("init_dir", ctypes.c_void_p)]
+
+
+class NcgHullTopology(ctypes.Structure):
+    _fields_ = [("n_shapes", ctypes.c_uint64), ("n_hull_points", ctypes.c_uint64), ("n_faces", ctypes.c_uint64),
+                ("n_face_slots", ctypes.c_uint64), ("n_edges", ctypes.c_uint64), ("n_vertex_slots", ctypes.c_uint64),
+                ("shape", ctypes.c_void_p), ("face_normal", ctypes.c_void_p), ("face_range", ctypes.c_void_p),
+                ("face_vertex", ctypes.c_void_p), ("face_edge", ctypes.c_void_p), ("edge_vertex", ctypes.c_void_p),
+                ("edge_dir", ctypes.c_void_p), ("vertex_range", ctypes.c_void_p), ("vertex_face", ctypes.c_void_p),
+                ("vertex_edge", ctypes.c_void_p)]
 
 
 class NcgStats(ctypes.Structure):
@@ -124,6 +136,11 @@ def load(build_if_missing=True):
     L.ncg_bp_copy.argtypes = [vp, vp, vp, vp, vp]
     L.ncg_gather_pairs.argtypes = [vp, vp, vp, vp, ctypes.c_uint64, vp, vp, vp, vp, vp]
     L.ncg_manifold_batch.argtypes = [vp, P(NcgBatch), f32, f32, f32, vp, vp, vp, vp, vp, vp]
+    L.ncg_manifold_batch_hulls.argtypes = [vp, P(NcgBatch), P(NcgHullTopology), f32, f32, f32, vp, vp, vp, vp, vp,
+                                           vp]
+    L.ncg_hull_topology_build.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_uint64, P(NcgHullTopology),
+                                          P(ctypes.c_uint32)]
+    L.ncg_hull_topology_release.argtypes = [P(NcgHullTopology)]
     L.ncg_contact_graph_create.argtypes = [vp, P(NcgBatch), f32, vp, vp, vp, vp, vp, P(vp)]
     L.ncg_graph_launch.argtypes = [vp, vp]
     L.ncg_graph_destroy.argtypes = [vp]

@@ -18,11 +18,11 @@ LIB_DIR = os.path.join(HERE, "_lib")
 # with NCG_DEFINES, e.g. "-DNCG_EPA_THREAD_VC=64"); the default is the in-tree build.
 LIB_PATH = os.environ.get("NCG_LIB") or os.path.join(LIB_DIR, "libncg.so")
 SOURCES = ["ncg_kernels.cu", "ncg_gjk.cu", "ncg_epa_stages.cu", "ncg_gjk_f32.cu", "ncg_epa_stages_f32.cu",
-           "ncg_mlp.cu", "ncg_toi.cu", "ncg_bp.cu", "ncg_manifold.cu"]
+           "ncg_mlp.cu", "ncg_toi.cu", "ncg_bp.cu", "ncg_manifold.cu", "ncg_hull.cpp"]
 HEADERS = ["ncg_core.cuh", "ncg_epa.cuh", "ncg_dw.cuh", "ncg_query.cuh", "ncg_tc.cuh", "ncg_mlp.h", "ncg_toi.cuh", "ncg_toi.h", "ncg_sort.cuh", "ncg_pipeline.cuh", "ncg_bp.h", "ncg_manifold.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
-              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-shared"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-shared"]
 
 
 def nvcc():

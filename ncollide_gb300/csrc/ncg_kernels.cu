@@ -740,6 +740,13 @@ int ncg_ray_cast_batch(ncg_ctx* c, const ncg_batch* b, const float* rays, float 
 int ncg_manifold_batch(ncg_ctx* c, const ncg_batch* b, float prediction, float angular1, float angular2,
                        ncg_contact* contact, uint8_t* has_contact, float* out_dir, ncg_manifold* out, uint32_t* status,
                        void* stream) {
+    return ncg_manifold_batch_hulls(c, b, nullptr, prediction, angular1, angular2, contact, has_contact, out_dir, out,
+                                    status, stream);
+}
+
+int ncg_manifold_batch_hulls(ncg_ctx* c, const ncg_batch* b, const ncg_hull_topology* topology, float prediction,
+                             float angular1, float angular2, ncg_contact* contact, uint8_t* has_contact,
+                             float* out_dir, ncg_manifold* out, uint32_t* status, void* stream) {
     if (!(prediction >= 0.0f) || !(angular1 >= 0.0f) || !(angular2 >= 0.0f)) {
         g_last_error = "the contact prediction must be >= 0";
         return NCG_EINVAL;
@@ -757,7 +764,18 @@ int ncg_manifold_batch(ncg_ctx* c, const ncg_batch* b, float prediction, float a
     if (rc != NCG_OK) return rc;
     const ncg::ManifoldParams mp{prediction, std::cos(angular1), std::sin(angular1), std::cos(angular2),
                                  std::sin(angular2)};
-    rc = ncg::manifold_launch(*b, contact, has_contact, mp, out, status, c->num_sms, st);
+    ncg::HullTopo topo{};
+    if (topology) {
+        if (topology->n_shapes < b->n_shapes || topology->n_hull_points < b->n_hull_points || !topology->shape) {
+            g_last_error = "ncg_manifold_batch_hulls: the topology covers fewer shapes or hull points than the batch";
+            return NCG_EINVAL;
+        }
+        topo = ncg::HullTopo{topology->shape,       topology->face_normal, topology->face_range,
+                             topology->face_vertex, topology->face_edge,   topology->edge_vertex,
+                             topology->edge_dir,    topology->vertex_range, topology->vertex_face,
+                             topology->vertex_edge};
+    }
+    rc = ncg::manifold_launch(*b, contact, has_contact, mp, topo, out, status, c->num_sms, st);
     if (rc == NCG_OK) c->launches += 1;
     return rc;
 }

@@ -1,11 +1,13 @@
 // ncg_manifold.cu — the contact-manifold step of
 // ConvexPolyhedronConvexPolyhedronManifoldGenerator::generate_contacts
-// (convex_polyhedron_convex_polyhedron_manifold_generator.rs:84-176) for Cuboid
-// pairs, one thread per pair, in f32 as the reference computes it: from the
-// GJK/EPA contact, the support faces (penetrating) or the support features
-// within the angular tolerances (separated) of both cuboids (cuboid.rs:148-405),
-// their polygonal clipping (convex_polygonal_feature3.rs:217-339) and the
-// feature checks of add_contact_to_manifold (:341-400).
+// (convex_polyhedron_convex_polyhedron_manifold_generator.rs:84-176) for pairs
+// of Cuboid and ConvexHull shapes, one thread per pair, in f32 as the
+// reference computes it: from the GJK/EPA contact, the support faces
+// (penetrating) or the support features within the angular tolerances
+// (separated) of both shapes (cuboid.rs:148-405; for a ConvexHull convex.rs:
+// 383-546 over its face topology, built by ncg_hull.cpp), their polygonal
+// clipping (convex_polygonal_feature3.rs:217-339) and the feature checks of
+// add_contact_to_manifold (:341-400).
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -21,11 +23,12 @@ namespace {
 
 NCG_DEV uint32_t feat(uint32_t kind, uint32_t id) { return (kind << 28) | id; }
 
+// A ConvexPolygonalFeature of at most NCG_POLY_MAX vertices.
 struct Poly {
     int nv, ne, nn;
-    vec3<float> v[4];
-    uint32_t vid[4], eid[4];
-    vec3<float> en[4];
+    vec3<float> v[NCG_POLY_MAX];
+    uint32_t vid[NCG_POLY_MAX], eid[NCG_POLY_MAX];
+    vec3<float> en[NCG_POLY_MAX];
     bool has_normal;
     vec3<float> normal;
     uint32_t feature;
@@ -96,6 +99,18 @@ NCG_DEV void cuboid_face(vec3<float> h, uint32_t i, Poly& out) {
     }
 }
 
+// recompute_edge_normals (convex_polygonal_feature3.rs:162-176).
+NCG_DEV void edge_normals(Poly& out) {
+    out.nn = 0;
+    for (int a = 0; a < out.nv; ++a) {
+        const int b = (a + 1) % out.nv;
+        const vec3<float> sn = cross(out.v[b] - out.v[a], out.normal);
+        vec3<float> u;
+        float n;
+        out.en[out.nn++] = try_normalize(sn, FLT_EPSILON, u, n) ? u : zero3<float>();
+    }
+}
+
 NCG_DEV void transform_by(Poly& f, const Pose& m) {
     for (int k = 0; k < f.nv; ++k) f.v[k] = xform(m, f.v[k]);
     for (int k = 0; k < f.nn; ++k) f.en[k] = qrot(m.q, f.en[k]);
@@ -151,6 +166,93 @@ NCG_DEV void support_feature_toward(const Pose& m, vec3<float> h, vec3<float> di
     }
     out.push(xform(m, sp), feat(NCG_FEATURE_VERTEX, spid));
     out.feature = feat(NCG_FEATURE_VERTEX, spid);
+}
+
+// ---- ConvexHull as a polyhedron (convex.rs:383-546) over its topology
+NCG_DEV vec3<float> f3(float4 a) { return {a.x, a.y, a.z}; }
+NCG_DEV vec3<float> hull_point(const ncg_batch& b, const Shape& s, uint32_t i) {
+    return f3(__ldg(reinterpret_cast<const float4*>(b.hull_points) + s.off + i));
+}
+NCG_DEV vec3<float> hull_face_normal(const HullTopo& t, uint32_t f) {
+    return f3(__ldg(reinterpret_cast<const float4*>(t.face_normal) + f));
+}
+
+// ConvexHull::face (convex.rs:453-470) in the local frame; false when the face
+// has more vertices than a Poly holds.
+NCG_DEV bool hull_face(const ncg_batch& b, const HullTopo& t, const Shape& s, uint32_t sid, uint32_t face, Poly& out) {
+    out.clear();
+    const uint32_t f = t.shape[4 * sid] + face;
+    const uint32_t first = t.face_range[2 * f], count = t.face_range[2 * f + 1];
+    if (count > NCG_POLY_MAX) return false;
+    for (uint32_t i = first; i < first + count; ++i) {
+        const uint32_t vid = t.face_vertex[i];
+        out.push(hull_point(b, s, vid), feat(NCG_FEATURE_VERTEX, vid));
+        out.eid[out.ne++] = feat(NCG_FEATURE_EDGE, t.face_edge[i]);
+    }
+    out.normal = hull_face_normal(t, f);
+    out.has_normal = true;
+    out.feature = feat(NCG_FEATURE_FACE, face);
+    edge_normals(out);
+    return true;
+}
+
+// ConvexHull::support_face_toward (convex.rs:502-523): the face whose normal
+// has the largest dot product with the direction (the first on ties).
+NCG_DEV bool hull_support_face_toward(const ncg_batch& b, const HullTopo& t, const Shape& s, uint32_t sid,
+                                      const Pose& m, vec3<float> dir, Poly& out) {
+    const vec3<float> l = qrot_inv(m.q, dir);
+    const uint32_t f0 = t.shape[4 * sid], nf = t.shape[4 * sid + 1];
+    uint32_t best = 0;
+    float max_dot = dot(hull_face_normal(t, f0), l);
+    for (uint32_t i = 1; i < nf; ++i) {
+        const float d = dot(hull_face_normal(t, f0 + i), l);
+        if (d > max_dot) {
+            max_dot = d;
+            best = i;
+        }
+    }
+    if (!hull_face(b, t, s, sid, best, out)) return false;
+    transform_by(out, m);
+    return true;
+}
+
+// ConvexHull::support_feature_toward (convex.rs:525-546) with
+// support_feature_id_toward_eps (:383-416): the support point's first
+// adjacent face whose normal is within the angle of the direction, else its
+// first adjacent edge within the angle of orthogonal to it, else the vertex.
+NCG_DEV bool hull_support_feature_toward(const ncg_batch& b, const HullTopo& t, const Shape& s, uint32_t sid,
+                                         const Pose& m, vec3<float> dir, float cang, float sang, Poly& out) {
+    out.clear();
+    const vec3<float> l = qrot_inv(m.q, dir);
+    const uint32_t sp = ThreadScan{reinterpret_cast<const float4*>(b.hull_points)}.argmax(s, l);
+    const uint32_t f0 = t.shape[4 * sid], e0 = t.shape[4 * sid + 2];
+    const size_t vr = 2 * ((size_t)s.off + sp);
+    const uint32_t first = t.vertex_range[vr], count = t.vertex_range[vr + 1];
+    for (uint32_t i = first; i < first + count; ++i) {
+        const uint32_t face = t.vertex_face[i];
+        if (dot(hull_face_normal(t, f0 + face), l) >= cang) {
+            if (!hull_face(b, t, s, sid, face, out)) return false;
+            transform_by(out, m);
+            return true;
+        }
+    }
+    for (uint32_t i = first; i < first + count; ++i) {
+        const uint32_t edge = t.vertex_edge[i];
+        const vec3<float> ed = f3(__ldg(reinterpret_cast<const float4*>(t.edge_dir) + e0 + edge));
+        if (fabsf(dot(ed, l)) <= sang) {
+            const uint32_t v1 = t.edge_vertex[2 * (e0 + edge)], v2 = t.edge_vertex[2 * (e0 + edge) + 1];
+            out.push(hull_point(b, s, v1), feat(NCG_FEATURE_VERTEX, v1));
+            out.push(hull_point(b, s, v2), feat(NCG_FEATURE_VERTEX, v2));
+            out.feature = feat(NCG_FEATURE_EDGE, edge);
+            out.eid[out.ne++] = out.feature;
+            transform_by(out, m);
+            return true;
+        }
+    }
+    out.push(hull_point(b, s, sp), feat(NCG_FEATURE_VERTEX, sp));
+    out.feature = feat(NCG_FEATURE_VERTEX, sp);
+    transform_by(out, m);
+    return true;
 }
 
 struct P2 {
@@ -231,8 +333,10 @@ NCG_DEV bool line_toi_with_plane(vec3<float> c, vec3<float> n, vec3<float> o, ve
 struct Out {
     ncg_manifold_point* pts;
     int n;
+    bool full;
     NCG_DEV void emit(vec3<float> w1, vec3<float> w2, vec3<float> normal, float linear, uint32_t f1, uint32_t f2) {
         const float depth = depth_wo(w1, w2, normal);
+        if (-depth <= linear && n >= NCG_MANIFOLD_MAX) full = true;
         if (-depth <= linear && n < NCG_MANIFOLD_MAX) {
             ncg_manifold_point& p = pts[n++];
             p.world1[0] = w1.x; p.world1[1] = w1.y; p.world1[2] = w1.z;
@@ -251,7 +355,7 @@ NCG_DEV void clip(const Poly& f1, const Poly& f2, vec3<float> normal, float line
     a = a / vnorm(a);
     const vec3<float> b0 = cross(a, normal), b1 = a;
     const vec3<float> ref = f1.v[0];
-    P2 p1[4], p2[4];
+    P2 p1[NCG_POLY_MAX], p2[NCG_POLY_MAX];
     for (int k = 0; k < f1.nv; ++k) {
         const vec3<float> d = f1.v[k] - ref;
         p1[k] = P2{dot(b0, d), dot(b1, d)};
@@ -303,8 +407,32 @@ NCG_DEV bool feature_accepted(const Poly& f, uint32_t id) {
     return false;
 }
 
+// A shape's support face / feature toward a direction: Cuboid, or ConvexHull
+// with its topology (false: no topology, or a face too large for a Poly).
+NCG_DEV bool is_polyhedron(const Shape& s, uint32_t sid, const HullTopo& t) {
+    if (s.kind == NCG_CUBOID) return true;
+    return s.kind == NCG_CONVEX_HULL && t.shape != nullptr && t.shape[4 * sid + 1] > 0;
+}
+NCG_DEV bool face_toward(const ncg_batch& b, const HullTopo& t, const Shape& s, uint32_t sid, const Pose& m,
+                         vec3<float> dir, Poly& out) {
+    if (s.kind == NCG_CUBOID) {
+        support_face_toward(m, vec3<float>{s.p0, s.p1, s.p2}, dir, out);
+        return true;
+    }
+    return hull_support_face_toward(b, t, s, sid, m, dir, out);
+}
+NCG_DEV bool feature_toward(const ncg_batch& b, const HullTopo& t, const Shape& s, uint32_t sid, const Pose& m,
+                            vec3<float> dir, float cang, float sang, Poly& out) {
+    if (s.kind == NCG_CUBOID) {
+        support_feature_toward(m, vec3<float>{s.p0, s.p1, s.p2}, dir, cang, sang, out);
+        return true;
+    }
+    return hull_support_feature_toward(b, t, s, sid, m, dir, cang, sang, out);
+}
+
 __global__ void __launch_bounds__(128) k_manifold(ncg_batch b, const ncg_contact* contact, const uint8_t* has,
-                                                  ManifoldParams mp, ncg_manifold* out, uint32_t* status) {
+                                                  ManifoldParams mp, HullTopo topo, ncg_manifold* out,
+                                                  uint32_t* status) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n_pairs; i += stride) {
         ncg_manifold& o = out[i];
@@ -321,9 +449,22 @@ __global__ void __launch_bounds__(128) k_manifold(ncg_batch b, const ncg_contact
         o.normal[1] = nn.y;
         o.normal[2] = nn.z;
         Shape s1, s2;
-        const bool cub = load_shape(b, b.g1[i], s1) && load_shape(b, b.g2[i], s2) && s1.kind == NCG_CUBOID &&
-                         s2.kind == NCG_CUBOID;
-        if (!cub) {
+        const uint32_t id1 = b.g1[i], id2 = b.g2[i];
+        const bool poly = load_shape(b, id1, s1) && load_shape(b, id2, s2) && is_polyhedron(s1, id1, topo) &&
+                          is_polyhedron(s2, id2, topo);
+        const Pose m1 = load_pose(b.m1 + i), m2 = load_pose(b.m2 + i);
+        Poly f1, f2;
+        const float depth = depth_wo(w1, w2, nn);
+        bool ok = poly;
+        if (ok) {
+            if (depth > 0.0f) {
+                ok = face_toward(b, topo, s1, id1, m1, nn, f1) && face_toward(b, topo, s2, id2, m2, -nn, f2);
+            } else {
+                ok = feature_toward(b, topo, s1, id1, m1, nn, mp.cang1, mp.sang1, f1) &&
+                     feature_toward(b, topo, s2, id2, m2, -nn, mp.cang2, mp.sang2, f2);
+            }
+        }
+        if (!ok) {
             ncg_manifold_point& p = o.points[0];
             p.world1[0] = w1.x; p.world1[1] = w1.y; p.world1[2] = w1.z;
             p.world2[0] = w2.x; p.world2[1] = w2.y; p.world2[2] = w2.z;
@@ -333,20 +474,10 @@ __global__ void __launch_bounds__(128) k_manifold(ncg_batch b, const ncg_contact
             status[i] |= NCG_STATUS_NOT_POLYHEDRA;
             continue;
         }
-        const Pose m1 = load_pose(b.m1 + i), m2 = load_pose(b.m2 + i);
-        const vec3<float> h1{s1.p0, s1.p1, s1.p2}, h2{s2.p0, s2.p1, s2.p2};
-        Poly f1, f2;
-        const float depth = depth_wo(w1, w2, nn);
-        if (depth > 0.0f) {
-            support_face_toward(m1, h1, nn, f1);
-            support_face_toward(m2, h2, -nn, f2);
-        } else {
-            support_feature_toward(m1, h1, nn, mp.cang1, mp.sang1, f1);
-            support_feature_toward(m2, h2, -nn, mp.cang2, mp.sang2, f2);
-        }
         ncg_manifold_point tmp[NCG_MANIFOLD_MAX];
-        Out t{tmp, 0};
+        Out t{tmp, 0, false};
         clip(f1, f2, nn, mp.linear, t);
+        if (t.full) status[i] |= NCG_STATUS_MANIFOLD_FULL;
         if (t.n == 0) {
             ncg_manifold_point& p = tmp[t.n++];
             p.world1[0] = w1.x; p.world1[1] = w1.y; p.world1[2] = w1.z;
@@ -365,10 +496,10 @@ __global__ void __launch_bounds__(128) k_manifold(ncg_batch b, const ncg_contact
 }  // namespace
 
 int manifold_launch(const ncg_batch& b, const ncg_contact* contact, const uint8_t* has, const ManifoldParams& mp,
-                    ncg_manifold* out, uint32_t* status, int num_sms, cudaStream_t st) {
+                    const HullTopo& topo, ncg_manifold* out, uint32_t* status, int num_sms, cudaStream_t st) {
     const uint64_t need = (b.n_pairs + 127) / 128;
     const uint64_t cap = (uint64_t)num_sms * 8;
-    k_manifold<<<(unsigned)(need < cap ? need : cap), 128, 0, st>>>(b, contact, has, mp, out, status);
+    k_manifold<<<(unsigned)(need < cap ? need : cap), 128, 0, st>>>(b, contact, has, mp, topo, out, status);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_last_error(std::string("k_manifold launch: ") + cudaGetErrorString(e));

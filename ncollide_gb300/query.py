@@ -409,22 +409,26 @@ def gather_pairs(ctx: Context, objects: DeviceBatch, pairs_u32, stream=None):
     return DeviceBatch(objects.shapes, objects.hull_points, m1, g1, m2, g2, None, objects.n_shapes)
 
 
-def manifold_batch(ctx: Context, db: DeviceBatch, prediction=0.0, angular1=0.0, angular2=0.0, stream=None):
+def manifold_batch(ctx: Context, db: DeviceBatch, prediction=0.0, angular1=0.0, angular2=0.0, stream=None,
+                   topology=None):
     """ConvexPolyhedronConvexPolyhedronManifoldGenerator::generate_contacts for
     every pair.  Returns the contact query's contact / has_contact / dir and
     manifold: uint8 [N, 16 + 16 * 36] device tensor in the ncg_manifold layout
     (normal[3] f32, n u32, 16 points of world1[3], world2[3], depth, feature1,
-    feature2), and status."""
+    feature2), and status.  topology: a hulls.DeviceTopology of the batch's
+    shapes, to treat ConvexHull shapes as polyhedra (ncg_manifold_batch_hulls)."""
     n, dev = db.n_pairs, db.m1.device
     out = {"contact": _empty(n, (10,), torch.float32, dev), "has_contact": _empty(n, (), torch.uint8, dev),
            "dir": _empty(n, (3,), torch.float32, dev),
            "manifold": _empty(n, (16 + 36 * N.MANIFOLD_MAX,), torch.uint8, dev),
            "status": _empty(n, (), torch.int32, dev)}
     cb = db.c_struct()
-    N.check(ctx._L.ncg_manifold_batch(ctx.handle, ctypes.byref(cb), ctypes.c_float(prediction),
-                                      ctypes.c_float(angular1), ctypes.c_float(angular2), _ptr(out["contact"]),
-                                      _ptr(out["has_contact"]), _ptr(out["dir"]), _ptr(out["manifold"]),
-                                      _ptr(out["status"]), _stream(stream)), "ncg_manifold_batch")
+    N.check(ctx._L.ncg_manifold_batch_hulls(ctx.handle, ctypes.byref(cb),
+                                            None if topology is None else ctypes.byref(topology.struct),
+                                            ctypes.c_float(prediction), ctypes.c_float(angular1),
+                                            ctypes.c_float(angular2), _ptr(out["contact"]), _ptr(out["has_contact"]),
+                                            _ptr(out["dir"]), _ptr(out["manifold"]), _ptr(out["status"]),
+                                            _stream(stream)), "ncg_manifold_batch_hulls")
     return out
 
 

@@ -328,3 +328,17 @@ def _rotate(q, v):
     qv = q[:, :3]
     t = 2.0 * np.cross(qv, v)
     return v + q[:, 3:4] * t + np.cross(qv, t)
+
+
+def hull_pairs_pooled(n=1 << 18, seed=17, pool=4096, hull_n=(8, 256), kinds=(CUBOID, CONVEX_HULL), dmax=1.0):
+    """ConvexHull and Cuboid pairs over a pool of shared shapes (the hulls'
+    face topology is built once per pool shape): the manifold generator's
+    polyhedron pairs, poses as in mixed_convex with d ~ U[0, dmax]."""
+    rng = np.random.default_rng(seed)
+    shapes, pts = random_shapes(rng, pool, kinds=kinds, hull_n=hull_n)
+    radii = _circumradius(shapes, pts)
+    g1 = rng.integers(0, pool, n).astype(np.uint32)
+    g2 = rng.integers(0, pool, n).astype(np.uint32)
+    m1, m2 = _poses(rng, n, radii[g1], radii[g2], dmax=dmax)
+    return PairBatch(shapes, pts, m1, g1, m2, g2, scale=radii[g1] + radii[g2],
+                     meta={"workload": "hull_pairs_pooled", "n": n, "seed": seed, "pool": pool})

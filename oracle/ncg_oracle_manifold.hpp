@@ -1,8 +1,9 @@
 // ncg_oracle_manifold.hpp — TEST INFRASTRUCTURE ONLY: CPU restatement (f32)
 // of the contact-manifold step of ConvexPolyhedronConvexPolyhedronManifoldGenerator
-// for Cuboid pairs: from the GJK/EPA contact, the support features of both
-// cuboids toward the normal, their polygonal clipping, and the contacts the
-// generator pushes into the manifold.
+// for pairs of Cuboid and ConvexHull shapes: from the GJK/EPA contact, the
+// support features of both shapes toward the normal (a ConvexHull's over the
+// face topology the library builds, src/shape/convex.rs:383-546), their
+// polygonal clipping, and the contacts the generator pushes into the manifold.
 //
 // Reference (ncollide 0.33):
 //   src/pipeline/narrow_phase/contact_generator/convex_polyhedron_convex_polyhedron_manifold_generator.rs:84-176
@@ -22,6 +23,7 @@
 #include <cstdint>
 #include <cstring>
 
+#include "../include/ncg.h"
 #include "ncg_oracle.hpp"
 
 namespace ncgo {
@@ -30,6 +32,7 @@ enum { FEAT_UNKNOWN = 0, FEAT_VERTEX = 1, FEAT_EDGE = 2, FEAT_FACE = 3 };
 inline uint32_t feat(int kind, uint32_t id) { return ((uint32_t)kind << 28) | id; }
 
 constexpr int MANIFOLD_MAX = 16;
+constexpr int POLY_MAX = 32;
 
 struct ManifoldPoint {
     V3<float> w1, w2;
@@ -39,12 +42,12 @@ struct ManifoldPoint {
 
 struct PolyFeature {
     int nv = 0;
-    V3<float> v[4];
-    uint32_t vid[4];
+    V3<float> v[POLY_MAX];
+    uint32_t vid[POLY_MAX];
     int ne = 0;  // edge feature ids pushed
-    uint32_t eid[4];
+    uint32_t eid[POLY_MAX];
     int nn = 0;  // edge normals pushed
-    V3<float> en[4];
+    V3<float> en[POLY_MAX];
     bool has_normal = false;
     V3<float> normal;
     uint32_t feature = feat(FEAT_UNKNOWN, 0);
@@ -256,7 +259,7 @@ inline bool line_toi_with_plane_f(V3<float> c, V3<float> n, V3<float> o, V3<floa
 
 // ConvexPolygonalFeature::clip (convex_polygonal_feature3.rs:217-339).
 inline int clip(const PolyFeature& f1, const PolyFeature& f2, const V3<float>& normal, float linear,
-                ManifoldPoint* out, int n_out) {
+                ManifoldPoint* out, int n_out, bool* full = nullptr) {
     if (f1.nv <= 2 && f2.nv <= 2) return n_out;
     // nalgebra 0.30 orthonormal_subspace_basis of the normal: a, then a x normal first
     V3<float> a;
@@ -265,7 +268,7 @@ inline int clip(const PolyFeature& f1, const PolyFeature& f2, const V3<float>& n
     a = a / norm(a);
     const V3<float> basis0 = cross(a, normal), basis1 = a;
     const V3<float> ref = f1.v[0];
-    V2 p1[4], p2[4];
+    V2 p1[POLY_MAX], p2[POLY_MAX];
     for (int k = 0; k < f1.nv; ++k) {
         const V3<float> d = f1.v[k] - ref;
         p1[k] = V2{dot(basis0, d), dot(basis1, d)};
@@ -276,6 +279,7 @@ inline int clip(const PolyFeature& f1, const PolyFeature& f2, const V3<float>& n
     }
     auto emit = [&](V3<float> w1, V3<float> w2, uint32_t a1, uint32_t a2) {
         const float depth = depth_wo(w1, w2, normal);
+        if (-depth <= linear && n_out >= MANIFOLD_MAX && full) *full = true;
         if (-depth <= linear && n_out < MANIFOLD_MAX) out[n_out++] = ManifoldPoint{w1, w2, depth, a1, a2};
     };
     if (f2.nv > 2) {
@@ -345,6 +349,135 @@ inline int cuboid_manifold(const Iso<float>& m1, const V3<float>& h1, const Iso<
     }
     ManifoldPoint tmp[MANIFOLD_MAX];
     int n = clip(f1, f2, normal, linear, tmp, 0);
+    if (n == 0) tmp[n++] = ManifoldPoint{w1, w2, depth, f1.feature, f2.feature};
+    int k = 0;
+    for (int i = 0; i < n; ++i)
+        if (feature_accepted(f1, tmp[i].f1) && feature_accepted(f2, tmp[i].f2)) out[k++] = tmp[i];
+    return k;
+}
+
+// ---- ConvexHull as a polyhedron over its topology (ncg_hull_topology, host
+// arrays): ConvexHull::face, support_face_toward, support_feature_toward with
+// support_feature_id_toward_eps (convex.rs:383-416, 453-470, 502-546).
+struct HullView {
+    const ncg_hull_topology* t;
+    const float* pts;  // the batch's hull points, 4 floats each
+    uint32_t off, n, sid;
+    V3<float> point(uint32_t i) const {
+        const float* q = pts + 4 * ((size_t)off + i);
+        return {q[0], q[1], q[2]};
+    }
+    V3<float> face_normal(uint32_t f) const { return {t->face_normal[4 * f], t->face_normal[4 * f + 1], t->face_normal[4 * f + 2]}; }
+};
+
+inline bool hull_face(const HullView& h, uint32_t face, PolyFeature& out) {
+    out = PolyFeature();
+    const uint32_t f = h.t->shape[4 * h.sid] + face;
+    const uint32_t first = h.t->face_range[2 * f], count = h.t->face_range[2 * f + 1];
+    if (count > (uint32_t)POLY_MAX) return false;
+    for (uint32_t i = first; i < first + count; ++i) {
+        const uint32_t vid = h.t->face_vertex[i];
+        out.push(h.point(vid), feat(FEAT_VERTEX, vid));
+        out.eid[out.ne++] = feat(FEAT_EDGE, h.t->face_edge[i]);
+    }
+    out.has_normal = true;
+    out.normal = h.face_normal(f);
+    out.feature = feat(FEAT_FACE, face);
+    out.nn = 0;
+    for (int a = 0; a < out.nv; ++a) {
+        const int b = (a + 1) % out.nv;
+        const V3<float> sn = cross(out.v[b] - out.v[a], out.normal);
+        V3<float> u;
+        if (try_normalize(sn, std::numeric_limits<float>::epsilon(), &u, (float*)nullptr)) out.en[out.nn++] = u;
+        else out.en[out.nn++] = zero3<float>();
+    }
+    return true;
+}
+
+inline bool hull_support_face_toward(const HullView& h, const Iso<float>& m, const V3<float>& dir, PolyFeature& out) {
+    const V3<float> l = inverse_transform_vector(m, dir);
+    const uint32_t f0 = h.t->shape[4 * h.sid], nf = h.t->shape[4 * h.sid + 1];
+    uint32_t best = 0;
+    float max_dot = dot(h.face_normal(f0), l);
+    for (uint32_t i = 1; i < nf; ++i) {
+        const float d = dot(h.face_normal(f0 + i), l);
+        if (d > max_dot) { max_dot = d; best = i; }
+    }
+    if (!hull_face(h, best, out)) return false;
+    transform_by(out, m);
+    return true;
+}
+
+inline bool hull_support_feature_toward(const HullView& h, const Iso<float>& m, const V3<float>& dir, float cang,
+                                        float sang, PolyFeature& out) {
+    out = PolyFeature();
+    const V3<float> l = inverse_transform_vector(m, dir);
+    // point_cloud_support_point_id: the first maximum
+    uint32_t sp = 0;
+    float best = dot(h.point(0), l);
+    for (uint32_t i = 1; i < h.n; ++i) {
+        const float d = dot(h.point(i), l);
+        if (d > best) { best = d; sp = i; }
+    }
+    const uint32_t f0 = h.t->shape[4 * h.sid], e0 = h.t->shape[4 * h.sid + 2];
+    const size_t vr = 2 * ((size_t)h.off + sp);
+    const uint32_t first = h.t->vertex_range[vr], count = h.t->vertex_range[vr + 1];
+    for (uint32_t i = first; i < first + count; ++i) {
+        const uint32_t face = h.t->vertex_face[i];
+        if (dot(h.face_normal(f0 + face), l) >= cang) {
+            if (!hull_face(h, face, out)) return false;
+            transform_by(out, m);
+            return true;
+        }
+    }
+    for (uint32_t i = first; i < first + count; ++i) {
+        const uint32_t edge = h.t->vertex_edge[i];
+        const float* d4 = h.t->edge_dir + 4 * ((size_t)e0 + edge);
+        if (std::fabs(dot(V3<float>{d4[0], d4[1], d4[2]}, l)) <= sang) {
+            const uint32_t v1 = h.t->edge_vertex[2 * ((size_t)e0 + edge)], v2 = h.t->edge_vertex[2 * ((size_t)e0 + edge) + 1];
+            out.push(h.point(v1), feat(FEAT_VERTEX, v1));
+            out.push(h.point(v2), feat(FEAT_VERTEX, v2));
+            out.feature = feat(FEAT_EDGE, edge);
+            out.eid[out.ne++] = out.feature;
+            transform_by(out, m);
+            return true;
+        }
+    }
+    out.push(h.point(sp), feat(FEAT_VERTEX, sp));
+    out.feature = feat(FEAT_VERTEX, sp);
+    transform_by(out, m);
+    return true;
+}
+
+// A Cuboid (h) or ConvexHull (hv) side of a pair.
+struct PolySide {
+    bool hull;
+    V3<float> h;
+    HullView hv;
+};
+inline bool side_face_toward(const PolySide& s, const Iso<float>& m, const V3<float>& dir, PolyFeature& out) {
+    if (!s.hull) { cuboid_support_face_toward(m, s.h, dir, out); return true; }
+    return hull_support_face_toward(s.hv, m, dir, out);
+}
+inline bool side_feature_toward(const PolySide& s, const Iso<float>& m, const V3<float>& dir, float cang, float sang,
+                                PolyFeature& out) {
+    if (!s.hull) { cuboid_support_feature_toward(m, s.h, dir, cang, sang, out); return true; }
+    return hull_support_feature_toward(s.hv, m, dir, cang, sang, out);
+}
+
+// generate_contacts for a pair of polyhedra; -1 when a face does not fit a
+// PolyFeature (the caller falls back to the single contact).
+inline int poly_manifold(const Iso<float>& m1, const PolySide& a, const Iso<float>& m2, const PolySide& b, V3<float> w1,
+                         V3<float> w2, V3<float> normal, float linear, float cang1, float sang1, float cang2,
+                         float sang2, ManifoldPoint* out, bool* full) {
+    PolyFeature f1, f2;
+    const float depth = depth_wo(w1, w2, normal);
+    bool ok;
+    if (depth > 0.0f) ok = side_face_toward(a, m1, normal, f1) && side_face_toward(b, m2, -normal, f2);
+    else ok = side_feature_toward(a, m1, normal, cang1, sang1, f1) && side_feature_toward(b, m2, -normal, cang2, sang2, f2);
+    if (!ok) return -1;
+    ManifoldPoint tmp[MANIFOLD_MAX];
+    int n = clip(f1, f2, normal, linear, tmp, 0, full);
     if (n == 0) tmp[n++] = ManifoldPoint{w1, w2, depth, f1.feature, f2.feature};
     int k = 0;
     for (int i = 0; i < n; ++i)

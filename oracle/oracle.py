@@ -59,7 +59,7 @@ def lib():
         L.ncgo_pairs.argtypes = [vp, u32, vp, u64]
         L.ncgo_pairs.restype = ctypes.c_int64
         L.ncgo_manifold.argtypes = [vp, u32, u64, vp, vp, vp, vp, vp, vp, ctypes.c_float, ctypes.c_float,
-                                    ctypes.c_float, vp, vp, i32]
+                                    ctypes.c_float, vp, vp, i32, vp, u64, vp]
         L.ncgo_manifold.restype = i32
         L.ncgo_simplex_kat.restype = i32
         _lib = L
@@ -294,9 +294,12 @@ MANIFOLD_DTYPE = np.dtype([("normal", np.float32, 3), ("n", np.uint32),
                                                 ("feature2", np.uint32)]), MANIFOLD_MAX)])
 
 
-def manifold(batch, contact9, has, linear=0.0, angular1=0.0, angular2=0.0, threads=None):
+def manifold(batch, contact9, has, linear=0.0, angular1=0.0, angular2=0.0, threads=None, topology=None):
     """Manifolds (MANIFOLD_DTYPE [N]) and status from each pair's contact query
-    result: contact9 [N,9] = world1, world2, normal (float32), has [N]."""
+    result: contact9 [N,9] = world1, world2, normal (float32), has [N].
+    topology: the ConvexHull topology (an ncg_hull_topology of host arrays,
+    ncollide_gb300.hulls.HostTopology) to treat ConvexHull shapes as
+    polyhedra; None keeps their pairs to the single contact."""
     L = lib()
     n = batch.n_pairs
     out = np.zeros(n, MANIFOLD_DTYPE)
@@ -309,6 +312,8 @@ def manifold(batch, contact9, has, linear=0.0, angular1=0.0, angular2=0.0, threa
     c = np.ascontiguousarray(contact9, np.float32).reshape(n, 9)
     h = np.ascontiguousarray(has, np.uint8)
     threads = threads if threads is not None else (os.cpu_count() or 1)
+    pts = np.ascontiguousarray(batch.hull_points, np.float32)
     L.ncgo_manifold(_p(shapes), len(shapes), n, _p(m1), _p(g1), _p(m2), _p(g2), _p(c), _p(h), float(linear),
-                    float(angular1), float(angular2), _p(out), _p(status), int(threads))
+                    float(angular1), float(angular2), _p(out), _p(status), int(threads), _p(pts), pts.shape[0],
+                    None if topology is None else ctypes.addressof(topology.struct))
     return out, status

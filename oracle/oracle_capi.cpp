@@ -387,10 +387,27 @@ int64_t ncgo_pairs(const float* boxes6, uint32_t n, uint64_t* out, uint64_t cap)
 // static chunk of pairs per thread.
 int ncgo_manifold(const ncg_shape* shapes, uint32_t n_shapes, uint64_t n, const ncg_pose* m1, const uint32_t* g1,
                   const ncg_pose* m2, const uint32_t* g2, const float* contact9, const uint8_t* has, float linear,
-                  float angular1, float angular2, ncg_manifold* out, uint32_t* status, int n_threads) {
+                  float angular1, float angular2, ncg_manifold* out, uint32_t* status, int n_threads,
+                  const float* hull_points, uint64_t n_hull_points, const ncg_hull_topology* topo) {
     InF32 in{shapes, n_shapes, nullptr, 0, m1, g1, m2, g2, nullptr};
     const float cang1 = std::cos(angular1), sang1 = std::sin(angular1);
     const float cang2 = std::cos(angular2), sang2 = std::sin(angular2);
+    // a Cuboid, or a ConvexHull with a topology, is a polyhedron
+    auto side = [&](uint32_t id, PolySide& ps) -> bool {
+        if (id >= n_shapes) return false;
+        const ncg_shape& sh = shapes[id];
+        if (sh.kind == NCG_CUBOID) {
+            ps.hull = false;
+            ps.h = V3<float>{sh.p[0], sh.p[1], sh.p[2]};
+            return true;
+        }
+        if (sh.kind != NCG_CONVEX_HULL || !topo || !hull_points || id >= topo->n_shapes ||
+            (uint64_t)sh.hull_off + sh.hull_n > n_hull_points || topo->shape[4 * (size_t)id + 1] == 0)
+            return false;
+        ps.hull = true;
+        ps.hv = HullView{topo, hull_points, sh.hull_off, sh.hull_n, id};
+        return true;
+    };
     auto range = [&](uint64_t lo, uint64_t hi) {
     for (uint64_t i = lo; i < hi; ++i) {
         ncg_manifold& o = out[i];
@@ -402,21 +419,19 @@ int ncgo_manifold(const ncg_shape* shapes, uint32_t n_shapes, uint64_t n, const 
         o.normal[0] = nn.x;
         o.normal[1] = nn.y;
         o.normal[2] = nn.z;
-        const bool cub = g1[i] < n_shapes && g2[i] < n_shapes && shapes[g1[i]].kind == NCG_CUBOID &&
-                         shapes[g2[i]].kind == NCG_CUBOID;
+        PolySide a, b;
         ManifoldPoint pts[MANIFOLD_MAX];
-        int k;
-        if (cub) {
-            const ncg_shape& s1 = shapes[g1[i]];
-            const ncg_shape& s2 = shapes[g2[i]];
-            k = cuboid_manifold(pose1<float>(in, i), V3<float>{s1.p[0], s1.p[1], s1.p[2]}, pose2<float>(in, i),
-                                V3<float>{s2.p[0], s2.p[1], s2.p[2]}, w1, w2, nn, linear, cang1, sang1, cang2, sang2,
-                                pts);
-        } else {
+        int k = -1;
+        bool full = false;
+        if (side(g1[i], a) && side(g2[i], b))
+            k = poly_manifold(pose1<float>(in, i), a, pose2<float>(in, i), b, w1, w2, nn, linear, cang1, sang1, cang2,
+                              sang2, pts, &full);
+        if (k < 0) {
             pts[0] = ManifoldPoint{w1, w2, depth_wo(w1, w2, nn), 0u, 0u};
             k = 1;
             status[i] = NCG_STATUS_NOT_POLYHEDRA;
         }
+        if (full) status[i] |= NCG_STATUS_MANIFOLD_FULL;
         o.n = (uint32_t)k;
         for (int j = 0; j < k; ++j) {
             ncg_manifold_point& p = o.points[j];

@@ -15,25 +15,25 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def run(ctx, b, prediction, a1, a2):
+def run(ctx, b, prediction, a1, a2, topo=None):
     db = Q.DeviceBatch.from_host(b)
-    o = Q.manifold_batch(ctx, db, prediction, a1, a2)
+    o = Q.manifold_batch(ctx, db, prediction, a1, a2, topology=None if topo is None else topo.to_device())
     torch.cuda.synchronize()
     man = o["manifold"].cpu().numpy().view(O.MANIFOLD_DTYPE).reshape(-1)
     return o, man
 
 
-def check(ctx, b, prediction, a1, a2, tol):
-    o, man = run(ctx, b, prediction, a1, a2)
+def check(ctx, b, prediction, a1, a2, tol, topo=None):
+    o, man = run(ctx, b, prediction, a1, a2, topo)
     eps, epa_tol = (0.0, 0.0) if tol == N.TOL_REFERENCE else (-1.0, 1e-6)
     r = O.query(b, O.CONTACT, O.MIXED, param=float(np.float32(prediction)), eps=eps, epa_tol=epa_tol)
     has = o["has_contact"].cpu().numpy()
     assert np.array_equal(has, r.tag)
     c = o["contact"].cpu().numpy()
     c9 = c[:, :9].copy()
-    want, wst = O.manifold(b, c9, has, linear=prediction, angular1=a1, angular2=a2)
+    want, wst = O.manifold(b, c9, has, linear=prediction, angular1=a1, angular2=a2, topology=topo)
     st = o["status"].cpu().numpy().view(np.uint32)
-    assert np.array_equal(st & N.STATUS_NOT_POLYHEDRA, wst)
+    assert np.array_equal(st & (N.STATUS_NOT_POLYHEDRA | N.STATUS_MANIFOLD_FULL), wst)
     assert np.array_equal(man["n"], want["n"])
     assert np.array_equal(man["normal"][has == 1], want["normal"][has == 1])
     for k in range(O.MANIFOLD_MAX):
@@ -83,3 +83,20 @@ def test_manifold_bad_arguments(ctx_factory):
     for args in ((-1.0, 0.0, 0.0), (0.0, -0.1, 0.0), (0.0, 0.0, float("nan"))):
         with pytest.raises(N.NcgError):
             Q.manifold_batch(ctx, db, *args)
+
+
+@pytest.mark.parametrize("prediction,angle,dmax", [(0.0, 0.0, 1.0), (0.1, 0.05, 1.0), (0.05, 0.3, 0.6)])
+def test_manifold_convex_hull_pairs(ctx_factory, prediction, angle, dmax):
+    """ConvexHull and Cuboid pairs with the hulls' face topology
+    (ncg_manifold_batch_hulls): support faces and features of the hulls from
+    their topology, clipped against each other and against cuboid faces, bit
+    for bit the oracle's; pairs whose hull has no topology keep the single
+    contact with NCG_STATUS_NOT_POLYHEDRA on both sides."""
+    from ncollide_gb300 import hulls as H
+    ctx = ctx_factory(tolerance=N.TOL_PRECISE)
+    b = W.hull_pairs_pooled(8192, seed=44, pool=512, dmax=dmax)
+    topo = H.HostTopology(b)
+    man, want = check(ctx, b, prediction, angle, angle, N.TOL_PRECISE, topo)
+    k = b.shapes["kind"]
+    hull_pair = (k[b.g1] == W.CONVEX_HULL) | (k[b.g2] == W.CONVEX_HULL)
+    assert (man["n"][hull_pair] >= 2).sum() > 100  # polygonal contacts, not only single points
