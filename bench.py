@@ -1264,9 +1264,13 @@ def main():
     hull_pts = (sample.shapes["hull_n"][sample.g1].astype(np.float64) * (sample.shapes["kind"][sample.g1] == 5) +
                 sample.shapes["hull_n"][sample.g2].astype(np.float64) * (sample.shapes["kind"][sample.g2] == 5))
     # the thread stage's items: pairs whose hull GJK ran one thread per pair
-    # (hull_gjk_warp v >= 2 sends pairs scanning >= 2^v hull points to the warp GJK)
-    hw = tuning.get("hull_gjk_warp", 0)
+    # (hull_gjk_warp v >= 2 sends pairs scanning >= 2^v hull points to the warp
+    # GJK) and whose EPA starts there (hull_epa_warp v >= 2 starts it in the
+    # warp stage for pairs scanning >= 2^v hull points)
+    hw, ew = tuning.get("hull_gjk_warp", 0), tuning.get("hull_epa_warp", 0)
     in_thread = epa & ((hull_pts < (1 << hw)) if hw >= 2 else ((hull_pts == 0) if hw == 1 else True))
+    if ew >= 2:
+        in_thread &= hull_pts < (1 << ew)
     epa_item_bytes = 160.0 + 136.0 + 61.0 + (16.0 * hull_pts[in_thread].mean() if in_thread.any() else 0.0)
     units, unit_bytes, unit_name = {
         "classify": (batch.n_pairs, 72.0, "pair"),

@@ -34,7 +34,8 @@ extern "C" {
 
 /* 2: ncg_stats gained n_epa_thread (56 bytes); NCG_TUNE_HULL_STAGE_*, ncg_autotune,
  * ncg_ctx_get_tuning and NCG_EINTERNAL added.
- * 3: ncg_ctx_set_arithmetic (NCG_ARITH_SPLIT, NCG_ARITH_F32) added.
+ * 3: ncg_ctx_set_arithmetic (NCG_ARITH_SPLIT, NCG_ARITH_F32), NCG_TUNE_HULL_EPA_WARP
+ * (NCG_N_TUNE 7), the ConvexHull topology and ncg_manifold_batch_hulls added.
  * ncg_abi_version() returns it. */
 #define NCG_ABI_VERSION 3
 
@@ -250,6 +251,11 @@ int ncg_ctx_set_dispatch(ncg_ctx* ctx, int dispatch);
  *   NCG_TUNE_HULL_STAGE_CAP  points of that shared-memory stage per warp
  *                            (multiple of 32, 32..2048; default 1024); a hull
  *                            that does not fit is scanned from global memory
+ *   NCG_TUNE_HULL_EPA_WARP   v in 2..14: the EPA of ConvexHull pairs scanning
+ *                            >= 2^v points whose GJK ran one thread per pair
+ *                            starts in the warp stage (warp-parallel support
+ *                            scans) instead of the thread stage; 0 = never
+ *                            (default)
  * Results do not depend on any of these. */
 enum ncg_tune {
     NCG_TUNE_HULL_GJK_WARP = 0,
@@ -257,9 +263,10 @@ enum ncg_tune {
     NCG_TUNE_EPA_BLOCKS = 2,
     NCG_TUNE_L1_CARVEOUT = 3,
     NCG_TUNE_HULL_STAGE_MIN = 4,
-    NCG_TUNE_HULL_STAGE_CAP = 5
+    NCG_TUNE_HULL_STAGE_CAP = 5,
+    NCG_TUNE_HULL_EPA_WARP = 6
 };
-#define NCG_N_TUNE 6
+#define NCG_N_TUNE 7
 int ncg_ctx_set_tuning(ncg_ctx* ctx, int key, int value);
 
 /* Autotuner (no reference counterpart; the reference has no launch tuning).

@@ -42,8 +42,9 @@ EXPORTED = [
     "ncg_manifold_batch_hulls",
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
-TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT, TUNE_HULL_STAGE_MIN, TUNE_HULL_STAGE_CAP = range(6)
-N_TUNE = 6
+(TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT, TUNE_HULL_STAGE_MIN, TUNE_HULL_STAGE_CAP,
+ TUNE_HULL_EPA_WARP) = range(7)
+N_TUNE = 7
 QUERY_CONTACT, QUERY_DISTANCE, QUERY_PROXIMITY, QUERY_CLOSEST_POINTS = range(4)
 DISPATCH_SUPPORT_MAP, DISPATCH_QUERY = 0, 1
 TOI_OUT_OF_ITERATIONS, TOI_CONVERGED, TOI_FAILED, TOI_PENETRATING = range(4)

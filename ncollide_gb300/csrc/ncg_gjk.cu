@@ -197,11 +197,16 @@ NCG_DEV unsigned long long hull_warp_count(const Scratch& s, int warp_buckets) {
 
 // One thread per pair over a pair list (list 0: analytic pairs, list 1:
 // ConvexHull pairs after the warp kernel's, whose points the thread scans
-// itself); EPA starts in the thread stage, queue `epa_queue`.
+// itself); EPA starts in the thread stage, queue `epa_queue`, except for the
+// hull pairs of buckets [warp_buckets, epa_warp_buckets) (the largest hulls
+// after the warp kernel's), whose EPA starts in the warp stage (queue Q_WARP):
+// a thread-per-pair EPA scans their hulls serially at every support point.
 __global__ void __launch_bounds__(128, NCG_GJK_THREAD_MIN_BLOCKS)
-k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int warp_buckets, int epa_queue) {
+k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int warp_buckets, int epa_queue,
+             int epa_warp_buckets) {
     const unsigned long long na = *(volatile unsigned long long*)&s.ctr->n_analytic;
     const unsigned long long nw = list == 0 ? 0ull : hull_warp_count(s, warp_buckets);
+    const unsigned long long nbig = list == 0 ? 0ull : hull_warp_count(s, epa_warp_buckets) - nw;
     const unsigned long long n = list == 0 ? na : *(volatile unsigned long long*)&s.ctr->n_hull - nw;
     const uint32_t* ids = list == 0 ? s.sorted : s.sorted + na + nw;
     ThreadScan scan{reinterpret_cast<const float4*>(b.hull_points)};
@@ -216,7 +221,7 @@ k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int wa
         base = __shfl_sync(m, base, lead);
         const unsigned long long k = base + rank;
         if (k >= n) break;
-        gjk_pair(b, qp, o, s, ids[k], scan, true, acc, epa_queue);
+        gjk_pair(b, qp, o, s, ids[k], scan, true, acc, k < nbig ? Q_WARP : epa_queue);
     }
 #else
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
@@ -224,7 +229,7 @@ k_gjk_thread(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int list, int wa
     const unsigned long long rounds = (n + stride - 1) / stride;
     for (unsigned long long r = 0; r < rounds; ++r) {
         unsigned long long k = start + r * stride;
-        if (k < n) gjk_pair(b, qp, o, s, ids[k], scan, true, acc, epa_queue);
+        if (k < n) gjk_pair(b, qp, o, s, ids[k], scan, true, acc, k < nbig ? Q_WARP : epa_queue);
     }
 #endif
     warp_add(&s.ctr->gjk_iters, acc);
@@ -331,8 +336,9 @@ void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o
 }
 
 void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,
-                       int list, int warp_buckets, int epa_queue, cudaStream_t st) {
-    k_gjk_thread<<<grid, 128, 0, st>>>(b, qp, o, s, list, warp_buckets, epa_queue);
+                       int list, int warp_buckets, int epa_queue, int epa_warp_buckets, cudaStream_t st) {
+    k_gjk_thread<<<grid, 128, 0, st>>>(b, qp, o, s, list, warp_buckets, epa_queue,
+                                       epa_warp_buckets > warp_buckets ? epa_warp_buckets : warp_buckets);
 }
 
 void gjk_launch_warp(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s,

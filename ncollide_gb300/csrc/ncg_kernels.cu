@@ -145,6 +145,7 @@ struct ncg_ctx {
     int warm = NCG_WARM_NONE;
     int dispatch = NCG_DISPATCH_SUPPORT_MAP;
     int hull_gjk_warp = 0;  // GJK of ConvexHull pairs: 0 one thread per pair, 1 one warp per pair
+    int hull_epa_warp = 0;  // v >= 2: EPA of ConvexHull pairs scanning >= 2^v points starts in the warp stage
     int occ_thread = 1, occ_warp = 1, occ_ethread = 1;
     int occ_smem[2] = {1, 1};  // warps per SM of k_epa with a store of EpaTier<1> / <2> in shared memory
     int occ_global = 1;        // warps per SM of k_epa on global slabs
@@ -333,7 +334,7 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     mark(0);
     const int gjk_grid = c->num_sms * (c->gjk_blocks > 0 ? c->gjk_blocks : c->occ_thread);
     const int epa_grid = c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread);
-    sg.gjk_thread(gjk_grid, bb, qp, o, s, 0, 0, 0, st);
+    sg.gjk_thread(gjk_grid, bb, qp, o, s, 0, 0, 0, 0, st);
     mark(1);
     launches += 3;
     // With the hull points still in flight, the analytic pairs' thread-stage
@@ -356,7 +357,11 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
         sg.gjk_warp(c->num_sms * (staged ? c->occ_hstage : c->occ_warp), bb, qp, o, s, warp_buckets,
                     staged ? (uint32_t)c->hstage_min : 0u, (uint32_t)c->hstage_cap, st);
     }
-    if (warp_buckets < NB_HULL) sg.gjk_thread(gjk_grid, bb, qp, o, s, 1, warp_buckets, hull_queue, st);
+    const int epa_warp_buckets =
+        c->hull_epa_warp < 2 ? 0 : std::max(0, std::min(NB_HULL, 3 + NB_HULL - c->hull_epa_warp));
+    if (warp_buckets < NB_HULL)
+        sg.gjk_thread(gjk_grid, bb, qp, o, s, 1, warp_buckets, hull_queue, query == Q_CONTACT ? epa_warp_buckets : 0,
+                      st);
     mark(2);
     launches += (warp_buckets > 0 ? 1 : 0) + (warp_buckets < NB_HULL ? 1 : 0);
     if (query == Q_CONTACT) {
@@ -483,6 +488,10 @@ int ncg_ctx_set_tuning(ncg_ctx* c, int key, int value) {
         if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
         c->l1_carveout = value;
         return set_carveout(value) ? NCG_OK : NCG_ECUDA;
+    case NCG_TUNE_HULL_EPA_WARP:
+        if (value < 0 || value > 3 + NB_HULL - 1 || value == 1) return NCG_EINVAL;
+        c->hull_epa_warp = value;
+        return NCG_OK;
     case NCG_TUNE_HULL_STAGE_MIN:
         if (value < 0 || value > 2048) return NCG_EINVAL;
         c->hstage_min = value;
@@ -1114,8 +1123,8 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     // The array keeps the previous call's contents: reset the counters and queues' heads.
     if (!cuda_ok(cudaMemsetAsync(s.ctr, 0, sizeof(DevCounters), st), "memset noalloc counters")) return NCG_ECUDA;
     dwa::gjk_launch_sort(bb, qp, o, s, st);
-    dwa::gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 0, 0, 0, st);
-    dwa::gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 1, 0, 0, st);
+    dwa::gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 0, 0, 0, 0, st);
+    dwa::gjk_launch_thread(d.num_sms * d.lim.occ_thread, bb, qp, o, s, 1, 0, 0, 0, st);
     dwa::epa_launch_thread(d.num_sms * d.lim.occ_ethread, bb, qp, o, s, 0, st);
     // warp stages in shared memory (128, then 1280 vertices), then the one global slab
     dwa::epa_launch_warp(d.num_sms * d.lim.occ_smem[0], tier_bytes<1>(), bb, qp, o, s, caps<1>(Q_WARP_LONG, Q_WARP, 3, -1),
@@ -1237,6 +1246,7 @@ int ncg_ctx_get_tuning(ncg_ctx* c, int key, int* value) {
     case NCG_TUNE_L1_CARVEOUT: *value = c->l1_carveout; return NCG_OK;
     case NCG_TUNE_HULL_STAGE_MIN: *value = c->hstage_min; return NCG_OK;
     case NCG_TUNE_HULL_STAGE_CAP: *value = c->hstage_cap; return NCG_OK;
+    case NCG_TUNE_HULL_EPA_WARP: *value = c->hull_epa_warp; return NCG_OK;
     default: g_last_error = "unknown tuning key"; return NCG_EINVAL;
     }
 }
@@ -1272,6 +1282,7 @@ int ncg_autotune(ncg_ctx* c, const ncg_batch* b, int query, float param, int rep
     struct Cand { int key; std::vector<int> values; };
     std::vector<Cand> space = {
         {NCG_TUNE_HULL_GJK_WARP, {0, 1, 8, 9, 10, 11}},
+        {NCG_TUNE_HULL_EPA_WARP, {0, 7, 8, 9, 10}},
         {NCG_TUNE_HULL_STAGE_MIN, {0, 1, 64, 256, 512}},
         {NCG_TUNE_HULL_STAGE_CAP, {1024, 2048}},
         {NCG_TUNE_GJK_BLOCKS, {0, 1, 2, 3}},

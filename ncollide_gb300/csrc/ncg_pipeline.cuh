@@ -250,9 +250,11 @@ constexpr size_t SPILL_BYTES = (EpaSpill::bytes(EpaTier<0>::VC, EpaTier<0>::FC) 
                          cudaStream_t st);                                                                         \
     /* One thread per pair over list 0 (analytic pairs) or 1 (the ConvexHull pairs */                             \
     /* after the first `warp_buckets` hull buckets); EPA work items go to */                                      \
-    /* thread-stage queue `epa_queue`. */                                                                          \
+    /* thread-stage queue `epa_queue`, those of the hull buckets before */                                        \
+    /* `epa_warp_buckets` to the warp stage. */                                                                   \
     void gjk_launch_thread(int grid, const ncg_batch& b, const QueryParams& qp, const Outputs& o,                 \
-                           const Scratch& s, int list, int warp_buckets, int epa_queue, cudaStream_t st);         \
+                           const Scratch& s, int list, int warp_buckets, int epa_queue, int epa_warp_buckets,     \
+                           cudaStream_t st);                                                                       \
     /* One warp per pair over the ConvexHull pairs of the first `warp_buckets` */                                 \
     /* hull buckets (the largest hulls); with stage_min > 0, pairs whose hulls */                                 \
     /* hold at least stage_min points are staged in shared memory (stage_cap */                                   \

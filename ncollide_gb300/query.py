@@ -29,7 +29,8 @@ from .shapes import CONTACT_DTYPE, PairBatch
 # Launch-tuning keys of ncg_ctx_set_tuning by name.
 TUNING_KEYS = {"hull_gjk_warp": N.TUNE_HULL_GJK_WARP, "gjk_blocks": N.TUNE_GJK_BLOCKS,
                "epa_blocks": N.TUNE_EPA_BLOCKS, "l1_carveout": N.TUNE_L1_CARVEOUT,
-               "hull_stage_min": N.TUNE_HULL_STAGE_MIN, "hull_stage_cap": N.TUNE_HULL_STAGE_CAP}
+               "hull_stage_min": N.TUNE_HULL_STAGE_MIN, "hull_stage_cap": N.TUNE_HULL_STAGE_CAP,
+               "hull_epa_warp": N.TUNE_HULL_EPA_WARP}
 
 
 class Context:

@@ -290,6 +290,22 @@ def test_hull_gjk_warp_modes_bit_exact(ctx_factory, hull_warp, query, param):
         ctx.set_tuning(N.TUNE_HULL_GJK_WARP, 0)
 
 
+@pytest.mark.parametrize("epa_warp", [2, 8, 10])
+@pytest.mark.parametrize("tol", TOLS)
+def test_hull_epa_warp_start_bit_exact(ctx_factory, epa_warp, tol):
+    """EPA of ConvexHull pairs whose GJK ran one thread per pair, started in the
+    warp stage for the hulls scanning >= 2^epa_warp points (2: every hull
+    pair), gives the same contacts as starting it in the thread stage."""
+    ctx = ctx_factory(tolerance=tol)
+    ctx.set_tuning(N.TUNE_HULL_EPA_WARP, epa_warp)
+    try:
+        check_query(ctx, W.mixed_convex(8192, seed=29), O.CONTACT_QUERY, 0.0, tol)
+        check_query(ctx, W.mixed_convex(4096, seed=31, thin=True), O.CONTACT_QUERY, 0.0, tol)
+        assert ctx.stats()["flags"] == 0
+    finally:
+        ctx.set_tuning(N.TUNE_HULL_EPA_WARP, 0)
+
+
 def _with_shared_hulls(batch, every=3):
     """Every `every`-th ConvexHull pair collides the first shape with itself
     (both shapes are the same slice of the point buffer)."""
@@ -324,7 +340,8 @@ def test_hull_stage_bit_exact(ctx_factory, hull_warp, stage_min, stage_cap, quer
 def test_hull_stage_tuning_rejects_bad_values(ctx_factory):
     ctx = ctx_factory()
     for key, v in ((N.TUNE_HULL_STAGE_CAP, 0), (N.TUNE_HULL_STAGE_CAP, 100), (N.TUNE_HULL_STAGE_CAP, 4096),
-                   (N.TUNE_HULL_STAGE_MIN, -1), (N.TUNE_HULL_STAGE_MIN, 4096)):
+                   (N.TUNE_HULL_STAGE_MIN, -1), (N.TUNE_HULL_STAGE_MIN, 4096), (N.TUNE_HULL_EPA_WARP, 1),
+                   (N.TUNE_HULL_EPA_WARP, -1), (N.TUNE_HULL_EPA_WARP, 99)):
         with pytest.raises(Exception):
             ctx.set_tuning(key, v)
 
