@@ -351,11 +351,12 @@ def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32, mlp_params=
     return out
 
 
-def learned_warm_start(args, local, tolerance, dispatch, headline_db, headline_batch):
+def learned_warm_start(args, local, tolerance, dispatch, headline_db, headline_batch, headline_tuning=None):
     """Trains the warm-start network on plain-GJK labels (20 epochs, batch 8192,
     4,194,304 pairs of the mixed distribution over a pool of shared shapes),
     evaluates it on 4,194,304 held-out pairs (other seed, other pool) and times
-    the warm-started contact against plain on the headline batch."""
+    the warm-started contact against plain on the headline batch (with the
+    headline's launch tuning)."""
     import torch
     from ncollide_gb300 import _native as Nn
     from ncollide_gb300 import query as Q
@@ -426,6 +427,8 @@ def learned_warm_start(args, local, tolerance, dispatch, headline_db, headline_b
     closest = {"plain": run_closest(dhe, Nn.WARM_NONE, 3), "mlp": run_closest(dhe, Nn.WARM_MLP, 3)}
     closest["gjk_iteration_reduction"] = 1.0 - closest["mlp"]["gjk_iters_mean"] / closest["plain"]["gjk_iters_mean"]
     closest["speedup_mlp_vs_plain"] = closest["mlp"]["pairs_per_s"] / closest["plain"]["pairs_per_s"]
+    if headline_tuning:
+        ctx.apply_tuning(headline_tuning)
     head_plain, op = run(headline_db, Nn.WARM_NONE, args.steps)
     head_mlp, om = run(headline_db, Nn.WARM_MLP, args.steps)
     ctx.set_warm_start(Nn.WARM_NONE)
@@ -972,14 +975,17 @@ def sharded_report(args, ctx, rank, world, local, batch0, out0):
             "gathered_equals_single_gpu": bool(same)}
 
 
-def f32_arithmetic_report(args, local, db, batch):
+def f32_arithmetic_report(args, local, db, batch, tuning=None):
     """The headline workload in the reference's f32 arithmetic (NCG_ARITH_F32,
-    reference tolerances, query dispatch): throughput with inputs resident and
-    every pair bit for bit against the oracle's f32 instantiation."""
+    reference tolerances, query dispatch, the headline's launch tuning):
+    throughput with inputs resident and every pair bit for bit against the
+    oracle's f32 instantiation."""
     import torch
     from ncollide_gb300 import query as Q
     from oracle import oracle as O
     ctx = Q.Context(local, tolerance="reference", dispatch=args.dispatch, arithmetic="f32")
+    if tuning:
+        ctx.apply_tuning(tuning)
     for _ in range(3):
         o = Q.contact_batch(ctx, db, 0.0)
     torch.cuda.synchronize()
@@ -1238,6 +1244,28 @@ def main():
         e2e = {"value": batch.n_pairs * args.steps / dt, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "api": "ncg_contact_batch_host"}
 
+    # ---- the same call captured once as a CUDA graph (ncg_contact_graph_create)
+    # and replayed each step: the per-frame form of a simulation loop
+    graph_leg = None
+    if rank == 0:
+        gr = Q.ContactGraph(ctx, db, 0.0)
+        for _ in range(2):
+            gr.launch(stream)
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for _ in range(args.steps):
+            go = gr.launch(stream)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        g_ms = g0.elapsed_time(g1) / args.steps
+        same = all(torch.equal(go[k], out[k]) for k in ("contact", "has_contact", "status", "dir"))
+        graph_leg = {"value": batch.n_pairs / (g_ms / 1e3), "unit": "pairs/s", "ms_per_step": g_ms,
+                     "kernels_per_replay": ctx.stats()["kernels_launched"], "graph_launches_per_step": 1,
+                     "outputs_identical_to_direct_call": bool(same)}
+        gr.close()
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -1271,13 +1299,18 @@ def main():
     in_thread = epa & ((hull_pts < (1 << hw)) if hw >= 2 else ((hull_pts == 0) if hw == 1 else True))
     if ew >= 2:
         in_thread &= hull_pts < (1 << ew)
-    epa_item_bytes = 160.0 + 136.0 + 61.0 + (16.0 * hull_pts[in_thread].mean() if in_thread.any() else 0.0)
+    # the warp stage's items: those that start there, and the thread stage's
+    # overflow (a 64-vertex store holds about 60 expansion steps)
+    in_warp = (epa & ~in_thread) | (in_thread & (rs.counters[:, 1] > 60))
+
+    def item_bytes(m):
+        return 160.0 + 136.0 + 61.0 + (16.0 * hull_pts[m].mean() if m.any() else 0.0)
     units, unit_bytes, unit_name = {
         "classify": (batch.n_pairs, 72.0, "pair"),
         "gjk_thread": (batch.n_pairs, bytes_pp, "pair"), "gjk_warp": (batch.n_pairs, bytes_pp, "pair"),
-        "epa_thread": (stats["n_epa_thread"], epa_item_bytes, "EPA item"),
-        "epa_warp": (stats["n_epa_overflow"], epa_item_bytes, "EPA item"),
-        "epa_wide": (stats["n_epa_overflow"], epa_item_bytes, "EPA item")}.get(dom, (batch.n_pairs, bytes_pp, "pair"))
+        "epa_thread": (stats["n_epa_thread"], item_bytes(in_thread), "EPA item"),
+        "epa_warp": (stats["n_epa_overflow"], item_bytes(in_warp), "EPA item"),
+        "epa_wide": (stats["n_epa_overflow"], item_bytes(in_warp), "EPA item")}.get(dom, (batch.n_pairs, bytes_pp, "pair"))
     dom_s = mean_stage[dom] / 1e3
     achieved = units * unit_bytes / dom_s / 1e9
     traffic = None
@@ -1314,7 +1347,7 @@ def main():
 
     stress = cuboids = toi_rep = ray_rep = scene = manifolds = queries = arith32 = None
     if not args.no_extras:
-        arith32 = f32_arithmetic_report(args, local, db, batch)
+        arith32 = f32_arithmetic_report(args, local, db, batch, tuning)
         queries = other_queries_report(args, local, args.tolerance, db, batch)
         scene = scene_pipeline_report(args, local, args.tolerance, args.dispatch)
         manifolds = manifold_report(args, local, args.tolerance)
@@ -1324,7 +1357,7 @@ def main():
         ray_rep = ray_cast_report(args, local, args.tolerance)
     learned = mlp_params = None
     if not args.no_mlp:
-        mlp_params, learned = learned_warm_start(args, local, args.tolerance, args.dispatch, db, batch)
+        mlp_params, learned = learned_warm_start(args, local, args.tolerance, args.dispatch, db, batch, tuning)
     coherent = None
     if not args.no_coherent:
         coherent = coherent_warm_start(args, local, args.tolerance, hbm_peak, fp32_peak, mlp_params)
@@ -1338,7 +1371,7 @@ def main():
                        "seed": SEED, "parallelism": f"weak x{world}" if world > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (%.2f GB resident)" % (batch.nbytes_inputs() / 1e9),
                        "tuning": tuning, "tuning_source": tuning_source},
-            "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
+            "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches, "cuda_graph_replay": graph_leg,
             "roofline": roofline, "cpu_baseline": cpu, "parity_vs_oracle": parity, "accuracy_vs_f64": acc,
             "warm_start_coherent": coherent,
             "warm_start_learned": learned,

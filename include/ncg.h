@@ -255,7 +255,8 @@ int ncg_ctx_set_dispatch(ncg_ctx* ctx, int dispatch);
  *                            >= 2^v points whose GJK ran one thread per pair
  *                            starts in the warp stage (warp-parallel support
  *                            scans) instead of the thread stage; 0 = never
- *                            (default)
+ *                            (default: with hulls shared by many pairs the
+ *                            thread stage's scans hit L2 and it is faster)
  * Results do not depend on any of these. */
 enum ncg_tune {
     NCG_TUNE_HULL_GJK_WARP = 0,

@@ -78,8 +78,10 @@ def test_f32_init_dir_and_hull_warp_bit_exact(ctx_factory):
         check_query(ctx, W.mixed_convex(4096, seed=19), O.CONTACT, 0.0, N.TOL_REFERENCE, O.F32)
     finally:
         ctx.set_tuning(N.TUNE_HULL_GJK_WARP, 0)
-    ctx.set_tuning(N.TUNE_HULL_EPA_WARP, 2)
-    try:
-        check_query(ctx, W.mixed_convex(4096, seed=21), O.CONTACT, 0.0, N.TOL_REFERENCE, O.F32)
-    finally:
-        ctx.set_tuning(N.TUNE_HULL_EPA_WARP, 0)
+    prev = ctx.tuning()["hull_epa_warp"]
+    for ew in (0, 2):
+        ctx.set_tuning(N.TUNE_HULL_EPA_WARP, ew)
+        try:
+            check_query(ctx, W.mixed_convex(4096, seed=21), O.CONTACT, 0.0, N.TOL_REFERENCE, O.F32)
+        finally:
+            ctx.set_tuning(N.TUNE_HULL_EPA_WARP, prev)

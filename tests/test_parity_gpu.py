@@ -290,20 +290,22 @@ def test_hull_gjk_warp_modes_bit_exact(ctx_factory, hull_warp, query, param):
         ctx.set_tuning(N.TUNE_HULL_GJK_WARP, 0)
 
 
-@pytest.mark.parametrize("epa_warp", [2, 8, 10])
+@pytest.mark.parametrize("epa_warp", [0, 2, 8, 10])
 @pytest.mark.parametrize("tol", TOLS)
 def test_hull_epa_warp_start_bit_exact(ctx_factory, epa_warp, tol):
     """EPA of ConvexHull pairs whose GJK ran one thread per pair, started in the
     warp stage for the hulls scanning >= 2^epa_warp points (2: every hull
-    pair), gives the same contacts as starting it in the thread stage."""
+    pair; 0: none, every EPA starts in the thread stage), gives the oracle's
+    contacts bit for bit whichever stage it starts in."""
     ctx = ctx_factory(tolerance=tol)
+    prev = ctx.tuning()["hull_epa_warp"]
     ctx.set_tuning(N.TUNE_HULL_EPA_WARP, epa_warp)
     try:
         check_query(ctx, W.mixed_convex(8192, seed=29), O.CONTACT_QUERY, 0.0, tol)
         check_query(ctx, W.mixed_convex(4096, seed=31, thin=True), O.CONTACT_QUERY, 0.0, tol)
         assert ctx.stats()["flags"] == 0
     finally:
-        ctx.set_tuning(N.TUNE_HULL_EPA_WARP, 0)
+        ctx.set_tuning(N.TUNE_HULL_EPA_WARP, prev)
 
 
 def _with_shared_hulls(batch, every=3):
