@@ -34,8 +34,9 @@ extern "C" {
 
 /* 2: ncg_stats gained n_epa_thread (56 bytes); NCG_TUNE_HULL_STAGE_*, ncg_autotune,
  * ncg_ctx_get_tuning and NCG_EINTERNAL added.
- * 3: ncg_ctx_set_arithmetic (NCG_ARITH_SPLIT, NCG_ARITH_F32), NCG_TUNE_HULL_EPA_WARP
- * (NCG_N_TUNE 7), the ConvexHull topology and ncg_manifold_batch_hulls added.
+ * 3: ncg_ctx_set_arithmetic (NCG_ARITH_SPLIT, NCG_ARITH_F32), NCG_TUNE_HULL_EPA_WARP and
+ * NCG_TUNE_HULL_LOCALITY (NCG_N_TUNE 8), the ConvexHull topology and
+ * ncg_manifold_batch_hulls added.
  * ncg_abi_version() returns it. */
 #define NCG_ABI_VERSION 3
 
@@ -257,6 +258,12 @@ int ncg_ctx_set_dispatch(ncg_ctx* ctx, int dispatch);
  *                            scans) instead of the thread stage; 0 = never
  *                            (default: with hulls shared by many pairs the
  *                            thread stage's scans hit L2 and it is faster)
+ *   NCG_TUNE_HULL_LOCALITY   1 (default): in a batch whose pairs reference each
+ *                            shape four times or more on average, the pairs of
+ *                            each ConvexHull size bucket are grouped by the
+ *                            index range (1/4096 of the shapes) of their first
+ *                            ConvexHull, so that pairs sharing hulls run close
+ *                            together and their points stay in L2; 0: not
  * Results do not depend on any of these. */
 enum ncg_tune {
     NCG_TUNE_HULL_GJK_WARP = 0,
@@ -265,9 +272,10 @@ enum ncg_tune {
     NCG_TUNE_L1_CARVEOUT = 3,
     NCG_TUNE_HULL_STAGE_MIN = 4,
     NCG_TUNE_HULL_STAGE_CAP = 5,
-    NCG_TUNE_HULL_EPA_WARP = 6
+    NCG_TUNE_HULL_EPA_WARP = 6,
+    NCG_TUNE_HULL_LOCALITY = 7
 };
-#define NCG_N_TUNE 7
+#define NCG_N_TUNE 8
 int ncg_ctx_set_tuning(ncg_ctx* ctx, int key, int value);
 
 /* Autotuner (no reference counterpart; the reference has no launch tuning).
@@ -528,7 +536,7 @@ int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
  * allocation themselves.  This entry point needs no ncg_ctx and never calls
  * cudaMalloc, cudaFree or any allocating routine: its scratch (pair lists, EPA
  * work items and one global-memory EPA slab) is a fixed array of
- * NCG_NOALLOC_SCRATCH_BYTES (7.5 MiB) compiled into the library,
+ * NCG_NOALLOC_SCRATCH_BYTES (8.0 MiB) compiled into the library,
  * which every GPU that loads the library holds until the process exits.
  * Limit: at most NCG_NOALLOC_MAX_PAIRS pairs per call; a larger batch returns
  * NCG_EINVAL with a message in ncg_last_error().
@@ -553,7 +561,7 @@ int ncg_proximity_batch_host(ncg_ctx* ctx, const ncg_batch* batch, float margin,
  * below by their summed EPA time.
  * This entry point has no counterpart in the reference. */
 #define NCG_NOALLOC_MAX_PAIRS 32768
-#define NCG_NOALLOC_SCRATCH_BYTES 7827200
+#define NCG_NOALLOC_SCRATCH_BYTES 8420608
 int ncg_contact_batch_noalloc(const ncg_batch* batch, float prediction, int tolerance,
                               ncg_contact* out, uint8_t* has_contact, float* out_dir,
                               uint32_t* status, void* stream);

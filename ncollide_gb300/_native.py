@@ -43,8 +43,8 @@ EXPORTED = [
 ]
 MLP_N_INPUTS, MLP_N_PARAMS = 48, 23300
 (TUNE_HULL_GJK_WARP, TUNE_GJK_BLOCKS, TUNE_EPA_BLOCKS, TUNE_L1_CARVEOUT, TUNE_HULL_STAGE_MIN, TUNE_HULL_STAGE_CAP,
- TUNE_HULL_EPA_WARP) = range(7)
-N_TUNE = 7
+ TUNE_HULL_EPA_WARP, TUNE_HULL_LOCALITY) = range(8)
+N_TUNE = 8
 QUERY_CONTACT, QUERY_DISTANCE, QUERY_PROXIMITY, QUERY_CLOSEST_POINTS = range(4)
 DISPATCH_SUPPORT_MAP, DISPATCH_QUERY = 0, 1
 TOI_OUT_OF_ITERATIONS, TOI_CONVERGED, TOI_FAILED, TOI_PENETRATING = range(4)
@@ -55,7 +55,7 @@ STATUS_MANIFOLD_FULL = 1 << 10
 POLY_MAX = 32
 MANIFOLD_MAX = 16
 NOALLOC_MAX_PAIRS = 32768
-NOALLOC_SCRATCH_BYTES = 7827200
+NOALLOC_SCRATCH_BYTES = 8420608
 STAGES = ["classify", "gjk_thread", "gjk_warp", "epa_thread", "epa_warp", "epa_wide"]
 
 

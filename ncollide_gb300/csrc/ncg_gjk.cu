@@ -158,24 +158,89 @@ NCG_DEV void gjk_pair(const ncg_batch& b, const QueryParams& qp, const Outputs& 
     if (writer) write_outputs(qp, o, i, r, d, status, pack_iters(iters, 0));
 }
 
-// Validates every pair, writes the outputs of bad ones and counts the buckets.
+// The sort key of a valid pair: its analytic kind pair, or its ConvexHull
+// size bucket's locality sub-bucket.
+NCG_DEV int sort_key(int bucket, uint32_t sub) {
+    return bucket < NB_ANALYTIC ? bucket : NB_ANALYTIC + (bucket - NB_ANALYTIC) * HULL_SUB + (int)sub;
+}
+
+// Validates every pair, writes the outputs of bad ones and counts the buckets
+// and the sort keys.
 __global__ void k_classify(ncg_batch b, QueryParams qp, Outputs o, Scratch s) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int key = -1;
+    int key = -1, sk = 0;
     if (i < b.n_pairs) {
         Shape a, c;
         bool ok = load_shape(b, b.g1[i], a) && load_shape(b, b.g2[i], c);
         if (!ok) write_bad(qp, o, (uint32_t)i);
         else key = pair_bucket(a, c);
         s.bucket[i] = key < 0 ? NO_BUCKET : (uint8_t)key;
+        if (key >= NB_ANALYTIC) {
+            const uint32_t g = a.kind == NCG_CONVEX_HULL ? b.g1[i] : b.g2[i];
+            const uint32_t sub = s.loc_shift >= 32 ? 0u : min(g >> s.loc_shift, (uint32_t)HULL_SUB - 1u);
+            s.sub[i] = (uint16_t)sub;
+            sk = sort_key(key, sub);
+        } else if (key >= 0) {
+            sk = key;
+        }
     }
     (void)bucket_slot(s.ctr->bucket_n, key < 0 ? 0 : key, key >= 0);
+    (void)bucket_slot(s.ctr->key_n, sk, key >= 0);
 }
 
-// Scatters the pairs into `sorted`, bucket by bucket.
+// First slot of every sort key (one block: an exclusive scan of the counts)
+// and the lengths of the analytic and ConvexHull lists.
+__global__ void __launch_bounds__(1024) k_sort_base(Scratch s) {
+    __shared__ uint32_t part[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    constexpr int PER = (N_SORT_KEYS + 1023) / 1024;
+    uint32_t v[PER], sum = 0;
+    for (int j = 0; j < PER; ++j) {
+        const int k = t * PER + j;
+        v[j] = k < N_SORT_KEYS ? s.ctr->key_n[k] : 0u;
+        sum += v[j];
+    }
+    uint32_t incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) part[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t p = part[lane], q = p;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, q, o);
+            if (lane >= o) q += y;
+        }
+        part[lane] = q - p;  // exclusive over warps
+    }
+    __syncthreads();
+    uint32_t base = part[w] + incl - sum;
+    for (int j = 0; j < PER; ++j) {
+        const int k = t * PER + j;
+        if (k < N_SORT_KEYS) s.ctr->key_base[k] = base;
+        base += v[j];
+    }
+    if (t == 0) {
+        unsigned long long na = 0, nh = 0;
+        for (int k = 0; k < NB; ++k) (k < NB_ANALYTIC ? na : nh) += s.ctr->bucket_n[k];
+        s.ctr->n_analytic = na;
+        s.ctr->n_hull = nh;
+    }
+}
+
+// Scatters the pairs into `sorted` by sort key: analytic kind pairs, then
+// ConvexHull size buckets largest first, each by locality sub-bucket.  The
+// order inside a key is arbitrary: every pair's result depends on the pair
+// alone.
 __global__ void k_bucket(ncg_batch b, Scratch s) {
-    scatter_by_bucket(b.n_pairs, s.bucket, s.ctr->bucket_n, s.ctr->bucket_fill, s.sorted, &s.ctr->n_analytic,
-                      &s.ctr->n_hull);
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int key = i < b.n_pairs ? (int)s.bucket[i] : (int)NO_BUCKET;
+    const bool active = key != NO_BUCKET;
+    const int sk = active ? sort_key(key, key >= NB_ANALYTIC ? s.sub[i] : 0u) : 0;
+    const uint32_t slot = bucket_slot(s.ctr->key_fill, sk, active);
+    if (active) s.sorted[s.ctr->key_base[sk] + slot] = (uint32_t)i;
 }
 
 // Hull pairs in the first `warp_buckets` ConvexHull buckets (the largest
@@ -332,6 +397,7 @@ k_gjk_warp(ncg_batch b, QueryParams qp, Outputs o, Scratch s, int warp_buckets, 
 void gjk_launch_sort(const ncg_batch& b, const QueryParams& qp, const Outputs& o, const Scratch& s, cudaStream_t st) {
     const unsigned n = (unsigned)b.n_pairs;
     k_classify<<<(n + 255) / 256, 256, 0, st>>>(b, qp, o, s);
+    k_sort_base<<<1, 1024, 0, st>>>(s);
     k_bucket<<<(n + 255) / 256, 256, 0, st>>>(b, s);
 }
 

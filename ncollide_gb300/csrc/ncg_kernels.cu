@@ -146,6 +146,7 @@ struct ncg_ctx {
     int dispatch = NCG_DISPATCH_SUPPORT_MAP;
     int hull_gjk_warp = 0;  // GJK of ConvexHull pairs: 0 one thread per pair, 1 one warp per pair
     int hull_epa_warp = 0;  // v >= 2: EPA of ConvexHull pairs scanning >= 2^v points starts in the warp stage
+    int hull_locality = 1;  // 1: ConvexHull pairs sorted by hull index range when the batch reuses its shapes
     int occ_thread = 1, occ_warp = 1, occ_ethread = 1;
     int occ_smem[2] = {1, 1};  // warps per SM of k_epa with a store of EpaTier<1> / <2> in shared memory
     int occ_global = 1;        // warps per SM of k_epa on global slabs
@@ -232,6 +233,8 @@ Scratch carve_scratch(ncg_ctx* c) {
     s.ctr = (DevCounters*)p; p += CTR_SLOT;
     s.items = (EpaItem*)p; p += sizeof(EpaItem) * cap;
     s.bucket = (uint8_t*)p; p += 4 * cap;
+    s.sub = (uint16_t*)(s.bucket + 2 * cap);  // the bucket array's region holds 4 bytes per pair
+    s.loc_shift = 32;
     s.sorted = (uint32_t*)p; p += 4 * cap;
     for (int q = 0; q < N_EPA_QUEUES; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * cap; }
     s.spill_of = (uint32_t*)p; p += 4 * cap;
@@ -295,6 +298,13 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     if (!cuda_ok(cudaSetDevice(c->device), "cudaSetDevice")) return NCG_ECUDA;
     if (!ensure_scratch(c, b->n_pairs)) return NCG_ENOMEM;
     Scratch s = carve_scratch(c);
+    if (c->hull_locality && b->n_shapes > 0 && b->n_pairs >= 2 * (uint64_t)b->n_shapes) {
+        // a batch whose pairs reference each shape four times or more on
+        // average: HULL_SUB sub-buckets of consecutive shape indices
+        uint32_t shift = 0;
+        while (shift < 31 && ((b->n_shapes - 1) >> shift) >= (uint64_t)HULL_SUB) ++shift;
+        s.loc_shift = shift;
+    }
     QueryParams qp;
     qp.query = query;
     qp.dispatch = c->dispatch;
@@ -336,7 +346,7 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
     const int epa_grid = c->num_sms * (c->epa_blocks > 0 ? c->epa_blocks : c->occ_ethread);
     sg.gjk_thread(gjk_grid, bb, qp, o, s, 0, 0, 0, 0, st);
     mark(1);
-    launches += 3;
+    launches += 4;
     // With the hull points still in flight, the analytic pairs' thread-stage
     // EPA runs first (it reads no hull points); otherwise one thread-stage
     // launch serves both lists (a second launch adds a tail of ~1 ms).
@@ -375,7 +385,7 @@ int run_query(ncg_ctx* c, const ncg_batch* b, int query, float param, const Outp
         launches += 3;
     }
     if (!cuda_ok(cudaGetLastError(), "kernel launch")) return NCG_ECUDA;
-    if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st),
+    if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, CTR_HOST_BYTES, cudaMemcpyDeviceToHost, st),
                  "copy counters"))
         return NCG_ECUDA;
     c->launches = launches;
@@ -491,6 +501,10 @@ int ncg_ctx_set_tuning(ncg_ctx* c, int key, int value) {
     case NCG_TUNE_HULL_EPA_WARP:
         if (value < 0 || value > 3 + NB_HULL - 1 || value == 1) return NCG_EINVAL;
         c->hull_epa_warp = value;
+        return NCG_OK;
+    case NCG_TUNE_HULL_LOCALITY:
+        if (value < 0 || value > 1) return NCG_EINVAL;
+        c->hull_locality = value;
         return NCG_OK;
     case NCG_TUNE_HULL_STAGE_MIN:
         if (value < 0 || value > 2048) return NCG_EINVAL;
@@ -701,7 +715,7 @@ int ncg_time_of_impact_batch(ncg_ctx* c, const ncg_batch* b, const float* vel1, 
                                    &s.ctr->gjk_iters},
                         c->num_sms, st, &launches);
     if (rc != NCG_OK) return rc;
-    if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st),
+    if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, CTR_HOST_BYTES, cudaMemcpyDeviceToHost, st),
                  "copy counters"))
         return NCG_ECUDA;
     c->launches = launches;
@@ -736,7 +750,7 @@ int ncg_ray_cast_batch(ncg_ctx* c, const ncg_batch* b, const float* rays, float 
                                    &s.ctr->gjk_iters},
                         c->num_sms, st, &launches);
     if (rc != NCG_OK) return rc;
-    if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st),
+    if (!cuda_ok(cudaMemcpyAsync(c->host_ctr, s.ctr, CTR_HOST_BYTES, cudaMemcpyDeviceToHost, st),
                  "copy counters"))
         return NCG_ECUDA;
     c->launches = launches;
@@ -1012,7 +1026,8 @@ int ncg_proximity_batch_host(ncg_ctx* c, const ncg_batch* b, float margin, uint8
 // ncg_contact_batch_noalloc runs the contact pipeline on a fixed scratch array
 // in the library's device image instead of context-owned allocations.  Layout
 // of the array: counters (512 B), EPA work items, routing lists and stage
-// queues (7 x 4 B per pair), one tier-D EPA slab.
+// queues (7 x 4 B per pair), one tier-D EPA slab.  The counters hold the
+// pair sort's per-key counts (about 580 KB).
 namespace {
 constexpr uint64_t NA_MAX_PAIRS = NCG_NOALLOC_MAX_PAIRS;
 constexpr size_t NA_SLAB_BYTES =
@@ -1096,6 +1111,8 @@ extern "C" int ncg_contact_batch_noalloc(const ncg_batch* b, float prediction, i
     s.ctr = (DevCounters*)p; p += CTR_SLOT;
     s.items = (EpaItem*)p; p += NA_ITEMS_BYTES;
     s.bucket = (uint8_t*)p; p += 4 * NA_MAX_PAIRS;
+    s.sub = (uint16_t*)(s.bucket + 2 * NA_MAX_PAIRS);
+    s.loc_shift = 32;
     s.sorted = (uint32_t*)p; p += 4 * NA_MAX_PAIRS;
     for (int q = 0; q < N_EPA_QUEUES; ++q) { s.queue[q] = (uint32_t*)p; p += 4 * NA_MAX_PAIRS; }
     s.slabs[0] = p;
@@ -1247,6 +1264,7 @@ int ncg_ctx_get_tuning(ncg_ctx* c, int key, int* value) {
     case NCG_TUNE_HULL_STAGE_MIN: *value = c->hstage_min; return NCG_OK;
     case NCG_TUNE_HULL_STAGE_CAP: *value = c->hstage_cap; return NCG_OK;
     case NCG_TUNE_HULL_EPA_WARP: *value = c->hull_epa_warp; return NCG_OK;
+    case NCG_TUNE_HULL_LOCALITY: *value = c->hull_locality; return NCG_OK;
     default: g_last_error = "unknown tuning key"; return NCG_EINVAL;
     }
 }
@@ -1283,6 +1301,7 @@ int ncg_autotune(ncg_ctx* c, const ncg_batch* b, int query, float param, int rep
     std::vector<Cand> space = {
         {NCG_TUNE_HULL_GJK_WARP, {0, 1, 8, 9, 10, 11}},
         {NCG_TUNE_HULL_EPA_WARP, {0, 7, 8, 9, 10}},
+        {NCG_TUNE_HULL_LOCALITY, {1, 0}},
         {NCG_TUNE_HULL_STAGE_MIN, {0, 1, 64, 256, 512}},
         {NCG_TUNE_HULL_STAGE_CAP, {1024, 2048}},
         {NCG_TUNE_GJK_BLOCKS, {0, 1, 2, 3}},

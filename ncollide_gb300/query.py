@@ -30,7 +30,7 @@ from .shapes import CONTACT_DTYPE, PairBatch
 TUNING_KEYS = {"hull_gjk_warp": N.TUNE_HULL_GJK_WARP, "gjk_blocks": N.TUNE_GJK_BLOCKS,
                "epa_blocks": N.TUNE_EPA_BLOCKS, "l1_carveout": N.TUNE_L1_CARVEOUT,
                "hull_stage_min": N.TUNE_HULL_STAGE_MIN, "hull_stage_cap": N.TUNE_HULL_STAGE_CAP,
-               "hull_epa_warp": N.TUNE_HULL_EPA_WARP}
+               "hull_epa_warp": N.TUNE_HULL_EPA_WARP, "hull_locality": N.TUNE_HULL_LOCALITY}
 
 
 class Context:

@@ -308,6 +308,28 @@ def test_hull_epa_warp_start_bit_exact(ctx_factory, epa_warp, tol):
         ctx.set_tuning(N.TUNE_HULL_EPA_WARP, prev)
 
 
+@pytest.mark.parametrize("query,param", [(O.CONTACT, 0.0), (O.DISTANCE, 0.0), (O.PROXIMITY, 0.1),
+                                         (O.CLOSEST, 0.5)])
+def test_hull_locality_sort_bit_exact(ctx_factory, query, param):
+    """A batch that reuses its shapes (16,384 pairs over 1,024 shapes) is
+    sorted with its ConvexHull pairs grouped by hull index range
+    (NCG_TUNE_HULL_LOCALITY): the oracle's results bit for bit, and the same
+    outputs with the grouping off."""
+    ctx = ctx_factory(tolerance=N.TOL_PRECISE, dispatch="support_map")
+    prev = ctx.tuning()["hull_locality"]
+    b = W.mixed_convex_pooled(16384, seed=61, pool=1024)
+    try:
+        ctx.set_tuning(N.TUNE_HULL_LOCALITY, 1)
+        g1, _ = check_query(ctx, b, query, param, N.TOL_PRECISE)
+        ctx.set_tuning(N.TUNE_HULL_LOCALITY, 0)
+        g0, _ = check_query(ctx, b, query, param, N.TOL_PRECISE)
+        for k in g1:
+            if g1[k] is not None:
+                assert np.array_equal(g1[k].view(np.uint8), g0[k].view(np.uint8)), k
+    finally:
+        ctx.set_tuning(N.TUNE_HULL_LOCALITY, prev)
+
+
 def _with_shared_hulls(batch, every=3):
     """Every `every`-th ConvexHull pair collides the first shape with itself
     (both shapes are the same slice of the point buffer)."""
