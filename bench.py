@@ -252,6 +252,10 @@ def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32, mlp_params=
     for _ in range(frames - 1):
         poses.append((_advance_poses_t(poses[-1][0], gen), _advance_poses_t(poses[-1][1], gen)))
     ctx = Q.Context(local, tolerance=tolerance, dispatch="support_map")
+    if args.only == "coherent":  # a profiling run of this leg alone takes the command line's overrides
+        for kv in args.tune:
+            k, v = kv.split("=", 1)
+            ctx.set_tuning(k, int(v))
     dirs = torch.empty((n, 3), dtype=torch.float32, device=db.m1.device)
     g_plain = Q.ContactGraph(ctx, db, 0.0)
     g_mlp = None
