@@ -302,6 +302,8 @@ def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32, mlp_params=
                 times.append(e0.elapsed_time(e1))
                 iters.append(st["gjk_iters"] / n)
         last = {k: (None if v is None else v[:4096].cpu().numpy()) for k, v in out.items()}
+        if strategy == "plain":  # the last frame's first 65,536 pairs, for the bit-exact check
+            parity_last = {k: out[k][:65536].cpu().numpy() for k in ("contact", "has_contact", "dir", "status")}
         ms = sum(times) / len(times)
         res[strategy] = {"pairs_per_s": n / (ms / 1e3), "ms_per_frame": ms,
                          "gjk_iters_per_pair": sum(iters) / len(iters), "frames_timed": len(times),
@@ -341,6 +343,13 @@ def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32, mlp_params=
         r["hbm_frac"] = r["hbm_gbs"] / peak_hbm
         r["fp32_frac"] = r["pairs_per_s"] * flops_pp / 1e12 / peak_fp32
         both_ok &= r["classification_mismatch_vs_f64"] >= 0
+    # the plain method's last frame, bit for bit against the oracle on its
+    # first 65,536 pairs (run inside the whole batch, sorted by hull locality)
+    kp = 65536
+    pb = b0.subset(np.arange(kp))
+    pb = type(pb)(pb.shapes, pb.hull_points, poses[-1][0][:kp].cpu().numpy(), pb.g1,
+                  poses[-1][1][:kp].cpu().numpy(), pb.g2, None, pb.scale, dict(pb.meta))
+    parity = mixed_parity(pb, O.CONTACT, 0.0, tolerance, parity_last)
     g_plain.close()
     if g_mlp is not None:
         g_mlp.close()
@@ -351,7 +360,8 @@ def coherent_warm_start(args, local, tolerance, peak_hbm, peak_fp32, mlp_params=
            "speedup_previous_frame_vs_plain": res["previous_frame_dir"]["pairs_per_s"] / res["plain"]["pairs_per_s"],
            "speedup_mlp_vs_plain": (res["mlp"]["pairs_per_s"] / res["plain"]["pairs_per_s"]) if "mlp" in res else None,
            "bytes_per_pair": bytes_pp, "flops_per_pair": flops_pp,
-           "accuracy_sample": "first 4096 pairs of the last frame"}
+           "accuracy_sample": "first 4096 pairs of the last frame",
+           "parity_vs_oracle_last_frame_first_65536": parity}
     return out
 
 
